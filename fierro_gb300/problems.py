@@ -1,0 +1,168 @@
+"""Problem decks: the material / fill / boundary / control records the SGH
+solver's ``input()`` produces (Explicit-Lagrange-Kokkos/SGH_solver/input.cpp:50-653),
+as plain data, plus builders for the benchmark problems (Sedov and Noh on box
+meshes).  The same deck drives the GB300 library, the CPU oracle and the
+reference oracle build, so all three see identical inputs.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import List
+
+import numpy as np
+
+from .mesh import HexMesh, box_mesh, hex_volumes
+
+# region::vol_tag (mesh.h:824-830)
+REGION = {"global": 0, "box": 1, "cylinder": 2, "sphere": 3}
+# init_conds::init_velocity_conds (mesh.h:839-852)
+VELOCITY = {"cartesian": 0, "radial": 1, "spherical": 2, "radial_linear": 3,
+            "spherical_linear": 4, "tg_vortex": 5}
+# bdy::bdy_tag and bdy::bdy_hydro_conds (mesh.h:897-918)
+SURFACE = {"x_plane": 0, "y_plane": 1, "z_plane": 2, "cylinder": 3, "sphere": 4}
+HYDRO_BC = {"fixed": 0, "reflected": 1}
+
+
+@dataclass
+class Material:
+    """material_t (state.h:130-178) with its model state variables:
+    statev(0) = gamma, statev(1) = minimum sound speed, statev(2) = c_v."""
+    q1: float = 1.0
+    q1ex: float = 1.0
+    q2: float = 1.3333
+    q2ex: float = 0.0
+    gamma: float = 5.0 / 3.0
+    csmin: float = 1.0e-14
+    cv: float = 1.0
+
+    def state_vars(self, n: int) -> List[float]:
+        sv = [self.gamma, self.csmin, self.cv] + [0.0] * max(0, n - 3)
+        return sv[:n]
+
+
+@dataclass
+class Fill:
+    """mat_fill_t (mesh.h:858-890)."""
+    volume: str = "global"
+    mat_id: int = 0
+    x1: float = 0.0
+    x2: float = 0.0
+    y1: float = 0.0
+    y2: float = 0.0
+    z1: float = 0.0
+    z2: float = 0.0
+    radius1: float = 0.0
+    radius2: float = 0.0
+    velocity: str = "cartesian"
+    u: float = 0.0
+    v: float = 0.0
+    w: float = 0.0
+    speed: float = 0.0
+    sie: float = 0.0
+    den: float = 1.0
+
+
+@dataclass
+class Boundary:
+    """boundary_t (mesh.h:924-935)."""
+    surface: str = "x_plane"
+    value: float = 0.0
+    hydro_bc: str = "reflected"
+
+
+@dataclass
+class Params:
+    """The scalar controls of sgh_solve (mesh.h:1175-1208) with the reference
+    defaults (driver.cpp:35-62, input.cpp:73-82)."""
+    time_final: float = 1.0e16
+    dt_max: float = 1.0e-2
+    dt_min: float = 1.0e-8
+    dt_cfl: float = 0.4
+    dt_start: float = 1.0e-5
+    graphics_dt_ival: float = 1.0e8
+    graphics_cyc_ival: int = 1000000
+    cycle_stop: int = 100
+    rk_num_stages: int = 2
+    fuzz: float = 1.0e-16
+    tiny: float = 1.0e-12
+    small: float = 1.0e-8
+
+
+@dataclass
+class Problem:
+    name: str
+    mesh: HexMesh
+    materials: List[Material]
+    fills: List[Fill]
+    boundaries: List[Boundary]
+    params: Params
+    num_state_vars: int = 6
+    info: dict = field(default_factory=dict)
+
+    def state_vars(self) -> np.ndarray:
+        return np.array([m.state_vars(self.num_state_vars) for m in self.materials], dtype=np.float64)
+
+    def config_text(self) -> str:
+        """The deck in the text format read by the reference oracle's input()."""
+        p = self.params
+        out = [
+            "dt_start %r" % p.dt_start, "time_final %r" % p.time_final, "dt_max %r" % p.dt_max,
+            "dt_min %r" % p.dt_min, "dt_cfl %r" % p.dt_cfl, "graphics_dt_ival %r" % p.graphics_dt_ival,
+            "graphics_cyc_ival %d" % p.graphics_cyc_ival, "cycle_stop %d" % p.cycle_stop,
+            "rk_num_stages %d" % p.rk_num_stages, "num_state_vars %d" % self.num_state_vars,
+        ]
+        for m in self.materials:
+            sv = " ".join(repr(float(v)) for v in m.state_vars(self.num_state_vars))
+            out.append("material %r %r %r %r %s" % (m.q1, m.q1ex, m.q2, m.q2ex, sv))
+        for f in self.fills:
+            vals = [REGION[f.volume], f.mat_id, f.x1, f.x2, f.y1, f.y2, f.z1, f.z2, f.radius1,
+                    f.radius2, VELOCITY[f.velocity], f.u, f.v, f.w, f.speed, f.sie, f.den]
+            out.append("fill " + " ".join(repr(float(v)) for v in vals))
+        for b in self.boundaries:
+            out.append("bc %d %r %d" % (SURFACE[b.surface], float(b.value), HYDRO_BC[b.hydro_bc]))
+        return "\n".join(out) + "\n"
+
+
+def _planes_at_zero(kind="reflected"):
+    return [Boundary("x_plane", 0.0, kind), Boundary("y_plane", 0.0, kind), Boundary("z_plane", 0.0, kind)]
+
+
+def sedov(n: int = 12, length: float = 1.2, energy: float = 0.2467, gamma: float = 1.4,
+          cycles: int = 200, jitter: float = 0.0, seed: int = 0, permute: bool = False,
+          geo_digits: int | None = None, mesh: HexMesh | None = None, cfl: float = 0.4) -> Problem:
+    """Sedov 3D blast: rho=1, sie=1e-10, u=0 everywhere; the element at the origin
+    corner holds total energy `energy` (sie = energy / (rho V)); reflecting planes
+    x=y=z=0.  Defaults are the 12^3 Sedov case on [0,1.2]^3."""
+    if mesh is None:
+        mesh = box_mesh(n, length=length, jitter=jitter, seed=seed, permute=permute,
+                        geo_digits=geo_digits, name="sedov%d" % n)
+    h = length / n
+    # the element whose centroid lies in [0,h]^3 is the origin-corner element
+    cen = mesh.coords[mesh.nodes_in_elem].mean(axis=1)
+    origin = np.nonzero(np.all((cen >= 0.0) & (cen <= h), axis=1))[0]
+    assert origin.size == 1, "origin element not unique"
+    e0 = int(origin[0])
+    v0 = float(hex_volumes(mesh.coords, mesh.nodes_in_elem[e0:e0 + 1])[0])
+    sie0 = energy / (1.0 * v0)
+    fills = [
+        Fill("global", 0, den=1.0, sie=1.0e-10, velocity="cartesian"),
+        Fill("box", 0, x1=0.0, x2=h, y1=0.0, y2=h, z1=0.0, z2=h, den=1.0, sie=sie0, velocity="cartesian"),
+    ]
+    params = Params(time_final=1.0, dt_cfl=cfl, cycle_stop=cycles)
+    mat = Material(q1=1.0, q1ex=1.0, q2=1.3333, q2ex=0.0, gamma=gamma, csmin=1.0e-14, cv=1.0)
+    return Problem("sedov", mesh, [mat], fills, _planes_at_zero(), params,
+                   info={"origin_elem": e0, "origin_sie": sie0, "h": h})
+
+
+def noh(n: int = 32, length: float = 1.0, gamma: float = 5.0 / 3.0, speed: float = -1.0,
+        cycles: int = 500, jitter: float = 0.0, seed: int = 0, permute: bool = False,
+        geo_digits: int | None = None, mesh: HexMesh | None = None, cfl: float = 0.3) -> Problem:
+    """Noh 3D implosion: rho=1, sie=1e-10, node velocity = speed * r/|r| (zero at the
+    origin), symmetry planes x=y=z=0, MARS q1=1, q2=1.3333, q1ex=1, q2ex=0."""
+    if mesh is None:
+        mesh = box_mesh(n, length=length, jitter=jitter, seed=seed, permute=permute,
+                        geo_digits=geo_digits, name="noh%d" % n)
+    fills = [Fill("global", 0, den=1.0, sie=1.0e-10, velocity="spherical", speed=speed)]
+    params = Params(time_final=0.6, dt_cfl=cfl, cycle_stop=cycles)
+    mat = Material(q1=1.0, q1ex=1.0, q2=1.3333, q2ex=0.0, gamma=gamma, csmin=1.0e-14, cv=1.0)
+    return Problem("noh", mesh, [mat], fills, _planes_at_zero(), params)

@@ -1,0 +1,135 @@
+"""Build recipe for the oracle side (test infrastructure only).
+
+Two products, both written only under oracle/_ref/ (git-ignored):
+
+* liborc_sgh.so -- the plain-C restatement in oracle/sgh_oracle.c, compiled with
+  -ffp-contract=off so its doubles follow the reference's uncontracted evaluation.
+* fierro_ref / fierro_ref_geo / fierro_ref_fast -- the reference's own SGH solver
+  (Explicit-Lagrange-Kokkos/SGH_solver/*.cpp, unmodified) compiled with g++ -fopenmp
+  against the project-written MATAR/Kokkos stand-in oracle/compat/matar.h, with
+  input.cpp, the mesh reader and the driver replaced by the files in oracle/ref/.
+  fierro_ref_geo links the reference's own EnSight reader (read_mesh.cpp);
+  fierro_ref reads binary meshes; fierro_ref_fast is fierro_ref with the compiler's
+  default floating-point contraction (used for timing only).
+
+The reference sources are compiled where they lie when the reference tree is
+present.  They are also staged into oracle/_ref/src/ (git-ignored) so that a
+machine without the reference tree, but with a copy of this working directory,
+can rebuild the same executables for its own CPU architecture.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+STAGE = os.path.join(OUT, "src")
+REF_SGH = "/root/reference/Explicit-Lagrange-Kokkos/SGH_solver"
+
+REF_UNITS = [
+    "sgh_solve.cpp", "setup.cpp", "geometry.cpp", "momentum.cpp", "force_sgh.cpp",
+    "energy_sgh.cpp", "properties.cpp", "eos.cpp", "boundary.cpp", "time_integration.cpp",
+    "user_mat.cpp", "user_mat_init.cpp",
+]
+REF_HEADERS = ["mesh.h", "state.h"]
+REF_GEO_READER = "read_mesh.cpp"
+
+
+def _run(cmd):
+    p = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if p.returncode != 0:
+        raise RuntimeError("command failed: %s\n%s" % (" ".join(cmd), p.stdout))
+    return p.stdout
+
+
+def _newer(target, deps):
+    if not os.path.exists(target):
+        return False
+    t = os.path.getmtime(target)
+    return all(os.path.getmtime(d) <= t for d in deps if os.path.exists(d))
+
+
+def build_oracle_lib(verbose=False):
+    """Compile oracle/sgh_oracle.c into oracle/_ref/liborc_sgh.so."""
+    os.makedirs(OUT, exist_ok=True)
+    src = os.path.join(HERE, "sgh_oracle.c")
+    hdr = os.path.join(HERE, "sgh_oracle.h")
+    lib = os.path.join(OUT, "liborc_sgh.so")
+    if _newer(lib, [src, hdr, __file__]):
+        return lib
+    _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+          "-o", lib, src, "-lm"])
+    return lib
+
+
+def _source_dir():
+    if os.path.isdir(REF_SGH):
+        os.makedirs(STAGE, exist_ok=True)
+        for f in REF_UNITS + REF_HEADERS + [REF_GEO_READER]:
+            dst = os.path.join(STAGE, f)
+            srcf = os.path.join(REF_SGH, f)
+            if not os.path.exists(dst) or os.path.getmtime(dst) < os.path.getmtime(srcf):
+                shutil.copy2(srcf, dst)
+                os.chmod(dst, 0o644)
+        return REF_SGH
+    if os.path.isdir(STAGE) and all(os.path.exists(os.path.join(STAGE, f)) for f in REF_UNITS):
+        return STAGE
+    return None
+
+
+def build_reference(verbose=False, jobs=None):
+    """Compile the reference SGH solver executables.  Returns a dict of paths, or
+    None when neither the reference tree nor a staged copy is available."""
+    src_dir = _source_dir()
+    if src_dir is None:
+        return None
+    os.makedirs(os.path.join(OUT, "obj"), exist_ok=True)
+    compat = os.path.join(HERE, "compat")
+    ref_dir = os.path.join(HERE, "ref")
+    base = ["g++", "-std=c++17", "-O3", "-fopenmp", "-w", "-I", compat, "-I", src_dir]
+    variants = {"exact": ["-ffp-contract=off"], "fast": []}
+    units = [(os.path.join(src_dir, u), u) for u in REF_UNITS + [REF_GEO_READER]]
+    units += [(os.path.join(ref_dir, u), u) for u in
+              ["ref_input.cpp", "ref_harness.cpp", "ref_read_mesh_bin.cpp"]]
+    headers = [os.path.join(src_dir, h) for h in REF_HEADERS] + [os.path.join(compat, "matar.h")]
+
+    jobs_list = []
+    for var, flags in variants.items():
+        for path, name in units:
+            obj = os.path.join(OUT, "obj", "%s.%s.o" % (name, var))
+            if not _newer(obj, [path] + headers + [__file__]):
+                jobs_list.append(base + flags + ["-c", path, "-o", obj])
+    with ThreadPoolExecutor(max_workers=jobs or os.cpu_count() or 4) as ex:
+        list(ex.map(_run, jobs_list))
+
+    def objs(var, reader):
+        names = REF_UNITS + [reader, "ref_input.cpp", "ref_harness.cpp"]
+        return [os.path.join(OUT, "obj", "%s.%s.o" % (n, var)) for n in names]
+
+    out = {
+        "fierro_ref": (objs("exact", "ref_read_mesh_bin.cpp"), "exact"),
+        "fierro_ref_geo": (objs("exact", REF_GEO_READER), "exact"),
+        "fierro_ref_fast": (objs("fast", "ref_read_mesh_bin.cpp"), "fast"),
+    }
+    paths = {}
+    for exe, (ob, _) in out.items():
+        target = os.path.join(OUT, exe)
+        if not _newer(target, ob):
+            _run(["g++", "-fopenmp", "-o", target] + ob + ["-lm"])
+        paths[exe] = target
+    return paths
+
+
+def main():
+    lib = build_oracle_lib()
+    print("oracle lib:", lib)
+    paths = build_reference()
+    print("reference:", paths if paths else "unavailable (no reference sources)")
+
+
+if __name__ == "__main__":
+    sys.exit(main())

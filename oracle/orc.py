@@ -1,0 +1,253 @@
+"""Python access to the CPU oracle (test infrastructure only).
+
+* ``Oracle`` -- ctypes wrapper over oracle/_ref/liborc_sgh.so, the C restatement.
+* ``run_reference`` -- runs the reference's own SGH solver built by
+  oracle/build_ref.py on a problem deck and returns its final state.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+import struct
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = os.path.join(HERE, "_ref")
+
+ORC_NODE_COORDS, ORC_NODE_VEL, ORC_NODE_MASS, ORC_ELEM_DEN, ORC_ELEM_PRES, ORC_ELEM_STRESS, \
+    ORC_ELEM_SSPD, ORC_ELEM_SIE, ORC_ELEM_VOL, ORC_ELEM_DIV, ORC_ELEM_MASS, ORC_ELEM_MAT_ID, \
+    ORC_ELEM_STATEV, ORC_CORNER_FORCE, ORC_BDY_NODE_MASK = range(15)
+
+
+class OrcMaterial(C.Structure):
+    _fields_ = [("eos_model", C.c_int), ("strength_type", C.c_int), ("q1", C.c_double),
+                ("q1ex", C.c_double), ("q2", C.c_double), ("q2ex", C.c_double)]
+
+
+class OrcBoundary(C.Structure):
+    _fields_ = [("surface", C.c_int), ("value", C.c_double), ("hydro_bc", C.c_int)]
+
+
+class OrcFill(C.Structure):
+    _fields_ = [("volume", C.c_int), ("mat_id", C.c_int)] + \
+        [(k, C.c_double) for k in ("x1", "x2", "y1", "y2", "z1", "z2", "radius1", "radius2")] + \
+        [("velocity", C.c_int)] + [(k, C.c_double) for k in ("u", "v", "w", "speed", "sie", "den")]
+
+
+class OrcParams(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("time_final", "dt_max", "dt_min", "dt_cfl", "dt_start",
+                                          "graphics_dt_ival")] + \
+        [(k, C.c_int64) for k in ("graphics_cyc_ival", "cycle_stop", "rk_num_stages")] + \
+        [(k, C.c_double) for k in ("fuzz", "tiny", "small")]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = os.path.join(REF_DIR, "liborc_sgh.so")
+        if not os.path.exists(path):
+            from . import build_ref  # noqa: F401  (package-relative when imported as oracle.orc)
+        _lib = C.CDLL(path)
+        _lib.orc_create.restype = C.c_void_p
+        _lib.orc_create.argtypes = [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p]
+        _lib.orc_destroy.argtypes = [C.c_void_p]
+        _lib.orc_set_materials.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p]
+        _lib.orc_set_boundaries.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        _lib.orc_setup.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        _lib.orc_init_time.argtypes = [C.c_void_p, C.c_void_p]
+        _lib.orc_run_cycles.restype = C.c_int64
+        _lib.orc_run_cycles.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
+        _lib.orc_run_stages.restype = C.c_int64
+        _lib.orc_run_stages.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
+        _lib.orc_energy.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        _lib.orc_time.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 3 + [C.POINTER(C.c_int64)]
+        _lib.orc_get.restype = C.c_int64
+        _lib.orc_get.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        _lib.orc_set.restype = C.c_int64
+        _lib.orc_set.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        _lib.orc_bmatrix.argtypes = [C.c_void_p] * 4
+        _lib.orc_vol_hex.restype = C.c_double
+        _lib.orc_vol_hex.argtypes = [C.c_void_p] * 3
+    return _lib
+
+
+def make_params(p) -> OrcParams:
+    return OrcParams(p.time_final, p.dt_max, p.dt_min, p.dt_cfl, p.dt_start, p.graphics_dt_ival,
+                     p.graphics_cyc_ival, p.cycle_stop, p.rk_num_stages, p.fuzz, p.tiny, p.small)
+
+
+class Oracle:
+    """One problem instance in the C restatement."""
+
+    def __init__(self, problem, setup=True):
+        from fierro_gb300.problems import REGION, VELOCITY, SURFACE, HYDRO_BC
+        L = lib()
+        m = problem.mesh
+        self.nn, self.ne = m.num_nodes, m.num_elems
+        self._nie = np.ascontiguousarray(m.nodes_in_elem, dtype=np.int64)
+        self._xyz = np.ascontiguousarray(m.coords, dtype=np.float64)
+        self.h = L.orc_create(self.nn, self.ne, self._nie.ctypes.data, self._xyz.ctypes.data)
+        if not self.h:
+            raise ValueError("oracle rejected the mesh")
+        mats = (OrcMaterial * len(problem.materials))(
+            *[OrcMaterial(0, 0, q.q1, q.q1ex, q.q2, q.q2ex) for q in problem.materials])
+        sv = np.ascontiguousarray(problem.state_vars())
+        if L.orc_set_materials(self.h, len(problem.materials), mats, problem.num_state_vars, sv.ctypes.data):
+            raise ValueError("oracle rejected the materials")
+        nb = len(problem.boundaries)
+        bcs = (OrcBoundary * max(nb, 1))(*[OrcBoundary(SURFACE[b.surface], b.value, HYDRO_BC[b.hydro_bc])
+                                           for b in problem.boundaries])
+        if L.orc_set_boundaries(self.h, nb, bcs):
+            raise ValueError("oracle rejected the boundaries")
+        self.params = make_params(problem.params)
+        if setup:
+            fl = problem.fills
+            fills = (OrcFill * max(len(fl), 1))(*[OrcFill(
+                REGION[f.volume], f.mat_id, f.x1, f.x2, f.y1, f.y2, f.z1, f.z2, f.radius1, f.radius2,
+                VELOCITY[f.velocity], f.u, f.v, f.w, f.speed, f.sie, f.den) for f in fl])
+            if L.orc_setup(self.h, len(fl), fills):
+                raise ValueError("oracle setup failed")
+        L.orc_init_time(self.h, C.byref(self.params))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def run_cycles(self, n: int) -> int:
+        return int(lib().orc_run_cycles(self.h, C.byref(self.params), n))
+
+    def run_stages(self, n: int) -> int:
+        return int(lib().orc_run_stages(self.h, C.byref(self.params), n))
+
+    def get(self, which: int) -> np.ndarray:
+        L = lib()
+        n = L.orc_get(self.h, which, None) if which != ORC_BDY_NODE_MASK else self.nn
+        dt = np.int32 if which == ORC_BDY_NODE_MASK else (np.int64 if which == ORC_ELEM_MAT_ID else np.float64)
+        out = np.empty(n, dtype=dt)
+        L.orc_get(self.h, which, out.ctypes.data)
+        return out
+
+    def set(self, which: int, arr: np.ndarray) -> None:
+        a = np.ascontiguousarray(arr)
+        lib().orc_set(self.h, which, a.ctypes.data)
+
+    def energy(self):
+        ie, ke = C.c_double(), C.c_double()
+        lib().orc_energy(self.h, C.byref(ie), C.byref(ke))
+        return ie.value, ke.value
+
+    def time(self):
+        t, dt, gt, cyc = C.c_double(), C.c_double(), C.c_double(), C.c_int64()
+        lib().orc_time(self.h, C.byref(t), C.byref(dt), C.byref(gt), C.byref(cyc))
+        return t.value, dt.value, gt.value, cyc.value
+
+    def state(self) -> dict:
+        """The compared fields: bin-1 node coords/vel, elem den/pres/sie/sspd/vol,
+        plus both bins, node mass and corner forces."""
+        nn, ne = self.nn, self.ne
+        x = self.get(ORC_NODE_COORDS).reshape(2, nn, 3)
+        v = self.get(ORC_NODE_VEL).reshape(2, nn, 3)
+        sie = self.get(ORC_ELEM_SIE).reshape(2, ne)
+        return {
+            "coords": x[1].copy(), "vel": v[1].copy(), "coords0": x[0].copy(), "vel0": v[0].copy(),
+            "den": self.get(ORC_ELEM_DEN), "pres": self.get(ORC_ELEM_PRES), "sie": sie[1].copy(),
+            "sie0": sie[0].copy(), "sspd": self.get(ORC_ELEM_SSPD), "vol": self.get(ORC_ELEM_VOL),
+            "div": self.get(ORC_ELEM_DIV), "mass": self.get(ORC_ELEM_MASS),
+            "node_mass": self.get(ORC_NODE_MASS),
+            "corner_force": self.get(ORC_CORNER_FORCE).reshape(ne * 8, 3),
+            "time": self.time()[0],
+        }
+
+
+def bmatrix(x, y, z):
+    B = np.empty((8, 3))
+    xs, ys, zs = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z))
+    lib().orc_bmatrix(xs.ctypes.data, ys.ctypes.data, zs.ctypes.data, B.ctypes.data)
+    return B
+
+
+def vol_hex(x, y, z):
+    xs, ys, zs = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z))
+    return lib().orc_vol_hex(xs.ctypes.data, ys.ctypes.data, zs.ctypes.data)
+
+
+# --------------------------------------------------------------------------- reference
+def reference_available(kind: str = "fierro_ref") -> bool:
+    return os.path.exists(os.path.join(REF_DIR, kind))
+
+
+def read_state_dump(path: str) -> dict:
+    with open(path, "rb") as f:
+        buf = f.read()
+    assert buf[:8] == b"FSGHSTAT"
+    nn, ne = struct.unpack("<QQ", buf[8:24])
+    a = np.frombuffer(buf, dtype="<f8", offset=24)
+    pos = 0
+
+    def take(n):
+        nonlocal pos
+        out = a[pos:pos + n]
+        pos += n
+        return out.copy()
+
+    t = take(1)[0]
+    x = take(2 * nn * 3).reshape(2, nn, 3)
+    v = take(2 * nn * 3).reshape(2, nn, 3)
+    nm = take(nn)
+    den, pres, sspd = take(ne), take(ne), take(ne)
+    sie = take(2 * ne).reshape(2, ne)
+    vol, div, mass = take(ne), take(ne), take(ne)
+    cf = take(8 * ne * 3).reshape(8 * ne, 3)
+    return {"coords": x[1], "vel": v[1], "coords0": x[0], "vel0": v[0], "den": den, "pres": pres,
+            "sie": sie[1], "sie0": sie[0], "sspd": sspd, "vol": vol, "div": div, "mass": mass,
+            "node_mass": nm, "corner_force": cf, "time": t}
+
+
+def run_reference(problem, cycles: int | None = None, kind: str = "fierro_ref", threads: int | None = None,
+                  geo_path: str | None = None, workdir: str | None = None) -> dict:
+    """Run the reference executable on the deck; returns the final state plus
+    'calc_seconds' (the reference's own cycle-loop timer, sgh_solve.cpp:637-641)."""
+    from fierro_gb300.mesh import write_mesh_bin
+    import copy
+    prob = copy.deepcopy(problem)
+    if cycles is not None:
+        prob.params.cycle_stop = int(cycles)
+    exe = os.path.join(REF_DIR, kind)
+    if not os.path.exists(exe):
+        raise FileNotFoundError(exe)
+    with tempfile.TemporaryDirectory(dir=workdir) as td:
+        cfg = os.path.join(td, "deck.txt")
+        with open(cfg, "w") as f:
+            f.write(prob.config_text())
+        if geo_path is not None:
+            mesh_path = geo_path
+        else:
+            mesh_path = os.path.join(td, "mesh.bin")
+            write_mesh_bin(mesh_path, prob.mesh)
+        out = os.path.join(td, "state.bin")
+        env = dict(os.environ)
+        if threads:
+            env["OMP_NUM_THREADS"] = str(threads)
+        env.setdefault("OMP_PROC_BIND", "spread")
+        env.setdefault("OMP_PLACES", "cores")
+        p = subprocess.run([exe, cfg, mesh_path, out], stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                           text=True, env=env)
+        if p.returncode != 0:
+            raise RuntimeError("reference run failed:\n" + p.stdout[-4000:])
+        st = read_state_dump(out)
+    m = re.search(r"Calculation time in seconds:\s*([0-9.eE+-]+)", p.stdout)
+    st["calc_seconds"] = float(m.group(1)) if m else float("nan")
+    m = re.search(r"Setup time in seconds:\s*([0-9.eE+-]+)", p.stdout)
+    st["setup_seconds"] = float(m.group(1)) if m else float("nan")
+    st["stdout"] = p.stdout
+    return st
