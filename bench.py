@@ -1,0 +1,335 @@
+#!/usr/bin/env python3
+"""SGH hot-path benchmark: element-cycles/s of the plain FP64 RK2 SGH cycle on the
+256^3 perturbed Sedov problem (16.8 M hexes, interior nodes jittered by
+U(-0.1h, 0.1h) per axis from a seed, element and node ids randomly permuted,
+gamma = 1.4, origin-corner energy 0.2467, CFL 0.4).  A step is one SGH cycle
+(two RK stages) over the whole mesh.
+
+Prints one JSON line (see the design doc for every key).  Default: 1 GPU, 20 timed
+cycles after 3 warm-up cycles.  Under torchrun (N > 1) every rank advances its own
+replica (the path is run as independent replicas, no collective in the data
+path); value = all ranks' element-cycles / max-over-ranks time.
+
+  python bench.py [--steps K] [--warmup W] [--n 256] [--fp-mode exact|fma]
+  python bench.py --impl reference     # the reference's own CPU SGH solver
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SGH element-cycles/s, 256^3 perturbed Sedov, FP64 RK2"
+UNIT = "element-cycles/s"
+
+
+def parse(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256, help="elements per edge of the Sedov box")
+    ap.add_argument("--fp-mode", default="exact", choices=["exact", "fma"])
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--cpu-n", type=int, default=120, help="edge of the CPU baseline sample mesh")
+    ap.add_argument("--cpu-cycles", type=int, default=6, help="timed cycles of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args(argv)
+
+
+def workload(n: int, seed: int):
+    from fierro_gb300 import problems
+    return problems.sedov(n, length=1.2, energy=0.2467, gamma=1.4, jitter=0.1, seed=seed, permute=True,
+                          cycles=10 ** 9)
+
+
+def config_of(args, n=None):
+    n = args.n if n is None else n
+    return {"workload": "sedov3d_%d^3_jitter0.1_permuted" % n, "elements": n ** 3, "nodes": (n + 1) ** 3,
+            "gamma": 1.4, "energy": 0.2467, "cfl": 0.4, "rk_stages": 2, "seed": args.seed,
+            "parallelism": "replicas" if args.gpus > 1 else "single",
+            "l2": "inputs larger than L2 (device state > 10 GB vs 129 MB L2)"}
+
+
+# ------------------------------------------------------------------ distributed
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world <= 1:
+        return None, 0, 1
+    import torch
+    import torch.distributed as dist
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    rank = int(os.environ.get("RANK", "0"))
+    if backend == "nccl":
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dist.init_process_group(backend=backend)
+    return dist, rank, world
+
+
+def reduce_max(dist, value: float) -> float:
+    """Max over ranks (the bench's time and the replicas' slowest rank)."""
+    if dist is None:
+        return value
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        time.sleep(0.3)
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.p.terminate()
+        self.p.wait(timeout=10)
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            for k, nm in enumerate(names):
+                if r[5 + k].strip().lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ algorithmic bytes
+def alg_bytes(kind: str, nn: int, ne: int, nnz: int) -> float:
+    """Compulsory HBM bytes of one launch of each kernel: every array it touches
+    counted once (FP64 state, int32 connectivity), gathers at perfect reuse."""
+    if kind == "k_force":
+        return ne * (32 + 192 + 5 * 8 + 4 + 4 + 192) + 4 * nnz + nn * 24
+    if kind == "k_node":
+        return nn * (4 + 8 + 1 + 48 + 72) + ne * (8 * 4 + 192)
+    if kind == "k_elem":
+        return ne * (32 + 192 + 8 + 8 + 8 + 16 + 5 * 8 + 192) + nn * 72
+    return 0.0
+
+
+def measure_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ CPU reference
+def run_reference_sample(args, n: int, cycles: int, warmup: int) -> dict:
+    """The reference's own SGH solver (compiled from its sources against the
+    MATAR/Kokkos stand-in, OpenMP on every host core) on a bounded sample of the
+    workload: the same jittered, permuted Sedov problem on an n^3 mesh."""
+    from oracle import build_ref, orc
+    if not orc.reference_available("fierro_ref_fast"):
+        build_ref.build_reference()
+    if not orc.reference_available("fierro_ref_fast"):
+        raise RuntimeError("reference executable unavailable (no reference sources on this machine)")
+    prob = workload(n, args.seed)
+    cores = os.cpu_count() or 1
+    st = orc.run_reference(prob, cycles=cycles, kind="fierro_ref_fast", threads=cores, warmup=warmup)
+    secs = st["calc_seconds"]
+    return {"value": prob.mesh.num_elems * cycles / secs, "unit": UNIT, "cores": cores, "kind": "reference",
+            "sample": "%d^3 jittered permuted Sedov (%d elements), %d cycles timed by the reference's own "
+                      "cycle-loop timer after %d warm-up cycles, OMP_NUM_THREADS=%d" %
+                      (n, prob.mesh.num_elems, cycles, warmup, cores),
+            "seconds": secs}
+
+
+def reference_arm(args):
+    dist, rank, world = dist_init(args)
+    if rank != 0:
+        return
+    try:
+        ref = run_reference_sample(args, args.cpu_n, max(1, args.steps), args.warmup)
+    except Exception as exc:  # pragma: no cover - depends on the machine
+        print(json.dumps({"impl": "reference", "unavailable": str(exc).splitlines()[0]}))
+        return
+    line = {"impl": "reference", "metric": METRIC, "value": ref["value"], "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * ref["seconds"] / max(1, args.steps), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": dict(config_of(args), sample_elements=args.cpu_n ** 3),
+            "cpu_baseline": {"value": ref["value"], "unit": UNIT, "cores": ref["cores"], "kind": "reference",
+                             "sample": ref["sample"]},
+            "e2e": {"value": ref["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------------ our arm
+def ours(args):
+    import numpy as np
+    import torch
+    dist, rank, world = dist_init(args)
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    from fierro_gb300 import sgh
+
+    t0 = time.time()
+    prob = workload(args.n, args.seed)
+    st = sgh.setup(prob)
+    stream = torch.cuda.Stream()
+    mode = sgh.FP_EXACT if args.fp_mode == "exact" else sgh.FP_FMA
+    solver = sgh.SGHSolver(prob, fp_mode=mode, stream=stream.cuda_stream)
+    solver.set_state(st)
+    t_setup = time.time() - t0
+    nn, ne = prob.mesh.num_nodes, prob.mesh.num_elems
+    fp64_rate = sgh.measure_fp64_rate()
+
+    solver.run(args.warmup)
+    torch.cuda.synchronize()
+    barrier(dist)
+    clocks = ClockSampler(dev)
+    clocks.start()
+    torch.cuda.synchronize()
+    barrier(dist)
+    ran, total_ms, kms = solver.run_timed(args.steps)
+    torch.cuda.synchronize()
+    barrier(dist)
+    ck = clocks.stop()
+    if ran != args.steps:
+        raise RuntimeError("only %d of %d cycles ran (time_final reached)" % (ran, args.steps))
+    t_max = reduce_max(dist, total_ms)
+    value = ne * args.steps * world / (t_max * 1e-3)
+
+    # per-kernel device time over the timed region
+    names = solver.launch_names()
+    per = {}
+    for nm, ms in zip(names, kms):
+        per[nm] = per.get(nm, 0.0) + ms
+    launches = {nm: names.count(nm) * args.steps for nm in set(names)}
+    share = {nm: per[nm] / max(total_ms, 1e-9) for nm in per}
+    dom = max(("k_force", "k_node", "k_elem"), key=lambda k: per[k])
+    nnz = int(solver_neighbor_count(prob))
+    dom_ms = per[dom] / launches[dom]
+    ab = alg_bytes(dom, nn, ne, nnz)
+    hbm_peak, peak_kind = measure_peaks()
+    achieved = ab / (dom_ms * 1e-3) / 1e9
+    cycle_bytes = sum(alg_bytes(k, nn, ne, nnz) * names.count(k) for k in ("k_force", "k_node", "k_elem"))
+    cycle_ms = total_ms / args.steps
+
+    # end to end through the C ABI with host buffers: upload the state, run the
+    # same K cycles, download the state (copies inside the timed region)
+    e2e = None
+    if not args.no_e2e:
+        host = sgh.empty_state(nn, ne, prob.num_state_vars)
+        h2d = sum(st[k].nbytes for k in ("node_coords", "node_vel", "node_mass", "elem_den", "elem_pres",
+                                         "elem_sspd", "elem_sie", "elem_vol", "elem_mass", "elem_mat_id",
+                                         "elem_statev", "elem_div", "elem_stress"))
+        d2h = sum(host[k].nbytes for k in host if k != "elem_statev" and k != "elem_mat_id")
+        torch.cuda.synchronize()
+        barrier(dist)
+        te0 = time.perf_counter()
+        solver.set_state(st)
+        solver.run(args.steps)
+        solver.get_state(host)
+        te1 = time.perf_counter()
+        barrier(dist)
+        e_max = reduce_max(dist, te1 - te0)
+        e2e = {"value": ne * args.steps * world / e_max, "unit": UNIT,
+               "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+               "path": "fierro_sgh_set_state + fierro_sgh_run(K) + fierro_sgh_get_state, host buffers in "
+                       "the reference layouts (AoS, caller numbering), one upload and one download per "
+                       "K-cycle solve; bytes per step = per solve / K"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            cpu = run_reference_sample(args, args.cpu_n, args.cpu_cycles, 1)
+        except Exception as exc:
+            cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "reference",
+                   "sample": "unavailable: " + str(exc).splitlines()[0]}
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": dict(config_of(args), fp_mode=args.fp_mode),
+        "gpu_launches": int(solver.launches_per_cycle * args.steps),
+        "e2e": e2e,
+        "roofline": {
+            "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved / hbm_peak, "traffic": None, "peak_kind": peak_kind,
+            "alg_bytes_per_launch": ab, "avg_launch_ms": dom_ms,
+            "binding_pipe": "fp64",
+            "fp64_peak_dfma_per_s": fp64_rate,
+            "cycle_alg_bytes": cycle_bytes, "cycle_hbm_gbs": cycle_bytes / (cycle_ms * 1e-3) / 1e9,
+        },
+        "kernels": {nm: {"launches": launches[nm], "ms": per[nm], "share": share[nm]} for nm in sorted(per)},
+        "cpu_baseline": None if cpu is None else {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "clocks": ck,
+        "setup_seconds": t_setup,
+        "device_bytes": solver.device_bytes,
+    }
+    print(json.dumps(line))
+    solver.close()
+
+
+def solver_neighbor_count(prob) -> int:
+    """nnz of the element-neighbour lists of a structured box (elements sharing a
+    node): interior 26, fewer on faces, edges and corners."""
+    m = prob.mesh
+    n = round(m.num_elems ** (1.0 / 3.0))
+    if n ** 3 != m.num_elems:
+        return 26 * m.num_elems
+    per_axis_sum = (n - 2) * 3 + 2 * 2 if n >= 2 else 1  # sum over i of (#neighbours along the axis incl. self)
+    return per_axis_sum ** 3 - m.num_elems
+
+
+def main(argv=None):
+    args = parse(argv)
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,691 @@
+// C ABI of libfierro_sgh: the persistent handle (device-resident mesh and state,
+// per-parity CUDA graphs of one cycle) and the one-shot fierro_sgh_solve.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "fierro_sgh.h"
+#include "sgh_device.h"
+#include "sgh_internal.h"
+
+using namespace fierro;
+
+#define CUDA_TRY(expr)                                                                            \
+  do {                                                                                            \
+    cudaError_t err_ = (expr);                                                                    \
+    if (err_ != cudaSuccess)                                                                      \
+      return set_error(err_ == cudaErrorMemoryAllocation ? FIERRO_ENOMEM : FIERRO_ECUDA, "%s: %s", \
+                       #expr, cudaGetErrorString(err_));                                          \
+  } while (0)
+
+struct fierro_sgh {
+  HostTopo topo;
+  int64_t nn = 0, ne = 0;
+  int nmat = 0;
+  int fp_mode = FIERRO_FP_EXACT;
+  const KernelSet* ks = nullptr;
+  LoopParams lp{};
+  int rk_num_stages = 2;
+  double dt_start = 1e-5;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::vector<void*> allocations;
+  size_t dev_bytes = 0;
+  // mesh
+  int *d_nie = nullptr, *d_cin_start = nullptr, *d_cin = nullptr, *d_eie_start = nullptr, *d_eie = nullptr;
+  int* d_mat = nullptr;
+  unsigned char* d_bc = nullptr;
+  double* d_qtab = nullptr;
+  // state
+  double *d_node_mass = nullptr, *d_elem_mass = nullptr, *d_gamma = nullptr, *d_csmin = nullptr;
+  double* d_x[2][3] = {};
+  double* d_v[2][3] = {};
+  double* d_h[3] = {};
+  double *d_den = nullptr, *d_pres = nullptr, *d_sspd = nullptr, *d_vol = nullptr, *d_div = nullptr;
+  double* d_sie[2] = {};
+  double *d_bmat = nullptr, *d_force = nullptr;
+  long long* d_cfl = nullptr;
+  int ncfl = 0;
+  Ctrl* d_ctrl = nullptr;
+  double *d_energy_part = nullptr, *d_energy_out = nullptr;
+  // pinned double buffer for permuted transfers
+  double* h_stage[2] = {};
+  cudaEvent_t stage_ev[2] = {};
+  size_t stage_elems = 0;
+  // loop position
+  int base = 0;          // bin holding the state uploaded by set_state
+  long long enq_cycles = 0;  // cycles enqueued since set_state
+  int stage = 0;         // next RK stage of the current cycle (stage stepping)
+  bool has_state = false;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+};
+
+namespace {
+
+template <typename T>
+int dalloc(fierro_sgh* h, T** p, size_t count) {
+  void* q = nullptr;
+  size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+  cudaError_t err = cudaMalloc(&q, bytes);
+  if (err != cudaSuccess)
+    return set_error(FIERRO_ENOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(err));
+  h->allocations.push_back(q);
+  h->dev_bytes += bytes;
+  *p = static_cast<T*>(q);
+  return FIERRO_OK;
+}
+
+#define TRY(expr)          \
+  do {                     \
+    int rc_ = (expr);      \
+    if (rc_) return rc_;   \
+  } while (0)
+
+int upload_raw(fierro_sgh* h, void* dst, const void* src, size_t bytes) {
+  CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return FIERRO_OK;
+}
+
+// Permuted upload through the pinned double buffer: dst[i] = src[map[i]*stride + off].
+int upload_gather(fierro_sgh* h, double* dst, const double* src, const std::vector<int64_t>& map,
+                  size_t stride, size_t off, int* slot) {
+  const int64_t n = (int64_t)map.size();
+  double* st = h->h_stage[*slot];
+  CUDA_TRY(cudaEventSynchronize(h->stage_ev[*slot]));
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) st[i] = src[(size_t)map[i] * stride + off];
+  CUDA_TRY(cudaMemcpyAsync(dst, st, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(cudaEventRecord(h->stage_ev[*slot], h->stream));
+  *slot ^= 1;
+  return FIERRO_OK;
+}
+
+// Permuted download: out[map[i]*stride + off] = src[i].
+int download_scatter(fierro_sgh* h, double* out, const double* src, const std::vector<int64_t>& map,
+                     size_t stride, size_t off) {
+  const int64_t n = (int64_t)map.size();
+  double* st = h->h_stage[0];
+  CUDA_TRY(cudaMemcpyAsync(st, src, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) out[(size_t)map[i] * stride + off] = st[i];
+  return FIERRO_OK;
+}
+
+int check_status(fierro_sgh* h) {
+  Ctrl c;
+  CUDA_TRY(cudaMemcpyAsync(&c, h->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (c.status & FIERRO_STATUS_BAD_VOLUME)
+    return set_error(FIERRO_ENUMERIC, "non-positive or non-finite element volume at cycle %lld", c.cycle);
+  if (c.status & FIERRO_STATUS_BAD_STATE)
+    return set_error(FIERRO_ENUMERIC, "non-finite energy or pressure at cycle %lld", c.cycle);
+  return FIERRO_OK;
+}
+
+// Bins at a cycle boundary after `done` executed cycles: state bin and start bin.
+int bin_now(const fierro_sgh* h, long long cycles_done) { return (int)((h->base + cycles_done) & 1); }
+
+ForceArgs force_args(fierro_sgh* h, int rb) {
+  ForceArgs a{};
+  a.ne = (int)h->ne;
+  a.nie = h->d_nie;
+  a.eie_start = h->d_eie_start;
+  a.eie = h->d_eie;
+  a.mat = h->d_mat;
+  a.qtab = h->d_qtab;
+  a.bmat = h->d_bmat;
+  a.u = h->d_v[rb][0];
+  a.v = h->d_v[rb][1];
+  a.w = h->d_v[rb][2];
+  a.den = h->d_den;
+  a.pres = h->d_pres;
+  a.sspd = h->d_sspd;
+  a.vol = h->d_vol;
+  a.div = h->d_div;
+  a.force = h->d_force;
+  a.ctrl = h->d_ctrl;
+  a.fuzz = h->lp.fuzz;
+  a.small = h->lp.small;
+  return a;
+}
+
+NodeArgs node_args(fierro_sgh* h, int c, double alpha) {
+  NodeArgs a{};
+  a.nn = (int)h->nn;
+  a.ne = (int)h->ne;
+  a.cin_start = h->d_cin_start;
+  a.cin = h->d_cin;
+  a.force = h->d_force;
+  a.node_mass = h->d_node_mass;
+  a.bc_mask = h->d_bc;
+  a.u0 = h->d_v[c][0];
+  a.v0 = h->d_v[c][1];
+  a.w0 = h->d_v[c][2];
+  a.x0 = h->d_x[c][0];
+  a.y0 = h->d_x[c][1];
+  a.z0 = h->d_x[c][2];
+  a.u1 = h->d_v[c ^ 1][0];
+  a.v1 = h->d_v[c ^ 1][1];
+  a.w1 = h->d_v[c ^ 1][2];
+  a.x1 = h->d_x[c ^ 1][0];
+  a.y1 = h->d_x[c ^ 1][1];
+  a.z1 = h->d_x[c ^ 1][2];
+  a.hx = h->d_h[0];
+  a.hy = h->d_h[1];
+  a.hz = h->d_h[2];
+  a.ctrl = h->d_ctrl;
+  a.rk_alpha = alpha;
+  return a;
+}
+
+ElemArgs elem_args(fierro_sgh* h, int cur_bin, int c, double alpha) {
+  ElemArgs a{};
+  a.ne = (int)h->ne;
+  a.nie = h->d_nie;
+  a.x = h->d_x[cur_bin][0];
+  a.y = h->d_x[cur_bin][1];
+  a.z = h->d_x[cur_bin][2];
+  a.u = h->d_v[cur_bin][0];
+  a.v = h->d_v[cur_bin][1];
+  a.w = h->d_v[cur_bin][2];
+  a.hx = h->d_h[0];
+  a.hy = h->d_h[1];
+  a.hz = h->d_h[2];
+  a.force = h->d_force;
+  a.mass = h->d_elem_mass;
+  a.sie0 = h->d_sie[c];
+  a.sie1 = h->d_sie[c ^ 1];
+  a.gamma = h->d_gamma;
+  a.csmin = h->d_csmin;
+  a.den = h->d_den;
+  a.pres = h->d_pres;
+  a.sspd = h->d_sspd;
+  a.vol = h->d_vol;
+  a.div = h->d_div;
+  a.bmat = h->d_bmat;
+  a.cfl_part = h->d_cfl;
+  a.ctrl = h->d_ctrl;
+  a.rk_alpha = alpha;
+  a.dt_cfl = h->lp.dt_cfl;
+  a.fuzz = h->lp.fuzz;
+  return a;
+}
+
+double stage_alpha(const fierro_sgh* h, int s) {
+  return 1.0 / ((double)h->rk_num_stages - (double)s);  // sgh_solve.cpp:353
+}
+
+// Stage s of a cycle whose start state is in bin c.
+void enqueue_stage(fierro_sgh* h, int c, int s) {
+  const double alpha = stage_alpha(h, s);
+  const int rb = (s == 0) ? c : (c ^ 1);
+  h->ks->force(force_args(h, rb), h->stream);
+  h->ks->node(node_args(h, c, alpha), h->stream);
+  h->ks->elem(elem_args(h, c ^ 1, c, alpha), (s == h->rk_num_stages - 1) ? 1 : 0, h->stream);
+}
+
+void enqueue_dt(fierro_sgh* h) {
+  DtArgs d{};
+  d.cfl_part = h->d_cfl;
+  d.nparts = h->ncfl;
+  d.ctrl = h->d_ctrl;
+  d.lp = h->lp;
+  h->ks->dt(d, h->stream);
+}
+
+void enqueue_cycle(fierro_sgh* h, int c) {
+  enqueue_dt(h);
+  for (int s = 0; s < h->rk_num_stages; ++s) enqueue_stage(h, c, s);
+  h->ks->end(h->d_ctrl, h->lp, h->stream);
+}
+
+int build_graphs(fierro_sgh* h) {
+  for (int c = 0; c < 2; ++c) {
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_cycle(h, c);
+    CUDA_TRY(cudaStreamEndCapture(h->stream, &g));
+    cudaError_t err = cudaGraphInstantiate(&h->graph[c], g, 0);
+    cudaGraphDestroy(g);
+    if (err != cudaSuccess) return set_error(FIERRO_ECUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(err));
+  }
+  return FIERRO_OK;
+}
+
+int validate_params(const fierro_sgh_params* p) {
+  if (!p) return set_error(FIERRO_EINVAL, "params is NULL");
+  if (p->rk_num_stages < 1 || p->rk_num_stages > 8)
+    return set_error(FIERRO_EINVAL, "rk_num_stages %lld out of range 1..8", (long long)p->rk_num_stages);
+  if (p->graphics_cyc_ival < 1) return set_error(FIERRO_EINVAL, "graphics_cyc_ival must be >= 1");
+  if (!(p->dt_cfl > 0) || !(p->dt_max > 0) || !(p->dt_min > 0) || !(p->dt_start > 0))
+    return set_error(FIERRO_EINVAL, "dt_cfl, dt_max, dt_min and dt_start must be positive");
+  return FIERRO_OK;
+}
+
+}  // namespace
+
+extern "C" int fierro_sgh_destroy(fierro_sgh* h) {
+  if (!h) return FIERRO_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (int c = 0; c < 2; ++c)
+    if (h->graph[c]) cudaGraphExecDestroy(h->graph[c]);
+  for (void* p : h->allocations) cudaFree(p);
+  for (int i = 0; i < 2; ++i) {
+    if (h->h_stage[i]) cudaFreeHost(h->h_stage[i]);
+    if (h->stage_ev[i]) cudaEventDestroy(h->stage_ev[i]);
+  }
+  if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return FIERRO_OK;
+}
+
+static int create_impl(fierro_sgh* h, const fierro_mesh* mesh, const fierro_material* materials,
+                       int64_t num_materials, const fierro_boundary* boundaries, int64_t num_bcs,
+                       const fierro_sgh_params* params, int fp_mode, void* stream) {
+  TRY(validate_params(params));
+  if (fp_mode != FIERRO_FP_EXACT && fp_mode != FIERRO_FP_FMA)
+    return set_error(FIERRO_EINVAL, "fp_mode %d unknown", fp_mode);
+  if (num_materials < 1 || !materials) return set_error(FIERRO_EINVAL, "need at least one material");
+  for (int64_t m = 0; m < num_materials; ++m) {
+    if (materials[m].eos_model != 0) return set_error(FIERRO_ENOTSUP, "material %lld: only the ideal-gas EOS", (long long)m);
+    if (materials[m].strength_type != 0)
+      return set_error(FIERRO_ENOTSUP, "material %lld: strength models are outside this path", (long long)m);
+  }
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  TRY(build_topology(mesh, boundaries, num_bcs, true, &h->topo));
+  h->nn = mesh->num_nodes;
+  h->ne = mesh->num_elems;
+  h->nmat = (int)num_materials;
+  h->fp_mode = fp_mode;
+  h->ks = (fp_mode == FIERRO_FP_EXACT) ? &kernels_exact() : &kernels_fma();
+  h->lp = LoopParams{params->time_final, params->dt_max,  params->dt_min, params->dt_cfl,
+                     params->graphics_dt_ival, params->fuzz, params->small, params->graphics_cyc_ival};
+  h->rk_num_stages = (int)params->rk_num_stages;
+  h->dt_start = params->dt_start;
+  if (stream) {
+    h->stream = static_cast<cudaStream_t>(stream);
+  } else {
+    CUDA_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    h->own_stream = true;
+  }
+  const size_t nn = (size_t)h->nn, ne = (size_t)h->ne;
+  const HostTopo& t = h->topo;
+  TRY(dalloc(h, &h->d_nie, ne * 8));
+  TRY(dalloc(h, &h->d_cin_start, nn + 1));
+  TRY(dalloc(h, &h->d_cin, ne * 8));
+  TRY(dalloc(h, &h->d_eie_start, ne + 1));
+  TRY(dalloc(h, &h->d_eie, t.eie.size()));
+  TRY(dalloc(h, &h->d_mat, ne));
+  TRY(dalloc(h, &h->d_bc, nn));
+  TRY(dalloc(h, &h->d_qtab, (size_t)num_materials * 4));
+  TRY(dalloc(h, &h->d_node_mass, nn));
+  TRY(dalloc(h, &h->d_elem_mass, ne));
+  TRY(dalloc(h, &h->d_gamma, ne));
+  TRY(dalloc(h, &h->d_csmin, ne));
+  for (int b = 0; b < 2; ++b)
+    for (int d = 0; d < 3; ++d) {
+      TRY(dalloc(h, &h->d_x[b][d], nn));
+      TRY(dalloc(h, &h->d_v[b][d], nn));
+    }
+  for (int d = 0; d < 3; ++d) TRY(dalloc(h, &h->d_h[d], nn));
+  TRY(dalloc(h, &h->d_den, ne));
+  TRY(dalloc(h, &h->d_pres, ne));
+  TRY(dalloc(h, &h->d_sspd, ne));
+  TRY(dalloc(h, &h->d_vol, ne));
+  TRY(dalloc(h, &h->d_div, ne));
+  TRY(dalloc(h, &h->d_sie[0], ne));
+  TRY(dalloc(h, &h->d_sie[1], ne));
+  TRY(dalloc(h, &h->d_bmat, ne * 24));
+  TRY(dalloc(h, &h->d_force, ne * 24));
+  h->ncfl = (int)((ne + kElemBlock - 1) / kElemBlock);
+  TRY(dalloc(h, &h->d_cfl, (size_t)h->ncfl));
+  TRY(dalloc(h, &h->d_ctrl, 1));
+  TRY(dalloc(h, &h->d_energy_part, 2 * 512));
+  TRY(dalloc(h, &h->d_energy_out, 2));
+  h->stage_elems = std::max(nn, ne);
+  for (int i = 0; i < 2; ++i) {
+    CUDA_TRY(cudaHostAlloc((void**)&h->h_stage[i], sizeof(double) * h->stage_elems, cudaHostAllocDefault));
+    CUDA_TRY(cudaEventCreateWithFlags(&h->stage_ev[i], cudaEventDisableTiming));
+    CUDA_TRY(cudaEventRecord(h->stage_ev[i], h->stream));
+  }
+  TRY(upload_raw(h, h->d_nie, t.nie.data(), sizeof(int32_t) * ne * 8));
+  TRY(upload_raw(h, h->d_cin_start, t.cin_start.data(), sizeof(int32_t) * (nn + 1)));
+  TRY(upload_raw(h, h->d_cin, t.cin.data(), sizeof(int32_t) * ne * 8));
+  TRY(upload_raw(h, h->d_eie_start, t.eie_start.data(), sizeof(int32_t) * (ne + 1)));
+  if (!t.eie.empty()) TRY(upload_raw(h, h->d_eie, t.eie.data(), sizeof(int32_t) * t.eie.size()));
+  TRY(upload_raw(h, h->d_bc, t.bc_mask.data(), nn));
+  std::vector<double> q((size_t)num_materials * 4);
+  for (int64_t m = 0; m < num_materials; ++m) {
+    q[m * 4 + 0] = materials[m].q1;
+    q[m * 4 + 1] = materials[m].q1ex;
+    q[m * 4 + 2] = materials[m].q2;
+    q[m * 4 + 3] = materials[m].q2ex;
+  }
+  TRY(upload_raw(h, h->d_qtab, q.data(), sizeof(double) * q.size()));
+  CUDA_TRY(cudaMemsetAsync(h->d_ctrl, 0, sizeof(Ctrl), h->stream));
+  CUDA_TRY(cudaMemsetAsync(h->d_force, 0, sizeof(double) * ne * 24, h->stream));
+  TRY(build_graphs(h));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return FIERRO_OK;
+}
+
+extern "C" int fierro_sgh_create(const fierro_mesh* mesh, const fierro_material* materials, int64_t num_materials,
+                                 const fierro_boundary* boundaries, int64_t num_bcs,
+                                 const fierro_sgh_params* params, int fp_mode, void* stream, fierro_sgh** out) {
+  clear_error();
+  if (!out) return set_error(FIERRO_EINVAL, "out is NULL");
+  *out = nullptr;
+  fierro_sgh* h = new (std::nothrow) fierro_sgh();
+  if (!h) return set_error(FIERRO_ENOMEM, "host allocation failed");
+  int rc = create_impl(h, mesh, materials, num_materials, boundaries, num_bcs, params, fp_mode, stream);
+  if (rc) {
+    std::string msg = fierro_last_error();
+    fierro_sgh_destroy(h);
+    set_error(rc, "%s", msg.c_str());
+    return rc;
+  }
+  *out = h;
+  return FIERRO_OK;
+}
+
+static int set_state_impl(fierro_sgh* h, const fierro_sgh_state* s, double time_value, double graphics_time,
+                          double dt) {
+  if (!s || !s->node_coords || !s->node_vel || !s->node_mass || !s->elem_den || !s->elem_pres || !s->elem_sspd ||
+      !s->elem_sie || !s->elem_vol || !s->elem_mass || !s->elem_mat_id || !s->elem_statev)
+    return set_error(FIERRO_EINVAL, "set_state: required state arrays missing");
+  if (s->num_state_vars < 2) return set_error(FIERRO_EINVAL, "set_state: need num_state_vars >= 2");
+  const int64_t nn = h->nn, ne = h->ne, nsv = s->num_state_vars;
+  const HostTopo& t = h->topo;
+  if (s->elem_stress)
+    for (int64_t i = 0; i < ne * 18; ++i)
+      if (s->elem_stress[i] != 0.0)
+        return set_error(FIERRO_ENOTSUP, "set_state: non-zero stress needs a strength model (outside this path)");
+  for (int64_t e = 0; e < ne; ++e) {
+    if (s->elem_mat_id[e] >= (uint64_t)h->nmat)
+      return set_error(FIERRO_EINVAL, "set_state: element %lld material id out of range", (long long)e);
+    if (!(s->elem_vol[e] > 0.0) || !std::isfinite(s->elem_vol[e]))
+      return set_error(FIERRO_ENUMERIC, "set_state: element %lld has volume %g", (long long)e, s->elem_vol[e]);
+    if (!(s->elem_mass[e] > 0.0)) return set_error(FIERRO_EINVAL, "set_state: element %lld mass <= 0", (long long)e);
+  }
+  for (int64_t n = 0; n < nn; ++n)
+    if (!(s->node_mass[n] > 0.0)) return set_error(FIERRO_EINVAL, "set_state: node %lld mass <= 0", (long long)n);
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  int slot = 0;
+  // reference bin 1 -> device bin 0 (current), bin 0 -> device bin 1
+  for (int rb = 0; rb < 2; ++rb) {
+    const int b = rb ^ 1;
+    for (int d = 0; d < 3; ++d) {
+      TRY(upload_gather(h, h->d_x[b][d], s->node_coords + (size_t)rb * nn * 3, t.node_int2ext, 3, d, &slot));
+      TRY(upload_gather(h, h->d_v[b][d], s->node_vel + (size_t)rb * nn * 3, t.node_int2ext, 3, d, &slot));
+    }
+    TRY(upload_gather(h, h->d_sie[b], s->elem_sie + (size_t)rb * ne, t.elem_int2ext, 1, 0, &slot));
+  }
+  TRY(upload_gather(h, h->d_node_mass, s->node_mass, t.node_int2ext, 1, 0, &slot));
+  TRY(upload_gather(h, h->d_den, s->elem_den, t.elem_int2ext, 1, 0, &slot));
+  TRY(upload_gather(h, h->d_pres, s->elem_pres, t.elem_int2ext, 1, 0, &slot));
+  TRY(upload_gather(h, h->d_sspd, s->elem_sspd, t.elem_int2ext, 1, 0, &slot));
+  TRY(upload_gather(h, h->d_vol, s->elem_vol, t.elem_int2ext, 1, 0, &slot));
+  TRY(upload_gather(h, h->d_elem_mass, s->elem_mass, t.elem_int2ext, 1, 0, &slot));
+  TRY(upload_gather(h, h->d_gamma, s->elem_statev, t.elem_int2ext, (size_t)nsv, 0, &slot));
+  TRY(upload_gather(h, h->d_csmin, s->elem_statev, t.elem_int2ext, (size_t)nsv, 1, &slot));
+  std::vector<int32_t> mat((size_t)ne);
+  for (int64_t e = 0; e < ne; ++e) mat[e] = (int32_t)s->elem_mat_id[t.elem_int2ext[e]];
+  TRY(upload_raw(h, h->d_mat, mat.data(), sizeof(int32_t) * (size_t)ne));
+  if (s->elem_div) TRY(upload_gather(h, h->d_div, s->elem_div, t.elem_int2ext, 1, 0, &slot));
+  Ctrl c{};
+  c.dt = dt;
+  c.time_value = time_value;
+  c.graphics_time = graphics_time;
+  TRY(upload_raw(h, h->d_ctrl, &c, sizeof(Ctrl)));
+  h->base = 0;
+  h->enq_cycles = 0;
+  h->stage = 0;
+  // prime: corner normals, divergence and CFL partials of the uploaded state
+  h->ks->elem(elem_args(h, 0, 0, 1.0), 2, h->stream);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  h->has_state = true;
+  return FIERRO_OK;
+}
+
+extern "C" int fierro_sgh_set_state(fierro_sgh* h, const fierro_sgh_state* s) {
+  clear_error();
+  if (!h) return set_error(FIERRO_EINVAL, "handle is NULL");
+  return set_state_impl(h, s, 0.0, h->lp.graphics_dt_ival, h->dt_start);
+}
+
+static int cycles_done(fierro_sgh* h, long long* cyc) {
+  Ctrl c;
+  CUDA_TRY(cudaMemcpyAsync(&c, h->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  *cyc = c.cycle;
+  return FIERRO_OK;
+}
+
+extern "C" int fierro_sgh_get_state(fierro_sgh* h, fierro_sgh_state* s) {
+  clear_error();
+  if (!h || !s) return set_error(FIERRO_EINVAL, "handle or state is NULL");
+  if (!h->has_state) return set_error(FIERRO_EINVAL, "get_state before set_state");
+  long long cyc = 0;
+  TRY(cycles_done(h, &cyc));
+  const int c = bin_now(h, cyc);  // cycle-start bin of the current (or next) cycle
+  // at a cycle boundary reference bin 1 is bin c; mid-cycle it is bin c^1
+  const int b1 = (h->stage == 0) ? c : (c ^ 1);
+  const int b0 = b1 ^ 1;
+  const int64_t nn = h->nn, ne = h->ne;
+  const HostTopo& t = h->topo;
+  const int bins[2] = {b0, b1};
+  for (int rb = 0; rb < 2; ++rb)
+    for (int d = 0; d < 3; ++d) {
+      if (s->node_coords)
+        TRY(download_scatter(h, s->node_coords + (size_t)rb * nn * 3, h->d_x[bins[rb]][d], t.node_int2ext, 3, d));
+      if (s->node_vel)
+        TRY(download_scatter(h, s->node_vel + (size_t)rb * nn * 3, h->d_v[bins[rb]][d], t.node_int2ext, 3, d));
+    }
+  if (s->elem_sie)
+    for (int rb = 0; rb < 2; ++rb)
+      TRY(download_scatter(h, s->elem_sie + (size_t)rb * ne, h->d_sie[bins[rb]], t.elem_int2ext, 1, 0));
+  if (s->node_mass) TRY(download_scatter(h, s->node_mass, h->d_node_mass, t.node_int2ext, 1, 0));
+  if (s->elem_den) TRY(download_scatter(h, s->elem_den, h->d_den, t.elem_int2ext, 1, 0));
+  if (s->elem_pres) TRY(download_scatter(h, s->elem_pres, h->d_pres, t.elem_int2ext, 1, 0));
+  if (s->elem_sspd) TRY(download_scatter(h, s->elem_sspd, h->d_sspd, t.elem_int2ext, 1, 0));
+  if (s->elem_vol) TRY(download_scatter(h, s->elem_vol, h->d_vol, t.elem_int2ext, 1, 0));
+  if (s->elem_div) TRY(download_scatter(h, s->elem_div, h->d_div, t.elem_int2ext, 1, 0));
+  if (s->elem_mass) TRY(download_scatter(h, s->elem_mass, h->d_elem_mass, t.elem_int2ext, 1, 0));
+  if (s->elem_stress) std::memset(s->elem_stress, 0, sizeof(double) * (size_t)ne * 18);
+  if (s->corner_force) {
+    // device [lid*3+dim][e] -> reference [(E*8+lid)*3+dim]
+    for (int r = 0; r < 24; ++r)
+      TRY(download_scatter(h, s->corner_force, h->d_force + (size_t)r * ne, t.elem_int2ext, 24, (size_t)r));
+  }
+  return FIERRO_OK;
+}
+
+extern "C" int fierro_sgh_enqueue_cycles(fierro_sgh* h, int64_t cycles) {
+  clear_error();
+  if (!h || !h->has_state) return set_error(FIERRO_EINVAL, "enqueue before set_state");
+  if (h->stage != 0) return set_error(FIERRO_EINVAL, "a cycle is partly run; finish it with run_stages");
+  for (int64_t i = 0; i < cycles; ++i) {
+    const int c = (int)((h->base + h->enq_cycles) & 1);
+    CUDA_TRY(cudaGraphLaunch(h->graph[c], h->stream));
+    h->enq_cycles++;
+  }
+  return FIERRO_OK;
+}
+
+extern "C" int fierro_sgh_synchronize(fierro_sgh* h) {
+  clear_error();
+  if (!h) return set_error(FIERRO_EINVAL, "handle is NULL");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return check_status(h);
+}
+
+// Re-align the host's cycle parity with the device after a run that may have
+// stopped early (stopped cycles do nothing, so the state stays put).
+static int realign(fierro_sgh* h) {
+  long long cyc = 0;
+  TRY(cycles_done(h, &cyc));
+  h->enq_cycles = cyc;
+  return FIERRO_OK;
+}
+
+extern "C" int fierro_sgh_run(fierro_sgh* h, int64_t cycles, int64_t* cycles_run) {
+  clear_error();
+  if (!h || !h->has_state) return set_error(FIERRO_EINVAL, "run before set_state");
+  long long before = 0;
+  TRY(realign(h));
+  before = h->enq_cycles;
+  TRY(fierro_sgh_enqueue_cycles(h, cycles));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  TRY(realign(h));
+  if (cycles_run) *cycles_run = h->enq_cycles - before;
+  return check_status(h);
+}
+
+extern "C" int fierro_sgh_run_stages(fierro_sgh* h, int64_t stages) {
+  clear_error();
+  if (!h || !h->has_state) return set_error(FIERRO_EINVAL, "run_stages before set_state");
+  TRY(realign(h));
+  for (int64_t i = 0; i < stages; ++i) {
+    const int c = (int)((h->base + h->enq_cycles) & 1);
+    if (h->stage == 0) enqueue_dt(h);
+    enqueue_stage(h, c, h->stage);
+    h->stage++;
+    if (h->stage == h->rk_num_stages) {
+      h->ks->end(h->d_ctrl, h->lp, h->stream);
+      h->stage = 0;
+      h->enq_cycles++;
+    }
+  }
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (h->stage == 0) TRY(realign(h));
+  return check_status(h);
+}
+
+extern "C" int fierro_sgh_run_timed(fierro_sgh* h, int64_t cycles, float* kernel_ms, float* total_ms,
+                                    int64_t* cycles_run) {
+  clear_error();
+  if (!h || !h->has_state) return set_error(FIERRO_EINVAL, "run before set_state");
+  if (h->stage != 0) return set_error(FIERRO_EINVAL, "a cycle is partly run; finish it with run_stages");
+  TRY(realign(h));
+  const long long before = h->enq_cycles;
+  const int L = (int)fierro_sgh_launches_per_cycle(h);
+  const size_t nev = (size_t)cycles * (size_t)L + 1;
+  std::vector<cudaEvent_t> ev(nev, nullptr);
+  for (auto& e : ev) CUDA_TRY(cudaEventCreate(&e));
+  size_t k = 0;
+  CUDA_TRY(cudaEventRecord(ev[k++], h->stream));
+  for (int64_t i = 0; i < cycles; ++i) {
+    const int c = (int)((h->base + h->enq_cycles) & 1);
+    enqueue_dt(h);
+    CUDA_TRY(cudaEventRecord(ev[k++], h->stream));
+    for (int s = 0; s < h->rk_num_stages; ++s) {
+      const double alpha = stage_alpha(h, s);
+      const int rb = (s == 0) ? c : (c ^ 1);
+      h->ks->force(force_args(h, rb), h->stream);
+      CUDA_TRY(cudaEventRecord(ev[k++], h->stream));
+      h->ks->node(node_args(h, c, alpha), h->stream);
+      CUDA_TRY(cudaEventRecord(ev[k++], h->stream));
+      h->ks->elem(elem_args(h, c ^ 1, c, alpha), (s == h->rk_num_stages - 1) ? 1 : 0, h->stream);
+      CUDA_TRY(cudaEventRecord(ev[k++], h->stream));
+    }
+    h->ks->end(h->d_ctrl, h->lp, h->stream);
+    CUDA_TRY(cudaEventRecord(ev[k++], h->stream));
+    h->enq_cycles++;
+  }
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaEventSynchronize(ev[k - 1]));
+  if (kernel_ms)
+    for (int i = 0; i < L; ++i) kernel_ms[i] = 0.0f;
+  for (size_t j = 1; j < k; ++j) {
+    float ms = 0.0f;
+    CUDA_TRY(cudaEventElapsedTime(&ms, ev[j - 1], ev[j]));
+    if (kernel_ms) kernel_ms[(j - 1) % (size_t)L] += ms;
+  }
+  if (total_ms) CUDA_TRY(cudaEventElapsedTime(total_ms, ev[0], ev[k - 1]));
+  for (auto& e : ev) cudaEventDestroy(e);
+  TRY(realign(h));
+  if (cycles_run) *cycles_run = h->enq_cycles - before;
+  return check_status(h);
+}
+
+extern "C" int fierro_sgh_time(fierro_sgh* h, double* time_value, double* dt, double* graphics_time,
+                               int64_t* cycle) {
+  clear_error();
+  if (!h) return set_error(FIERRO_EINVAL, "handle is NULL");
+  Ctrl c;
+  CUDA_TRY(cudaMemcpyAsync(&c, h->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (time_value) *time_value = c.time_value;
+  if (dt) *dt = c.dt;
+  if (graphics_time) *graphics_time = c.graphics_time;
+  if (cycle) *cycle = c.cycle;
+  return FIERRO_OK;
+}
+
+extern "C" int fierro_sgh_energy(fierro_sgh* h, double* ie, double* ke) {
+  clear_error();
+  if (!h || !h->has_state) return set_error(FIERRO_EINVAL, "energy before set_state");
+  long long cyc = 0;
+  TRY(cycles_done(h, &cyc));
+  const int c = bin_now(h, cyc);
+  const int b1 = (h->stage == 0) ? c : (c ^ 1);
+  EnergyArgs a{};
+  a.ne = (int)h->ne;
+  a.nn = (int)h->nn;
+  a.mass = h->d_elem_mass;
+  a.sie = h->d_sie[b1];
+  a.node_mass = h->d_node_mass;
+  a.u = h->d_v[b1][0];
+  a.v = h->d_v[b1][1];
+  a.w = h->d_v[b1][2];
+  a.part = h->d_energy_part;
+  a.out = h->d_energy_out;
+  h->ks->energy(a, h->stream);
+  double out[2];
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(out, h->d_energy_out, sizeof(out), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (ie) *ie = out[0];
+  if (ke) *ke = out[1];
+  return FIERRO_OK;
+}
+
+extern "C" int64_t fierro_sgh_launches_per_cycle(const fierro_sgh* h) {
+  return h ? 2 + 3 * (int64_t)h->rk_num_stages : 0;
+}
+
+extern "C" int64_t fierro_sgh_device_bytes(const fierro_sgh* h) { return h ? (int64_t)h->dev_bytes : 0; }
+
+extern "C" int fierro_sgh_solve(const fierro_mesh* mesh, const fierro_material* materials, int64_t num_materials,
+                                const fierro_boundary* boundaries, int64_t num_bcs, fierro_sgh_state* state,
+                                double* time_value, double time_final, double dt_max, double dt_min, double dt_cfl,
+                                double* graphics_time, int64_t graphics_cyc_ival, double graphics_dt_ival,
+                                int64_t cycle_stop, int64_t rk_num_stages, double dt, double fuzz, double tiny,
+                                double small, int fp_mode, int64_t* cycles_run) {
+  clear_error();
+  if (!time_value || !graphics_time || !state) return set_error(FIERRO_EINVAL, "solve: NULL argument");
+  fierro_sgh_params p{time_final, dt_max, dt_min, dt_cfl, dt, graphics_dt_ival, graphics_cyc_ival,
+                      cycle_stop, rk_num_stages, fuzz, tiny, small};
+  fierro_sgh* h = nullptr;
+  int rc = fierro_sgh_create(mesh, materials, num_materials, boundaries, num_bcs, &p, fp_mode, nullptr, &h);
+  if (rc) return rc;
+  rc = set_state_impl(h, state, *time_value, *graphics_time, dt);
+  int64_t ran = 0;
+  if (!rc) rc = fierro_sgh_run(h, cycle_stop, &ran);
+  if (!rc) rc = fierro_sgh_get_state(h, state);
+  if (!rc) rc = fierro_sgh_time(h, time_value, nullptr, graphics_time, nullptr);
+  if (cycles_run) *cycles_run = ran;
+  std::string msg = fierro_last_error();
+  fierro_sgh_destroy(h);
+  if (rc) set_error(rc, "%s", msg.c_str());
+  return rc;
+}

@@ -1,0 +1,129 @@
+// Device data layout and per-launch argument records of the SGH kernels.
+//
+// HBM layout (internal, Morton-ordered numbering):
+//   nodes    SoA float64: x,y,z and u,v,w in two ping-pong bins (cycle-start and
+//            current), half-velocity hx,hy,hz of the current stage, node mass,
+//            boundary bit mask (uint8)
+//   elements SoA float64: den, pres, sspd, vol, div, mass, gamma, c_min, sie in two
+//            bins; int32 nodes_in_elem [ne][8]
+//   bmat     [24][ne]  outward corner area normals B(lid, dim) of the current
+//            geometry (row lid*3+dim), written by the element kernel and read by
+//            the next stage's force kernel
+//   force    [24][ne]  corner forces, row lid*3+dim
+//   corner CSR per node (int32 corner id e*8+lid, reference summation order),
+//   neighbour CSR per element (int32)
+#ifndef FIERRO_SGH_DEVICE_H
+#define FIERRO_SGH_DEVICE_H
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace fierro {
+
+// Device-resident loop scalars (sgh_solve's time_value / dt / graphics_time).
+struct Ctrl {
+  double dt;
+  double time_value;
+  double graphics_time;
+  long long cycle;     // completed cycles
+  int active;          // the current cycle runs (set by the dt kernel)
+  int stopped;         // time_value reached time_final
+  unsigned int status; // FIERRO_STATUS_* bits
+  int pad;
+};
+
+#define FIERRO_STATUS_BAD_VOLUME 1u  // non-positive or non-finite element volume
+#define FIERRO_STATUS_BAD_STATE 2u   // non-finite energy, pressure or velocity
+
+struct LoopParams {
+  double time_final, dt_max, dt_min, dt_cfl, graphics_dt_ival, fuzz, small;
+  long long graphics_cyc_ival;
+};
+
+struct ForceArgs {
+  int ne;
+  const int* nie;
+  const int* eie_start;
+  const int* eie;
+  const int* mat;
+  const double* qtab;  // [nmat][4] = q1, q1ex, q2, q2ex
+  const double* bmat;
+  const double *u, *v, *w;  // current velocity (reference bin 1)
+  const double *den, *pres, *sspd, *vol, *div;
+  double* force;
+  const Ctrl* ctrl;
+  double fuzz, small;
+};
+
+struct NodeArgs {
+  int nn, ne;
+  const int* cin_start;
+  const int* cin;
+  const double* force;
+  const double* node_mass;
+  const unsigned char* bc_mask;
+  const double *u0, *v0, *w0, *x0, *y0, *z0;  // cycle start (reference bin 0)
+  double *u1, *v1, *w1, *x1, *y1, *z1;        // updated (reference bin 1)
+  double *hx, *hy, *hz;                       // half velocity (v1 + v0) / 2
+  const Ctrl* ctrl;
+  double rk_alpha;
+};
+
+// kind: 0 = stage update, 1 = last stage of a cycle (adds the CFL partial
+// minima), 2 = prime (geometry, divergence and CFL of the uploaded state only).
+struct ElemArgs {
+  int ne;
+  const int* nie;
+  const double *x, *y, *z;     // updated coordinates (reference bin 1)
+  const double *u, *v, *w;     // updated velocity
+  const double *hx, *hy, *hz;  // half velocity of this stage
+  const double* force;
+  const double* mass;
+  const double* sie0;
+  double* sie1;
+  const double *gamma, *csmin;
+  double *den, *pres, *sspd, *vol, *div;
+  double* bmat;
+  long long* cfl_part;  // per-block minimum of the element time steps (order keys)
+  Ctrl* ctrl;
+  double rk_alpha, dt_cfl, fuzz;
+};
+
+struct DtArgs {
+  const long long* cfl_part;
+  int nparts;
+  Ctrl* ctrl;
+  LoopParams lp;
+};
+
+struct EnergyArgs {
+  int ne, nn;
+  const double *mass, *sie;
+  const double *node_mass, *u, *v, *w;
+  double* part;  // [2][nblocks]
+  double* out;   // [2]
+};
+
+// One arithmetic mode's launchers (defined in sgh_kernels.cu, compiled once per mode).
+struct KernelSet {
+  void (*force)(const ForceArgs&, cudaStream_t);
+  void (*node)(const NodeArgs&, cudaStream_t);
+  void (*elem)(const ElemArgs&, int kind, cudaStream_t);
+  void (*dt)(const DtArgs&, cudaStream_t);
+  void (*end)(Ctrl*, const LoopParams&, cudaStream_t);
+  void (*energy)(const EnergyArgs&, cudaStream_t);
+  const char* name;
+};
+
+constexpr int kElemBlock = 128;
+constexpr int kForceBlock = 128;
+constexpr int kNodeBlock = 256;
+constexpr int kEnergyBlock = 256;
+
+const KernelSet& kernels_exact();
+const KernelSet& kernels_fma();
+
+}  // namespace fierro
+
+#endif

@@ -1,0 +1,52 @@
+// Internal declarations shared by the host C++ and CUDA translation units of
+// libfierro_sgh.  Not part of the public C ABI (include/fierro_sgh.h).
+#ifndef FIERRO_SGH_INTERNAL_H
+#define FIERRO_SGH_INTERNAL_H
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "fierro_sgh.h"
+
+namespace fierro {
+
+// Record an error for fierro_last_error() and return `code`.
+int set_error(int code, const char* fmt, ...);
+void clear_error();
+
+// Host-side mesh topology in the device ("internal") numbering.
+//
+// Elements and nodes are renumbered along a Morton curve of their positions, for
+// locality of the gathers.  Everything whose floating-point result depends on an
+// order keeps the reference's order: each node's corner list is sorted by the
+// caller's ("external") element id, which is the order in which
+// update_velocity_sgh sums corner forces (mesh.h:218-241, momentum.cpp:31-41),
+// and every element keeps its local node order 0..7.
+struct HostTopo {
+  int64_t nn = 0, ne = 0;
+  std::vector<int64_t> node_int2ext, node_ext2int, elem_int2ext, elem_ext2int;
+  std::vector<int32_t> nie;        // [ne][8] internal node ids of internal element e
+  std::vector<int32_t> cin_start;  // [nn+1] corner CSR per internal node
+  std::vector<int32_t> cin;        // internal corner ids e*8+lid, reference order
+  std::vector<int32_t> eie_start;  // [ne+1] neighbour CSR (elements sharing a node)
+  std::vector<int32_t> eie;
+  std::vector<uint8_t> bc_mask;    // [nn] bit d: velocity component d held at zero
+  int max_corners_per_node = 0;
+};
+
+// Validates the mesh and boundary deck and fills `t`.  `renumber` = false keeps
+// the caller's numbering (identity maps).
+int build_topology(const fierro_mesh* mesh, const fierro_boundary* bcs, int64_t num_bcs, bool renumber,
+                   HostTopo* t);
+
+// The boundary-condition bit mask per external node from the boundary patches
+// (faces owned by one element) that lie on each boundary set's surface
+// (setup.cpp:431-665).
+int boundary_masks(const fierro_mesh* mesh, const fierro_boundary* bcs, int64_t num_bcs,
+                   const double* coords_bin1, std::vector<uint8_t>* mask_ext,
+                   std::vector<std::vector<int64_t>>* set_nodes);
+
+}  // namespace fierro
+
+#endif

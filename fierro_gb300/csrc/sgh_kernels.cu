@@ -1,0 +1,477 @@
+// SGH cycle kernels for sm_103a (GB300), FP64.
+//
+// Compiled twice from this one source:
+//   FIERRO_FMA=0 with --fmad=false -> fierro::exact_impl: every floating-point
+//       operation is the reference's operation on the reference's operands in
+//       the reference's order (Explicit-Lagrange-Kokkos/SGH_solver), with IEEE
+//       division and square root, so results match its uncontracted evaluation;
+//   FIERRO_FMA=1 with --fmad=true  -> fierro::fma_impl: the same schedule, the
+//       compiler free to fuse multiply-adds, and the per-node division by mass
+//       done through one reciprocal.
+//
+// One cycle is 2 + 3*rk_num_stages launches:
+//   k_dt                    CFL minimum over the last stage's per-block partials,
+//                           dt growth/clamps (time_integration.cpp:54-154)
+//   per RK stage s:
+//     k_force   (elements)  MARS corner forces (force_sgh.cpp:12-399) from the
+//                           corner normals the previous element pass stored
+//     k_node    (nodes)     corner-force gather in the reference's summation order,
+//                           velocity update, boundary conditions, position update
+//                           (momentum.cpp:11-53, boundary.cpp:10-55, geometry.cpp:9-26)
+//     k_elem    (elements)  energy (energy_sgh.cpp:6-55), volume (geometry.cpp:238-310),
+//                           density/EOS (properties.cpp:9-114, eos.cpp:12-46), then
+//                           the corner normals and divergence the NEXT stage starts
+//                           from (momentum.cpp:221-292), and on the last stage the
+//                           per-element CFL time step of the next cycle
+//   k_end                   time advance, graphics-time bookkeeping, stop test
+//                           (sgh_solve.cpp:590-632)
+// rk_init's copies (time_integration.cpp:9-44) are replaced by swapping the roles
+// of two state bins.  Nothing is accumulated with atomics: every output has one
+// writer and every reduction has a fixed order.
+#include <cstdint>
+#include <cstdio>
+
+#include "sgh_device.h"
+
+#ifndef FIERRO_FMA
+#error "compile with -DFIERRO_FMA=0 or -DFIERRO_FMA=1"
+#endif
+
+#if FIERRO_FMA
+#define FIERRO_IMPL fma_impl
+#else
+#define FIERRO_IMPL exact_impl
+#endif
+
+namespace fierro {
+namespace FIERRO_IMPL {
+
+// Order-preserving map from a double to a signed 64-bit key (integer min/max run
+// on the integer pipes instead of the FP64 pipe).  -0.0 sorts just below +0.0.
+__device__ __forceinline__ long long okey(double d) {
+  const long long b = __double_as_longlong(d);
+  return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL);
+}
+__device__ __forceinline__ double okey_decode(long long k) {
+  return __longlong_as_double(k ^ ((k >> 63) & 0x7FFFFFFFFFFFFFFFLL));
+}
+
+#include "sgh_hex_geometry.cuh"
+
+// pow(v, 1.0/3.0) as the reference computes it (force_sgh.cpp:319-320).
+// The exponent is fl(1/3) = 1/3 - d, d = 2^-54/3, so the target is
+// cbrt(v) * v^-d = cbrt(v) * (1 - d ln v + O(d^2 ln^2 v)).  c0 = cbrt(v) (<= 1 ulp)
+// is refined by one Newton step for t^3 = v whose residual v - c0^3 is formed
+// with error-free products (fma), and the -c0 d ln v term is added; both are
+// sub-ulp corrections, so ln v and the step only need ~1e-6 relative accuracy.
+// The result is the correctly rounded power except within ~1e-6 ulp of a
+// rounding boundary.  Non-positive, subnormal and non-finite inputs use pow().
+__device__ __forceinline__ double pow_third(double v) {
+#if FIERRO_FMA
+  return cbrt(v);
+#else
+  if (!(v > 1.0e-290 && v < 1.0e290)) return pow(v, 1.0 / 3.0);
+  const double c0 = cbrt(v);
+  const double p = c0 * c0;
+  const double pe = fma(c0, c0, -p);
+  const double q = p * c0;
+  const double qe = fma(p, c0, -q) + pe * c0;
+  const double r = (v - q) - qe;  // v - q is exact (Sterbenz), qe carries the rest
+  const float rf = (float)r;
+  const float inv3p = __frcp_rn(3.0f * (float)p);
+  const float step = rf * inv3p;  // (v - c0^3) / (3 c0^2)
+  // ln v from the exponent and a single-precision log of the significand
+  const long long bits = __double_as_longlong(v);
+  const int ex = (int)((bits >> 52) & 0x7FF) - 1023;
+  const double m = __longlong_as_double((bits & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL);
+  const float lnv = (float)ex * 0.69314718f + __logf((float)m);
+  const float dlog = lnv * 1.8503717077085943e-17f;  // d = 2^-54 / 3
+  const double lo = (double)step - c0 * (double)dlog;
+  return c0 + lo;
+#endif
+}
+
+__device__ __forceinline__ long long block_min_key(long long k) {
+  for (int o = 16; o > 0; o >>= 1) {
+    long long t = __shfl_xor_sync(0xFFFFFFFFu, k, o);
+    k = t < k ? t : k;
+  }
+  __shared__ long long warp_min[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) warp_min[wid] = k;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  if (wid == 0) {
+    k = lane < nw ? warp_min[lane] : 0x7FFFFFFFFFFFFFFFLL;
+    for (int o = 16; o > 0; o >>= 1) {
+      long long t = __shfl_xor_sync(0xFFFFFFFFu, k, o);
+      k = t < k ? t : k;
+    }
+  }
+  return k;  // valid in thread 0
+}
+
+// ---------------------------------------------------------------------------
+// Corner forces (force_sgh.cpp:35-394, 3D, strength none).  The reference's
+// shock-direction, velocity-gradient and curl terms only feed unused values
+// (use_shock_dir = 0 at :227, phi_curl unused at :331) and are not computed.
+// Stress is zero for strength-free materials, so tau = -p I and the force's
+// stress term a_k tau(k,d) reduces exactly to B(d) p (two negations).
+__global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
+  if (!a.ctrl->active) return;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= a.ne) return;
+  const int ne = a.ne;
+  const int4 n03 = __ldg(reinterpret_cast<const int4*>(a.nie) + 2 * e);
+  const int4 n47 = __ldg(reinterpret_cast<const int4*>(a.nie) + 2 * e + 1);
+  const int nid[8] = {n03.x, n03.y, n03.z, n03.w, n47.x, n47.y, n47.z, n47.w};
+  double vu[8], vv[8], vw[8];
+#pragma unroll
+  for (int l = 0; l < 8; ++l) {
+    vu[l] = __ldg(a.u + nid[l]);
+    vv[l] = __ldg(a.v + nid[l]);
+    vw[l] = __ldg(a.w + nid[l]);
+  }
+  const double den = a.den[e], pres = a.pres[e], sspd = a.sspd[e], vol = a.vol[e], div = a.div[e];
+  const int mat = a.mat[e];
+  const double* q = a.qtab + 4 * mat;
+  const bool compress = div < 0;
+  const double qa = compress ? q[0] : q[1];  // q1 or q1ex
+  const double qb = compress ? q[2] : q[3];  // q2 or q2ex
+
+  // average velocity, the first Riemann-velocity estimate (:147-164); 0.125*v is
+  // exact, so the fused form equals the reference's product-then-add
+  double vs0 = 0.0, vs1 = 0.0, vs2 = 0.0;
+#pragma unroll
+  for (int l = 0; l < 8; ++l) {
+    vs0 = fma(0.125, vu[l], vs0);
+    vs1 = fma(0.125, vv[l], vs1);
+    vs2 = fma(0.125, vw[l], vs2);
+  }
+  // MARS impedances (:176-255)
+  double mu[8];
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  const double q1c = qa * sspd;
+#pragma unroll
+  for (int l = 0; l < 8; ++l) {
+    const double d0 = vu[l] - vs0, d1 = vv[l] - vs1, d2 = vw[l] - vs2;
+    const double mag_vel = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    const double muc = den * (q1c + qb * mag_vel);
+    const double b0 = a.bmat[(size_t)(l * 3 + 0) * ne + e];
+    const double b1 = a.bmat[(size_t)(l * 3 + 1) * ne + e];
+    const double b2 = a.bmat[(size_t)(l * 3 + 2) * ne + e];
+    const double mu_term = muc * sqrt(b0 * b0 + b1 * b1 + b2 * b2);
+    s0 = s0 + mu_term * vu[l];
+    s1 = s1 + mu_term * vv[l];
+    s2 = s2 + mu_term * vw[l];
+    s3 = s3 + mu_term;
+    mu[l] = mu_term;
+  }
+  double vstar0 = 0.0, vstar1 = 0.0, vstar2 = 0.0;
+  if (s3 > a.fuzz) {
+#if FIERRO_FMA
+    const double rs = 1.0 / s3;
+    vstar0 = s0 * rs;
+    vstar1 = s1 * rs;
+    vstar2 = s2 * rs;
+#else
+    vstar0 = s0 / s3;
+    vstar1 = s1 / s3;
+    vstar2 = s2 / s3;
+#endif
+  }
+  // shock detector (:287-315): r_face = 0.9 (div_nb + small) / (div + small) is
+  // monotone in div_nb (non-decreasing for div + small > 0, non-increasing for < 0),
+  // so the minimum over neighbours is attained at the smallest (resp. largest)
+  // neighbour divergence and needs one division instead of one per neighbour.
+  const double small = a.small;
+  const double D = div + small;
+  const int k0 = a.eie_start[e], k1 = a.eie_start[e + 1];
+  long long kmin = 0x7FFFFFFFFFFFFFFFLL, kmax = (long long)0x8000000000000000ULL;
+  for (int k = k0; k < k1; ++k) {
+    const long long key = okey(__ldg(a.div + __ldg(a.eie + k)));
+    kmin = key < kmin ? key : kmin;
+    kmax = key > kmax ? key : kmax;
+  }
+  double r_min = 1.0;
+  if (k1 > k0) {
+    const double dsel = okey_decode(D > 0 ? kmin : kmax);
+    const bool regular = isfinite(D) && D != 0.0 && isfinite(dsel);
+    if (regular) {
+      const double r_face = 0.9 * (dsel + small) / D;
+      r_min = okey(r_face) < okey(1.0) ? r_face : 1.0;
+    } else {
+      for (int k = k0; k < k1; ++k) {
+        const double r_face = 0.9 * (__ldg(a.div + __ldg(a.eie + k)) + small) / D;
+        r_min = fmin(r_face, r_min);
+      }
+    }
+  }
+  double phi = 1.0 - fmax(0.0, r_min);  // pow(phi, 1.0) == phi
+  // Mach-number detector (:318-328)
+  const double c_length = pow_third(vol);
+  const double alpha = fmin(1.0, 20.0 * (c_length * fabs(div)) / (sspd + a.fuzz));
+  phi = alpha * phi;
+  // corner forces (:338-359)
+#pragma unroll
+  for (int l = 0; l < 8; ++l) {
+    const double pm = phi * mu[l];
+    const double b0 = a.bmat[(size_t)(l * 3 + 0) * ne + e];
+    const double b1 = a.bmat[(size_t)(l * 3 + 1) * ne + e];
+    const double b2 = a.bmat[(size_t)(l * 3 + 2) * ne + e];
+    a.force[(size_t)(l * 3 + 0) * ne + e] = b0 * pres + pm * (vstar0 - vu[l]);
+    a.force[(size_t)(l * 3 + 1) * ne + e] = b1 * pres + pm * (vstar1 - vv[l]);
+    a.force[(size_t)(l * 3 + 2) * ne + e] = b2 * pres + pm * (vstar2 - vw[l]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Node update: corner-force gather in the reference's summation order, velocity,
+// boundary conditions, half velocity and position.
+__global__ void __launch_bounds__(kNodeBlock) k_node(const NodeArgs a) {
+  if (!a.ctrl->active) return;
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= a.nn) return;
+  const size_t ne = (size_t)a.ne;
+  double f0 = 0.0, f1 = 0.0, f2 = 0.0;
+  const int c0 = a.cin_start[n], c1 = a.cin_start[n + 1];
+  for (int c = c0; c < c1; ++c) {
+    const int cid = __ldg(a.cin + c);
+    const int e = cid >> 3, l = cid & 7;
+    f0 = f0 + __ldg(a.force + (size_t)(l * 3 + 0) * ne + e);
+    f1 = f1 + __ldg(a.force + (size_t)(l * 3 + 1) * ne + e);
+    f2 = f2 + __ldg(a.force + (size_t)(l * 3 + 2) * ne + e);
+  }
+  const double adt = a.rk_alpha * a.ctrl->dt;
+  const double m = a.node_mass[n];
+  const double u0 = a.u0[n], v0 = a.v0[n], w0 = a.w0[n];
+#if FIERRO_FMA
+  const double rm = 1.0 / m;
+  double u1 = u0 + adt * f0 * rm;
+  double v1 = v0 + adt * f1 * rm;
+  double w1 = w0 + adt * f2 * rm;
+#else
+  double u1 = u0 + adt * f0 / m;
+  double v1 = v0 + adt * f1 / m;
+  double w1 = w0 + adt * f2 / m;
+#endif
+  const unsigned bc = a.bc_mask[n];
+  if (bc & 1u) u1 = 0.0;
+  if (bc & 2u) v1 = 0.0;
+  if (bc & 4u) w1 = 0.0;
+  const double hu = (u1 + u0) * 0.5, hv = (v1 + v0) * 0.5, hw = (w1 + w0) * 0.5;
+  a.u1[n] = u1;
+  a.v1[n] = v1;
+  a.w1[n] = w1;
+  a.hx[n] = hu;
+  a.hy[n] = hv;
+  a.hz[n] = hw;
+  a.x1[n] = a.x0[n] + adt * hu;
+  a.y1[n] = a.y0[n] + adt * hv;
+  a.z1[n] = a.z0[n] + adt * hw;
+}
+
+// ---------------------------------------------------------------------------
+// Element update.  KIND 0: stage; 1: last stage (adds the CFL partials);
+// 2: prime (corner normals, divergence and CFL of an uploaded state).
+template <int KIND>
+__global__ void __launch_bounds__(kElemBlock) k_elem(const ElemArgs a) {
+  if (KIND != 2 && !a.ctrl->active) return;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = e < a.ne;
+  long long dkey = 0x7FFFFFFFFFFFFFFFLL;
+  if (live) {
+    const int ne = a.ne;
+    const int4 n03 = __ldg(reinterpret_cast<const int4*>(a.nie) + 2 * e);
+    const int4 n47 = __ldg(reinterpret_cast<const int4*>(a.nie) + 2 * e + 1);
+    const int nid[8] = {n03.x, n03.y, n03.z, n03.w, n47.x, n47.y, n47.z, n47.w};
+    double x[8], y[8], z[8], u[8], v[8], w[8];
+#pragma unroll
+    for (int l = 0; l < 8; ++l) {
+      x[l] = __ldg(a.x + nid[l]);
+      y[l] = __ldg(a.y + nid[l]);
+      z[l] = __ldg(a.z + nid[l]);
+      u[l] = __ldg(a.u + nid[l]);
+      v[l] = __ldg(a.v + nid[l]);
+      w[l] = __ldg(a.w + nid[l]);
+    }
+    double sie1 = 0.0;
+    if (KIND != 2) {
+      // energy (energy_sgh.cpp:16-52): power = sum_c F_c . (v1 + v0)/2, lid-major
+      double power = 0.0;
+#pragma unroll
+      for (int l = 0; l < 8; ++l) {
+        power = power + a.force[(size_t)(l * 3 + 0) * ne + e] * __ldg(a.hx + nid[l]);
+        power = power + a.force[(size_t)(l * 3 + 1) * ne + e] * __ldg(a.hy + nid[l]);
+        power = power + a.force[(size_t)(l * 3 + 2) * ne + e] * __ldg(a.hz + nid[l]);
+      }
+      const double adt = a.rk_alpha * a.ctrl->dt;
+      sie1 = a.sie0[e] - adt / a.mass[e] * power;
+      a.sie1[e] = sie1;
+    }
+    double vol_geo, Sx, Sy, Sz, d2min;
+    hex_geometry<KIND != 0>(x, y, z, u, v, w, a.bmat, ne, e, vol_geo, Sx, Sy, Sz, d2min);
+    // the priming pass keeps the uploaded volume, as get_divergence reads elem_vol
+    const double vol = (KIND == 2) ? a.vol[e] : vol_geo;
+    // divergence for the next stage (momentum.cpp:265-286), with this geometry
+    const double inverse_vol = 1.0 / vol;
+    double div = 0.0;
+    div = div + Sx * inverse_vol;
+    div = div + Sy * inverse_vol;
+    div = div + Sz * inverse_vol;
+    a.div[e] = div;
+    double sspd;
+    if (KIND != 2) {
+      a.vol[e] = vol;
+      // update_state (properties.cpp:39, eos.cpp:85-98)
+      const double den = a.mass[e] / vol;
+      const double gamma = a.gamma[e], csmin = a.csmin[e];
+      const double pres = (gamma - 1.0) * sie1 * den;
+      sspd = sqrt(gamma * (gamma - 1.0) * sie1);
+      if (sspd < csmin) sspd = csmin;
+      a.den[e] = den;
+      a.pres[e] = pres;
+      a.sspd[e] = sspd;
+      if (!(vol > 0.0) || !isfinite(vol)) atomicOr(&a.ctrl->status, FIERRO_STATUS_BAD_VOLUME);
+      if (!isfinite(sie1) || !isfinite(pres)) atomicOr(&a.ctrl->status, FIERRO_STATUS_BAD_STATE);
+    } else {
+      sspd = a.sspd[e];
+    }
+    if (KIND != 0) {
+      // element CFL step dt_cfl * min distance / (c + fuzz) (time_integration.cpp:124-131);
+      // min of the square roots == square root of the min (sqrt is monotone, exact)
+      const double dist_min = sqrt(d2min);
+      const double dt_l = a.dt_cfl * dist_min / (sspd + a.fuzz);
+      dkey = isnan(dt_l) ? 0x7FFFFFFFFFFFFFFFLL : okey(dt_l);
+    }
+  }
+  if (KIND != 0) {
+    const long long k = block_min_key(dkey);
+    if (threadIdx.x == 0) a.cfl_part[blockIdx.x] = k;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// get_timestep's scalar part (time_integration.cpp:69-150) on the device.  The
+// per-element clamp to [dt_min, dt_max] commutes with the minimum (it is
+// monotone), so it is applied once to the minimum.
+__global__ void __launch_bounds__(1024) k_dt(const DtArgs a) {
+  long long k = 0x7FFFFFFFFFFFFFFFLL;
+  for (int i = threadIdx.x; i < a.nparts; i += blockDim.x) {
+    const long long t = a.cfl_part[i];
+    k = t < k ? t : k;
+  }
+  k = block_min_key(k);
+  if (threadIdx.x != 0) return;
+  Ctrl* c = a.ctrl;
+  if (c->stopped) {
+    c->active = 0;
+    return;
+  }
+  double dt = c->dt * 1.1;
+  double min_dt_calc = (k == 0x7FFFFFFFFFFFFFFFLL) ? 1.7976931348623157e308 : okey_decode(k);
+  min_dt_calc = fmin(min_dt_calc, a.lp.dt_max);
+  min_dt_calc = fmax(min_dt_calc, a.lp.dt_min);
+  if (min_dt_calc < dt) dt = min_dt_calc;
+  dt = fmin(dt, (c->graphics_time - c->time_value) + a.lp.fuzz);
+  dt = fmin(dt, a.lp.time_final - c->time_value);
+  c->dt = dt;
+  c->active = 1;
+}
+
+// End of a cycle (sgh_solve.cpp:590-632).
+__global__ void k_end(Ctrl* c, const LoopParams lp) {
+  if (!c->active) return;
+  c->time_value += c->dt;
+  const long long cycle = c->cycle;
+  bool write = false;
+  if ((cycle + 1) % lp.graphics_cyc_ival == 0 && cycle > 0) write = true;
+  else if (c->time_value >= lp.time_final) write = true;
+  else if (c->time_value >= c->graphics_time) write = true;
+  if (write) c->graphics_time = c->time_value + lp.graphics_dt_ival;
+  if (c->time_value >= lp.time_final) c->stopped = 1;
+  c->cycle = cycle + 1;
+  c->active = 0;
+}
+
+// Energy tallies (sgh_solve.cpp:77-101): fixed-shape two-pass sums.
+__global__ void __launch_bounds__(kEnergyBlock) k_energy_part(const EnergyArgs a) {
+  __shared__ double sh[2][kEnergyBlock];
+  double ie = 0.0, ke = 0.0;
+  const int stride = gridDim.x * blockDim.x;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.ne; i += stride) ie += a.mass[i] * a.sie[i];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nn; i += stride) {
+    double k = 0;
+    k += a.u[i] * a.u[i];
+    k += a.v[i] * a.v[i];
+    k += a.w[i] * a.w[i];
+    ke += a.node_mass[i] * k;
+  }
+  sh[0][threadIdx.x] = ie;
+  sh[1][threadIdx.x] = ke;
+  __syncthreads();
+  for (int s = kEnergyBlock / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + s];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    a.part[blockIdx.x] = sh[0][0];
+    a.part[gridDim.x + blockIdx.x] = sh[1][0];
+  }
+}
+
+__global__ void k_energy_final(const EnergyArgs a, int nblocks) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double ie = 0.0, ke = 0.0;
+  for (int b = 0; b < nblocks; ++b) {
+    ie += a.part[b];
+    ke += a.part[nblocks + b];
+  }
+  a.out[0] = ie;
+  a.out[1] = 0.5 * ke;
+}
+
+// ---------------------------------------------------------------------------
+static unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+static void launch_force(const ForceArgs& a, cudaStream_t s) {
+  k_force<<<blocks_for(a.ne, kForceBlock), kForceBlock, 0, s>>>(a);
+}
+static void launch_node(const NodeArgs& a, cudaStream_t s) {
+  k_node<<<blocks_for(a.nn, kNodeBlock), kNodeBlock, 0, s>>>(a);
+}
+static void launch_elem(const ElemArgs& a, int kind, cudaStream_t s) {
+  const unsigned g = blocks_for(a.ne, kElemBlock);
+  if (kind == 0) k_elem<0><<<g, kElemBlock, 0, s>>>(a);
+  else if (kind == 1) k_elem<1><<<g, kElemBlock, 0, s>>>(a);
+  else k_elem<2><<<g, kElemBlock, 0, s>>>(a);
+}
+static void launch_dt(const DtArgs& a, cudaStream_t s) { k_dt<<<1, 1024, 0, s>>>(a); }
+static void launch_end(Ctrl* c, const LoopParams& lp, cudaStream_t s) { k_end<<<1, 1, 0, s>>>(c, lp); }
+static void launch_energy(const EnergyArgs& a, cudaStream_t s) {
+  const int nb = 512;
+  k_energy_part<<<nb, kEnergyBlock, 0, s>>>(a);
+  k_energy_final<<<1, 32, 0, s>>>(a, nb);
+}
+
+}  // namespace FIERRO_IMPL
+
+#if FIERRO_FMA
+const KernelSet& kernels_fma() {
+  static const KernelSet k = {fma_impl::launch_force, fma_impl::launch_node, fma_impl::launch_elem,
+                              fma_impl::launch_dt, fma_impl::launch_end, fma_impl::launch_energy, "fma"};
+  return k;
+}
+#else
+const KernelSet& kernels_exact() {
+  static const KernelSet k = {exact_impl::launch_force, exact_impl::launch_node, exact_impl::launch_elem,
+                              exact_impl::launch_dt, exact_impl::launch_end, exact_impl::launch_energy,
+                              "exact"};
+  return k;
+}
+#endif
+
+}  // namespace fierro

@@ -137,9 +137,9 @@ def sedov(n: int = 12, length: float = 1.2, energy: float = 0.2467, gamma: float
         mesh = box_mesh(n, length=length, jitter=jitter, seed=seed, permute=permute,
                         geo_digits=geo_digits, name="sedov%d" % n)
     h = length / n
-    # the element whose centroid lies in [0,h]^3 is the origin-corner element
-    cen = mesh.coords[mesh.nodes_in_elem].mean(axis=1)
-    origin = np.nonzero(np.all((cen >= 0.0) & (cen <= h), axis=1))[0]
+    # the origin-corner element is the one element holding the node at the origin
+    n0 = int(np.argmin(np.einsum("ij,ij->i", mesh.coords, mesh.coords)))
+    origin = np.nonzero(np.any(mesh.nodes_in_elem == n0, axis=1))[0]
     assert origin.size == 1, "origin element not unique"
     e0 = int(origin[0])
     v0 = float(hex_volumes(mesh.coords, mesh.nodes_in_elem[e0:e0 + 1])[0])

@@ -1,0 +1,296 @@
+"""Python mirror of the SGH solver interface over the libfierro_sgh C ABI.
+
+The names and argument meanings follow Explicit-Lagrange-Kokkos/SGH_solver:
+``setup`` (setup.cpp:10-424) builds the initial state, ``sgh_solve``
+(sgh_solve.cpp:8-692) runs the cycle loop, and ``SGHSolver`` is the persistent
+device-resident handle.  State travels as a dict of numpy arrays in the
+reference layouts (see include/fierro_sgh.h).
+
+There is no CPU fallback: importing this module loads the CUDA library and
+every call runs on the GPU; a missing library raises ImportError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Dict, Optional
+
+import numpy as np
+
+from .problems import HYDRO_BC, REGION, SURFACE, VELOCITY, Problem
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfierro_sgh.so")
+
+FIERRO_OK, FIERRO_EINVAL, FIERRO_ENOMEM, FIERRO_ECUDA, FIERRO_ENUMERIC, FIERRO_ETIMEDOUT, FIERRO_ENOTSUP = range(7)
+FP_EXACT, FP_FMA = 0, 1
+_ERRNAMES = {1: "EINVAL", 2: "ENOMEM", 3: "ECUDA", 4: "ENUMERIC", 5: "ETIMEDOUT", 6: "ENOTSUP"}
+
+
+class FierroError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("fierro %s: %s" % (_ERRNAMES.get(code, str(code)), msg))
+        self.code = code
+
+
+class Material(C.Structure):
+    _fields_ = [("eos_model", C.c_int), ("strength_type", C.c_int), ("q1", C.c_double),
+                ("q1ex", C.c_double), ("q2", C.c_double), ("q2ex", C.c_double)]
+
+
+class Boundary(C.Structure):
+    _fields_ = [("surface", C.c_int), ("value", C.c_double), ("hydro_bc", C.c_int)]
+
+
+class MatFill(C.Structure):
+    _fields_ = [("volume", C.c_int), ("mat_id", C.c_int)] + \
+        [(k, C.c_double) for k in ("x1", "x2", "y1", "y2", "z1", "z2", "radius1", "radius2")] + \
+        [("velocity", C.c_int)] + [(k, C.c_double) for k in ("u", "v", "w", "speed", "sie", "den")]
+
+
+class Params(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("time_final", "dt_max", "dt_min", "dt_cfl", "dt_start",
+                                          "graphics_dt_ival")] + \
+        [(k, C.c_int64) for k in ("graphics_cyc_ival", "cycle_stop", "rk_num_stages")] + \
+        [(k, C.c_double) for k in ("fuzz", "tiny", "small")]
+
+
+class Mesh(C.Structure):
+    _fields_ = [("num_nodes", C.c_int64), ("num_elems", C.c_int64), ("nodes_in_elem", C.c_void_p),
+                ("coords", C.c_void_p)]
+
+
+class State(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k in (
+        "node_coords", "node_vel", "node_mass", "elem_den", "elem_pres", "elem_stress", "elem_sspd",
+        "elem_sie", "elem_vol", "elem_div", "elem_mass", "elem_mat_id", "elem_statev", "corner_force")] + \
+        [("num_state_vars", C.c_int64)]
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libfierro_sgh.so is not built (run __graft_entry__.build()); "
+                          "the SGH path has no CPU fallback")
+    lib = C.CDLL(LIB_PATH)
+    vp, i64, dbl = C.c_void_p, C.c_int64, C.c_double
+    lib.fierro_last_error.restype = C.c_char_p
+    lib.fierro_version.restype = C.c_char_p
+    lib.fierro_sgh_setup.argtypes = [vp, vp, i64, vp, i64, vp, i64, vp, i64, vp]
+    lib.fierro_sgh_solve.argtypes = [vp, vp, i64, vp, i64, vp, C.POINTER(dbl), dbl, dbl, dbl, dbl,
+                                     C.POINTER(dbl), i64, dbl, i64, i64, dbl, dbl, dbl, dbl, C.c_int,
+                                     C.POINTER(i64)]
+    lib.fierro_sgh_create.argtypes = [vp, vp, i64, vp, i64, vp, C.c_int, vp, C.POINTER(vp)]
+    lib.fierro_sgh_destroy.argtypes = [vp]
+    lib.fierro_sgh_set_state.argtypes = [vp, vp]
+    lib.fierro_sgh_get_state.argtypes = [vp, vp]
+    lib.fierro_sgh_enqueue_cycles.argtypes = [vp, i64]
+    lib.fierro_sgh_run.argtypes = [vp, i64, C.POINTER(i64)]
+    lib.fierro_sgh_run_stages.argtypes = [vp, i64]
+    lib.fierro_sgh_synchronize.argtypes = [vp]
+    lib.fierro_sgh_time.argtypes = [vp, C.POINTER(dbl), C.POINTER(dbl), C.POINTER(dbl), C.POINTER(i64)]
+    lib.fierro_sgh_energy.argtypes = [vp, C.POINTER(dbl), C.POINTER(dbl)]
+    lib.fierro_sgh_launches_per_cycle.argtypes = [vp]
+    lib.fierro_sgh_launches_per_cycle.restype = i64
+    lib.fierro_sgh_device_bytes.argtypes = [vp]
+    lib.fierro_sgh_device_bytes.restype = i64
+    lib.fierro_sgh_run_timed.argtypes = [vp, i64, vp, C.POINTER(C.c_float), C.POINTER(i64)]
+    lib.fierro_measure_fp64_rate.argtypes = [C.POINTER(dbl)]
+    return lib
+
+
+_lib = _load()
+
+
+def lib():
+    return _lib
+
+
+def _check(rc: int):
+    if rc != FIERRO_OK:
+        raise FierroError(rc, _lib.fierro_last_error().decode())
+
+
+def version() -> str:
+    return _lib.fierro_version().decode()
+
+
+# ---------------------------------------------------------------- deck conversion
+def c_mesh(mesh) -> tuple:
+    nie = np.ascontiguousarray(mesh.nodes_in_elem, dtype=np.uint64)
+    xyz = np.ascontiguousarray(mesh.coords, dtype=np.float64)
+    m = Mesh(mesh.num_nodes, mesh.num_elems, nie.ctypes.data, xyz.ctypes.data)
+    return m, (nie, xyz)
+
+
+def c_materials(problem: Problem):
+    mats = problem.materials
+    return (Material * len(mats))(*[Material(0, 0, q.q1, q.q1ex, q.q2, q.q2ex) for q in mats])
+
+
+def c_boundaries(problem: Problem):
+    bl = problem.boundaries
+    return (Boundary * max(len(bl), 1))(*[Boundary(SURFACE[b.surface], b.value, HYDRO_BC[b.hydro_bc])
+                                          for b in bl])
+
+
+def c_fills(problem: Problem):
+    fl = problem.fills
+    return (MatFill * max(len(fl), 1))(*[MatFill(
+        REGION[f.volume], f.mat_id, f.x1, f.x2, f.y1, f.y2, f.z1, f.z2, f.radius1, f.radius2,
+        VELOCITY[f.velocity], f.u, f.v, f.w, f.speed, f.sie, f.den) for f in fl])
+
+
+def c_params(problem: Problem) -> Params:
+    p = problem.params
+    return Params(p.time_final, p.dt_max, p.dt_min, p.dt_cfl, p.dt_start, p.graphics_dt_ival,
+                  p.graphics_cyc_ival, p.cycle_stop, p.rk_num_stages, p.fuzz, p.tiny, p.small)
+
+
+def empty_state(nn: int, ne: int, nsv: int = 6, pinned: bool = False) -> Dict[str, np.ndarray]:
+    """Host arrays for one state in the reference layouts."""
+    return {
+        "node_coords": np.zeros((2, nn, 3)), "node_vel": np.zeros((2, nn, 3)), "node_mass": np.zeros(nn),
+        "elem_den": np.zeros(ne), "elem_pres": np.zeros(ne), "elem_stress": np.zeros((2, ne, 3, 3)),
+        "elem_sspd": np.zeros(ne), "elem_sie": np.zeros((2, ne)), "elem_vol": np.zeros(ne),
+        "elem_div": np.zeros(ne), "elem_mass": np.zeros(ne), "elem_mat_id": np.zeros(ne, dtype=np.uint64),
+        "elem_statev": np.zeros((ne, nsv)), "corner_force": np.zeros((8 * ne, 3)),
+    }
+
+
+def c_state(st: Dict[str, np.ndarray]) -> State:
+    s = State()
+    for k, _ in State._fields_[:-1]:
+        a = st.get(k)
+        if a is not None:
+            assert a.flags["C_CONTIGUOUS"], k
+            setattr(s, k, a.ctypes.data)
+    s.num_state_vars = st["elem_statev"].shape[1]
+    return s
+
+
+def setup(problem: Problem) -> Dict[str, np.ndarray]:
+    """setup (setup.cpp:10-424) on the host: the initial state of a problem deck."""
+    m, keep = c_mesh(problem.mesh)
+    st = empty_state(problem.mesh.num_nodes, problem.mesh.num_elems, problem.num_state_vars)
+    sv = np.ascontiguousarray(problem.state_vars())
+    _check(_lib.fierro_sgh_setup(C.byref(m), c_materials(problem), len(problem.materials), sv.ctypes.data,
+                                 problem.num_state_vars, c_fills(problem), len(problem.fills),
+                                 c_boundaries(problem), len(problem.boundaries), C.byref(c_state(st))))
+    return st
+
+
+def sgh_solve(problem: Problem, state: Dict[str, np.ndarray], cycle_stop: Optional[int] = None,
+              time_value: float = 0.0, fp_mode: int = FP_EXACT) -> dict:
+    """sgh_solve (sgh_solve.cpp:8-692) over host arrays: uploads, runs the cycle
+    loop on the GPU and writes the final state back into `state` (in place).
+    Returns time_value, graphics_time and the number of cycles run."""
+    p = problem.params
+    m, keep = c_mesh(problem.mesh)
+    tv = C.c_double(time_value)
+    gt = C.c_double(p.graphics_dt_ival)
+    ran = C.c_int64(0)
+    ncyc = p.cycle_stop if cycle_stop is None else cycle_stop
+    _check(_lib.fierro_sgh_solve(C.byref(m), c_materials(problem), len(problem.materials), c_boundaries(problem),
+                                 len(problem.boundaries), C.byref(c_state(state)), C.byref(tv), p.time_final,
+                                 p.dt_max, p.dt_min, p.dt_cfl, C.byref(gt), p.graphics_cyc_ival,
+                                 p.graphics_dt_ival, ncyc, p.rk_num_stages, p.dt_start, p.fuzz, p.tiny,
+                                 p.small, fp_mode, C.byref(ran)))
+    return {"time_value": tv.value, "graphics_time": gt.value, "cycles": ran.value}
+
+
+class SGHSolver:
+    """Persistent device-resident SGH solver for one mesh."""
+
+    def __init__(self, problem: Problem, fp_mode: int = FP_EXACT, stream: int | None = None):
+        self.problem = problem
+        self.nn, self.ne = problem.mesh.num_nodes, problem.mesh.num_elems
+        self.nsv = problem.num_state_vars
+        m, self._keep = c_mesh(problem.mesh)
+        self._params = c_params(problem)
+        h = C.c_void_p()
+        _check(_lib.fierro_sgh_create(C.byref(m), c_materials(problem), len(problem.materials),
+                                      c_boundaries(problem), len(problem.boundaries), C.byref(self._params),
+                                      fp_mode, C.c_void_p(stream) if stream else None, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            _lib.fierro_sgh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_state(self, st: Dict[str, np.ndarray]):
+        _check(_lib.fierro_sgh_set_state(self.h, C.byref(c_state(st))))
+
+    def get_state(self, st: Optional[Dict[str, np.ndarray]] = None) -> Dict[str, np.ndarray]:
+        if st is None:
+            st = empty_state(self.nn, self.ne, self.nsv)
+        _check(_lib.fierro_sgh_get_state(self.h, C.byref(c_state(st))))
+        return st
+
+    def run(self, cycles: int) -> int:
+        ran = C.c_int64(0)
+        _check(_lib.fierro_sgh_run(self.h, cycles, C.byref(ran)))
+        return ran.value
+
+    def run_timed(self, cycles: int):
+        """Runs `cycles` cycles with an event after every launch; returns
+        (cycles_run, total_ms, per-launch-slot ms summed over cycles)."""
+        L = self.launches_per_cycle
+        kms = (C.c_float * L)()
+        tot = C.c_float(0)
+        ran = C.c_int64(0)
+        _check(_lib.fierro_sgh_run_timed(self.h, cycles, kms, C.byref(tot), C.byref(ran)))
+        return ran.value, tot.value, list(kms)
+
+    def launch_names(self):
+        S = self.problem.params.rk_num_stages
+        return ["k_dt"] + [n for s in range(S) for n in ("k_force", "k_node", "k_elem")] + ["k_end"]
+
+    def enqueue(self, cycles: int):
+        _check(_lib.fierro_sgh_enqueue_cycles(self.h, cycles))
+
+    def synchronize(self):
+        _check(_lib.fierro_sgh_synchronize(self.h))
+
+    def run_stages(self, stages: int):
+        _check(_lib.fierro_sgh_run_stages(self.h, stages))
+
+    def time(self):
+        t, dt, gt, cyc = C.c_double(), C.c_double(), C.c_double(), C.c_int64()
+        _check(_lib.fierro_sgh_time(self.h, C.byref(t), C.byref(dt), C.byref(gt), C.byref(cyc)))
+        return t.value, dt.value, gt.value, cyc.value
+
+    def energy(self):
+        ie, ke = C.c_double(), C.c_double()
+        _check(_lib.fierro_sgh_energy(self.h, C.byref(ie), C.byref(ke)))
+        return ie.value, ke.value
+
+    @property
+    def launches_per_cycle(self) -> int:
+        return int(_lib.fierro_sgh_launches_per_cycle(self.h))
+
+    @property
+    def device_bytes(self) -> int:
+        return int(_lib.fierro_sgh_device_bytes(self.h))
+
+
+def measure_fp64_rate() -> float:
+    """Measured FP64 fused-multiply-add rate of the current GPU (FMA/s)."""
+    r = C.c_double(0)
+    _check(_lib.fierro_measure_fp64_rate(C.byref(r)))
+    return r.value
+
+
+def compared_fields(st: Dict[str, np.ndarray]) -> Dict[str, np.ndarray]:
+    """The fields parity is judged on (bin 1 = current values), as flat arrays."""
+    return {"coords": st["node_coords"][1], "vel": st["node_vel"][1], "den": st["elem_den"],
+            "pres": st["elem_pres"], "sie": st["elem_sie"][1], "sspd": st["elem_sspd"], "vol": st["elem_vol"]}

@@ -1,0 +1,189 @@
+/* fierro_sgh.h -- C ABI of the GB300-native SGH (staggered-grid hydrodynamics)
+ * Lagrangian cycle for unstructured 3D hexahedral meshes.
+ *
+ * Drop-in boundary for Fierro's Explicit-Lagrange-Kokkos/SGH_solver hot path:
+ * the record types mirror material_t / boundary_t / mat_fill_t
+ * (state.h:130-178, mesh.h:858-935), state arrays use the reference layouts, and
+ * fierro_sgh_solve / fierro_sgh_setup replace sgh_solve / setup
+ * (mesh.h:1175-1208, mesh.h:1006-1028).  Plain pointers and sizes only.
+ *
+ * Reference layouts of state arrays (all host memory, float64 unless noted):
+ *   node_coords, node_vel   [2][num_nodes][3]      (rk bin, node, dim)
+ *   node_mass               [num_nodes]
+ *   elem_den, elem_pres, elem_sspd, elem_vol, elem_div, elem_mass   [num_elems]
+ *   elem_sie                [2][num_elems]
+ *   elem_stress             [2][num_elems][3][3]
+ *   elem_mat_id             [num_elems]            (uint64 = size_t)
+ *   elem_statev             [num_elems][num_state_vars]   statev(0)=gamma, (1)=c_min
+ *   corner_force            [8*num_elems][3]       corner gid = elem*8 + node_lid
+ *   nodes_in_elem           [num_elems][8]         (uint64, 0-based, mesh.h:15-45 order)
+ *
+ * Errors: every call returns FIERRO_OK (0) or a FIERRO_E* code; the library never
+ * exits the process.  fierro_last_error() returns the text of the calling thread's
+ * last error.  A handle is used by one host thread at a time.
+ */
+#ifndef FIERRO_SGH_H
+#define FIERRO_SGH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FIERRO_OK 0
+#define FIERRO_EINVAL 1     /* bad argument, mesh or deck */
+#define FIERRO_ENOMEM 2     /* device or host allocation failed */
+#define FIERRO_ECUDA 3      /* CUDA runtime error */
+#define FIERRO_ENUMERIC 4   /* non-positive volume or non-finite state detected */
+#define FIERRO_ETIMEDOUT 5  /* a bounded device wait gave up */
+#define FIERRO_ENOTSUP 6    /* valid in the reference but outside this path */
+
+/* Arithmetic modes of the device kernels. */
+#define FIERRO_FP_EXACT 0   /* reference operation order, no contraction: doubles
+                               match the reference's uncontracted evaluation */
+#define FIERRO_FP_FMA 1     /* same schedule with fused multiply-adds and
+                               reciprocal reuse (differs in the last bits) */
+
+/* material_t (state.h:130-178).  eos_model 0 = ideal_gas (eos.cpp:12);
+ * strength_type must be 0 (model::none). */
+typedef struct {
+  int eos_model;
+  int strength_type;
+  double q1, q1ex, q2, q2ex;
+} fierro_material;
+
+/* boundary_t (mesh.h:924-935).  surface: 0 x-plane, 1 y-plane, 2 z-plane,
+ * 3 cylinder, 4 sphere.  hydro_bc: 0 fixed, 1 reflected (planes only). */
+typedef struct {
+  int surface;
+  double value;
+  int hydro_bc;
+} fierro_boundary;
+
+/* mat_fill_t (mesh.h:858-890).  volume: 0 global, 1 box, 2 cylinder, 3 sphere.
+ * velocity: 0 cartesian, 1 radial, 2 spherical, 5 tg_vortex. */
+typedef struct {
+  int volume;
+  int mat_id;
+  double x1, x2, y1, y2, z1, z2;
+  double radius1, radius2;
+  int velocity;
+  double u, v, w, speed, sie, den;
+} fierro_mat_fill;
+
+/* The scalar controls of sgh_solve (mesh.h:1175-1208; defaults driver.cpp:35-62). */
+typedef struct {
+  double time_final, dt_max, dt_min, dt_cfl, dt_start;
+  double graphics_dt_ival;
+  int64_t graphics_cyc_ival;
+  int64_t cycle_stop;
+  int64_t rk_num_stages;
+  double fuzz, tiny, small;
+} fierro_sgh_params;
+
+/* Mesh: num_nodes, num_elems and nodes_in_elem (mesh_t, mesh.h:68-817) plus the
+ * initial coordinates [num_nodes][3] (node_coords bin 1 after read_mesh_ensight). */
+typedef struct {
+  int64_t num_nodes;
+  int64_t num_elems;
+  const uint64_t* nodes_in_elem;
+  const double* coords;
+} fierro_mesh;
+
+/* Host state in the reference layouts (see top of file).  For set_state the
+ * fields marked (in) are required; for get_state any NULL field is skipped. */
+typedef struct {
+  double* node_coords;   /* (in) [2][Nn][3] */
+  double* node_vel;      /* (in) [2][Nn][3] */
+  double* node_mass;     /* (in) [Nn] */
+  double* elem_den;      /* (in) [Ne] */
+  double* elem_pres;     /* (in) [Ne] */
+  double* elem_stress;   /* [2][Ne][3][3]; must be zero (no strength model) */
+  double* elem_sspd;     /* (in) [Ne] */
+  double* elem_sie;      /* (in) [2][Ne] */
+  double* elem_vol;      /* (in) [Ne] */
+  double* elem_div;      /* [Ne] (recomputed by the first stage) */
+  double* elem_mass;     /* (in) [Ne] */
+  uint64_t* elem_mat_id; /* (in) [Ne] */
+  double* elem_statev;   /* (in) [Ne][num_state_vars] */
+  double* corner_force;  /* [8Ne][3] (output of the last stage) */
+  int64_t num_state_vars;
+} fierro_sgh_state;
+
+typedef struct fierro_sgh fierro_sgh;
+
+/* Text of the calling thread's last error ("" if none). */
+const char* fierro_last_error(void);
+/* Library version string. */
+const char* fierro_version(void);
+
+/* setup (setup.cpp:10-424) with get_vol first (driver.cpp:239), on the host:
+ * boundary tagging, fills, EOS, velocity ICs, BCs and node mass.  Writes the
+ * initial state (bin 1 and bin 0 as the reference leaves them) into `out`.
+ * state_vars is [num_materials][num_state_vars]. */
+int fierro_sgh_setup(const fierro_mesh* mesh, const fierro_material* materials, int64_t num_materials,
+                     const double* state_vars, int64_t num_state_vars,
+                     const fierro_mat_fill* fills, int64_t num_fills,
+                     const fierro_boundary* boundaries, int64_t num_bcs, fierro_sgh_state* out);
+
+/* sgh_solve (sgh_solve.cpp:8-692): run the cycle loop on the GPU from the state
+ * in `state` (host, reference layouts) and write the final state back.  On
+ * entry *time_value, *graphics_time and dt are the loop's starting values; on
+ * return *time_value and *graphics_time hold the final ones and, when non-NULL,
+ * *cycles_run the number of cycles executed.  Host<->device copies are part of
+ * the call.  fp_mode is FIERRO_FP_EXACT or FIERRO_FP_FMA. */
+int fierro_sgh_solve(const fierro_mesh* mesh, const fierro_material* materials, int64_t num_materials,
+                     const fierro_boundary* boundaries, int64_t num_bcs, fierro_sgh_state* state,
+                     double* time_value, double time_final, double dt_max, double dt_min, double dt_cfl,
+                     double* graphics_time, int64_t graphics_cyc_ival, double graphics_dt_ival,
+                     int64_t cycle_stop, int64_t rk_num_stages, double dt, double fuzz, double tiny,
+                     double small, int fp_mode, int64_t* cycles_run);
+
+/* ---- persistent handle: device-resident mesh and state ---------------------
+ * create: builds the device mesh (Morton-renumbered; reference summation orders
+ * kept), boundary node sets and materials.  stream may be NULL (the handle then
+ * owns a stream) or a cudaStream_t the caller owns. */
+int fierro_sgh_create(const fierro_mesh* mesh, const fierro_material* materials, int64_t num_materials,
+                      const fierro_boundary* boundaries, int64_t num_bcs, const fierro_sgh_params* params,
+                      int fp_mode, void* stream, fierro_sgh** out);
+int fierro_sgh_destroy(fierro_sgh* h);
+/* Upload a state (reference layouts) and reset time_value=0, dt=dt_start,
+ * graphics_time=graphics_dt_ival, cycle=0. */
+int fierro_sgh_set_state(fierro_sgh* h, const fierro_sgh_state* state);
+int fierro_sgh_get_state(fierro_sgh* h, fierro_sgh_state* state);
+/* Enqueue up to `cycles` cycles on the handle's stream without waiting.  The
+ * loop stops by itself once time_value reaches time_final (the remaining
+ * enqueued cycles do nothing). */
+int fierro_sgh_enqueue_cycles(fierro_sgh* h, int64_t cycles);
+/* Run `cycles` cycles and wait; *cycles_run (if non-NULL) = cycles executed. */
+int fierro_sgh_run(fierro_sgh* h, int64_t cycles, int64_t* cycles_run);
+/* Run single RK stages (a stage at a cycle start first computes dt). */
+int fierro_sgh_run_stages(fierro_sgh* h, int64_t stages);
+int fierro_sgh_synchronize(fierro_sgh* h);
+/* Loop scalars: time_value, dt of the last cycle, graphics_time, cycles done. */
+int fierro_sgh_time(fierro_sgh* h, double* time_value, double* dt, double* graphics_time, int64_t* cycle);
+/* Energy tallies of sgh_solve.cpp:77-101: IE = sum M e, KE = 1/2 sum m |v|^2
+ * (deterministic device reductions). */
+int fierro_sgh_energy(fierro_sgh* h, double* ie, double* ke);
+/* Run `cycles` cycles with a CUDA event recorded after every launch and wait.
+ * kernel_ms[i] (array of fierro_sgh_launches_per_cycle entries, may be NULL)
+ * receives the device time summed over the cycles of launch slot i of a cycle
+ * (slot 0 = dt, then force/node/elem per stage, last = end-of-cycle); *total_ms
+ * receives the device time from the first launch to the last.  Same results as
+ * fierro_sgh_run. */
+int fierro_sgh_run_timed(fierro_sgh* h, int64_t cycles, float* kernel_ms, float* total_ms, int64_t* cycles_run);
+/* Number of kernel launches one cycle enqueues (for launch accounting). */
+int64_t fierro_sgh_launches_per_cycle(const fierro_sgh* h);
+/* Bytes of device memory the handle holds. */
+int64_t fierro_sgh_device_bytes(const fierro_sgh* h);
+
+/* FP64 roof calibration on the current device: dependent-chain-free DFMA
+ * throughput, in fused multiply-adds per second (one FMA = 2 FLOP). */
+int fierro_measure_fp64_rate(double* dfma_per_second);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FIERRO_SGH_H */

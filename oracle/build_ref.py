@@ -1,8 +1,9 @@
 """Build recipe for the oracle side (test infrastructure only).
 
-Two products, both written only under oracle/_ref/ (git-ignored):
+Products, all written only under oracle/_ref/ (git-ignored):
 
-* liborc_sgh.so -- the plain-C restatement in oracle/sgh_oracle.c, compiled with
+* liborc_sgh.so, liborc_sgh_crpow.so -- the plain-C restatement in oracle/sgh_oracle.c
+  (libm pow, and a correctly rounded pow variant), compiled with
   -ffp-contract=off so its doubles follow the reference's uncontracted evaluation.
 * fierro_ref / fierro_ref_geo / fierro_ref_fast -- the reference's own SGH solver
   (Explicit-Lagrange-Kokkos/SGH_solver/*.cpp, unmodified) compiled with g++ -fopenmp
@@ -54,16 +55,18 @@ def _newer(target, deps):
 
 
 def build_oracle_lib(verbose=False):
-    """Compile oracle/sgh_oracle.c into oracle/_ref/liborc_sgh.so."""
+    """Compile oracle/sgh_oracle.c into oracle/_ref/liborc_sgh.so (libm pow, as the
+    reference) and oracle/_ref/liborc_sgh_crpow.so (correctly rounded pow)."""
     os.makedirs(OUT, exist_ok=True)
     src = os.path.join(HERE, "sgh_oracle.c")
     hdr = os.path.join(HERE, "sgh_oracle.h")
-    lib = os.path.join(OUT, "liborc_sgh.so")
-    if _newer(lib, [src, hdr, __file__]):
-        return lib
-    _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-          "-o", lib, src, "-lm"])
-    return lib
+    libs = {"liborc_sgh.so": [], "liborc_sgh_crpow.so": ["-DORC_CR_POW"]}
+    for name, extra in libs.items():
+        lib = os.path.join(OUT, name)
+        if not _newer(lib, [src, hdr, __file__]):
+            _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off"] + extra +
+                 ["-o", lib, src, "-lm"])
+    return os.path.join(OUT, "liborc_sgh.so")
 
 
 def _source_dir():

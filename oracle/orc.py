@@ -47,15 +47,18 @@ class OrcParams(C.Structure):
         [(k, C.c_double) for k in ("fuzz", "tiny", "small")]
 
 
-_lib = None
+_libs = {}
+VARIANTS = {"libm": "liborc_sgh.so", "crpow": "liborc_sgh_crpow.so"}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        path = os.path.join(REF_DIR, "liborc_sgh.so")
+def lib(variant: str = "libm"):
+    """The oracle library: 'libm' calls libm pow like the reference; 'crpow' uses
+    a correctly rounded pow(vol, 1/3) (see oracle/sgh_oracle.c)."""
+    if variant not in _libs:
+        path = os.path.join(REF_DIR, VARIANTS[variant])
         if not os.path.exists(path):
-            from . import build_ref  # noqa: F401  (package-relative when imported as oracle.orc)
+            from oracle import build_ref
+            build_ref.build_oracle_lib()
         _lib = C.CDLL(path)
         _lib.orc_create.restype = C.c_void_p
         _lib.orc_create.argtypes = [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p]
@@ -77,7 +80,8 @@ def lib():
         _lib.orc_bmatrix.argtypes = [C.c_void_p] * 4
         _lib.orc_vol_hex.restype = C.c_double
         _lib.orc_vol_hex.argtypes = [C.c_void_p] * 3
-    return _lib
+        _libs[variant] = _lib
+    return _libs[variant]
 
 
 def make_params(p) -> OrcParams:
@@ -88,9 +92,10 @@ def make_params(p) -> OrcParams:
 class Oracle:
     """One problem instance in the C restatement."""
 
-    def __init__(self, problem, setup=True):
+    def __init__(self, problem, setup=True, variant: str = "libm"):
         from fierro_gb300.problems import REGION, VELOCITY, SURFACE, HYDRO_BC
-        L = lib()
+        self.variant = variant
+        L = lib(variant)
         m = problem.mesh
         self.nn, self.ne = m.num_nodes, m.num_elems
         self._nie = np.ascontiguousarray(m.nodes_in_elem, dtype=np.int64)
@@ -118,19 +123,22 @@ class Oracle:
                 raise ValueError("oracle setup failed")
         L.orc_init_time(self.h, C.byref(self.params))
 
+    def _L(self):
+        return lib(self.variant)
+
     def __del__(self):
         if getattr(self, "h", None):
-            lib().orc_destroy(self.h)
+            self._L().orc_destroy(self.h)
             self.h = None
 
     def run_cycles(self, n: int) -> int:
-        return int(lib().orc_run_cycles(self.h, C.byref(self.params), n))
+        return int(self._L().orc_run_cycles(self.h, C.byref(self.params), n))
 
     def run_stages(self, n: int) -> int:
-        return int(lib().orc_run_stages(self.h, C.byref(self.params), n))
+        return int(self._L().orc_run_stages(self.h, C.byref(self.params), n))
 
     def get(self, which: int) -> np.ndarray:
-        L = lib()
+        L = self._L()
         n = L.orc_get(self.h, which, None) if which != ORC_BDY_NODE_MASK else self.nn
         dt = np.int32 if which == ORC_BDY_NODE_MASK else (np.int64 if which == ORC_ELEM_MAT_ID else np.float64)
         out = np.empty(n, dtype=dt)
@@ -139,16 +147,16 @@ class Oracle:
 
     def set(self, which: int, arr: np.ndarray) -> None:
         a = np.ascontiguousarray(arr)
-        lib().orc_set(self.h, which, a.ctypes.data)
+        self._L().orc_set(self.h, which, a.ctypes.data)
 
     def energy(self):
         ie, ke = C.c_double(), C.c_double()
-        lib().orc_energy(self.h, C.byref(ie), C.byref(ke))
+        self._L().orc_energy(self.h, C.byref(ie), C.byref(ke))
         return ie.value, ke.value
 
     def time(self):
         t, dt, gt, cyc = C.c_double(), C.c_double(), C.c_double(), C.c_int64()
-        lib().orc_time(self.h, C.byref(t), C.byref(dt), C.byref(gt), C.byref(cyc))
+        self._L().orc_time(self.h, C.byref(t), C.byref(dt), C.byref(gt), C.byref(cyc))
         return t.value, dt.value, gt.value, cyc.value
 
     def state(self) -> dict:
@@ -214,7 +222,7 @@ def read_state_dump(path: str) -> dict:
 
 
 def run_reference(problem, cycles: int | None = None, kind: str = "fierro_ref", threads: int | None = None,
-                  geo_path: str | None = None, workdir: str | None = None) -> dict:
+                  geo_path: str | None = None, workdir: str | None = None, warmup: int = 0) -> dict:
     """Run the reference executable on the deck; returns the final state plus
     'calc_seconds' (the reference's own cycle-loop timer, sgh_solve.cpp:637-641)."""
     from fierro_gb300.mesh import write_mesh_bin
@@ -238,6 +246,8 @@ def run_reference(problem, cycles: int | None = None, kind: str = "fierro_ref", 
         env = dict(os.environ)
         if threads:
             env["OMP_NUM_THREADS"] = str(threads)
+        if warmup:
+            env["FIERRO_REF_WARMUP"] = str(int(warmup))
         env.setdefault("OMP_PROC_BIND", "spread")
         env.setdefault("OMP_PLACES", "cores")
         p = subprocess.run([exe, cfg, mesh_path, out], stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
@@ -245,8 +255,8 @@ def run_reference(problem, cycles: int | None = None, kind: str = "fierro_ref", 
         if p.returncode != 0:
             raise RuntimeError("reference run failed:\n" + p.stdout[-4000:])
         st = read_state_dump(out)
-    m = re.search(r"Calculation time in seconds:\s*([0-9.eE+-]+)", p.stdout)
-    st["calc_seconds"] = float(m.group(1)) if m else float("nan")
+    ms = re.findall(r"Calculation time in seconds:\s*([0-9.eE+-]+)", p.stdout)
+    st["calc_seconds"] = float(ms[-1]) if ms else float("nan")
     m = re.search(r"Setup time in seconds:\s*([0-9.eE+-]+)", p.stdout)
     st["setup_seconds"] = float(m.group(1)) if m else float("nan")
     st["stdout"] = p.stdout

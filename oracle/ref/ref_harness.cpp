@@ -3,9 +3,10 @@
 // connectivity, dual views, get_vol, setup, sgh_solve) followed by a binary dump
 // of the final state.  It also supplies write_outputs (outputs.cpp:10-78) as a
 // no-op, since graphics dumps are outside the measured path.  Linked only into
-// the reference oracle executables built by oracle/build_ref.sh.
+// the reference oracle executables built by oracle/build_ref.py.
 //
 // usage: fierro_ref <config.txt> <mesh.geo|mesh.bin> <state_out.bin>
+// env FIERRO_REF_WARMUP=W runs W untimed cycles first (see main).
 // The dump (little endian): "FSGHSTAT", u64 num_nodes, u64 num_elems,
 // f64 time_value, then f64 arrays node_coords[2][Nn][3], node_vel[2][Nn][3],
 // node_mass[Nn], elem_den[Ne], elem_pres[Ne], elem_sspd[Ne], elem_sie[2][Ne],
@@ -102,6 +103,18 @@ int main(int argc, char* argv[]) {
     graphics_id = 0;
     graphics_times(0) = 0.0;
     graphics_time = graphics_dt_ival;
+
+    // optional untimed warm-up cycles (FIERRO_REF_WARMUP=W): a first sgh_solve call of
+    // W cycles, after which the deck's cycle_stop cycles run as a second call whose
+    // printed "Calculation time" is the timed one
+    const char* warm = std::getenv("FIERRO_REF_WARMUP");
+    const size_t warm_cycles = warm ? (size_t)std::strtoull(warm, nullptr, 10) : 0;
+    if (warm_cycles > 0)
+      sgh_solve(material, boundary, mesh, node_coords, node_vel, node_mass, elem_den, elem_pres,
+                elem_stress, elem_sspd, elem_sie, elem_vol, elem_div, elem_mass, elem_mat_id,
+                elem_statev, corner_force, corner_mass, time_value, time_final, dt_max, dt_min, dt_cfl,
+                graphics_time, graphics_cyc_ival, graphics_dt_ival, warm_cycles, rk_num_stages, dt, fuzz,
+                tiny, small, graphics_times, graphics_id);
 
     sgh_solve(material, boundary, mesh, node_coords, node_vel, node_mass, elem_den, elem_pres,
               elem_stress, elem_sspd, elem_sie, elem_vol, elem_div, elem_mass, elem_mat_id,

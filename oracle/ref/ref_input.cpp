@@ -1,7 +1,7 @@
 // Config-driven replacement for Explicit-Lagrange-Kokkos/SGH_solver/input.cpp,
 // the same input-swap mechanism the reference's own
 // tests-for-Explicit-Lagrange-Kokkos/input_for_*.cpp files use.  Linked only into
-// the reference oracle build (oracle/build_ref.sh), never into the library.
+// the reference oracle build (oracle/build_ref.py), never into the library.
 //
 // The problem is read from the text file named by fierro_ref_config_path:
 //   <key> <value>                    scalar controls (dt_start, time_final, ...)

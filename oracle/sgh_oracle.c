@@ -4,7 +4,7 @@
  * TEST INFRASTRUCTURE ONLY: the checker for the GB300 library, never part of it.
  * Build with -ffp-contract=off so every double matches the reference's
  * uncontracted evaluation.  Parity of this file against the reference itself
- * (compiled from its own sources by oracle/build_ref.sh) is pinned by
+ * (compiled from its own sources by oracle/build_ref.py) is pinned by
  * tests/test_oracle_ref.py and the fixtures in tests/golden/.
  */
 #include "sgh_oracle.h"
@@ -90,6 +90,44 @@ double orc_vol_hex(const double x[8], const double y[8], const double z[8]) {
     vol = (a == 0) ? x[i] * inner : vol + x[i] * inner;
   }
   return vol * twelth;
+}
+
+/* The Mach detector's pow(vol, 1.0/3.0) (force_sgh.cpp:319-320).  The default
+ * build calls libm pow, as the reference does.  With -DORC_CR_POW it is the
+ * correctly rounded vol^fl(1/3) instead: the exponent is 1/3 - d with
+ * d = 2^-54/3, so vol^fl(1/3) = cbrt(vol) (1 - d ln vol + ...); one Newton step on
+ * t^3 = vol with an error-free residual plus the -d ln vol term refine cbrt's
+ * result to well below an ulp before the final rounding.  glibc's pow is not
+ * correctly rounded for about 0.1% of arguments; this variant isolates that
+ * libm rounding from the rest of the arithmetic. */
+static double orc_pow_third(double v) {
+#ifdef ORC_CR_POW
+  if (!(v > 1.0e-290 && v < 1.0e290)) return pow(v, 1.0 / 3.0);
+  const double c0 = cbrt(v);
+  const double p = c0 * c0;
+  const double pe = fma(c0, c0, -p);
+  const double q = p * c0;
+  const double qe = fma(p, c0, -q) + pe * c0;
+  const double r = (v - q) - qe;
+  const double step = r / (3.0 * p);
+  int ex = 0;
+  const double m = frexp(v, &ex);
+  const double lnv = (double)ex * 0.6931471805599453 + log(m);
+  const double lo = step - c0 * (lnv * 1.8503717077085943e-17);
+  return c0 + lo;
+#else
+  return pow(v, 1.0 / 3.0);
+#endif
+}
+
+/* The CFL distance's pow(d, 2.0) (time_integration.cpp:107-109): libm pow by
+ * default, the IEEE square d*d (correctly rounded) with -DORC_CR_POW. */
+static double orc_pow2(double d) {
+#ifdef ORC_CR_POW
+  return d * d;
+#else
+  return pow(d, 2.0);
+#endif
 }
 
 /* ------------------------------------------------------------------------- */
@@ -473,8 +511,8 @@ static void get_timestep(orc_sim* s, const orc_params* p) {
       double dist[28];
       int a = 0, b = 1, loop = 0;
       for (int i = 0; i < 28; ++i) {
-        dist[i] = fabs(sqrt(pow((c[b][0] - c[a][0]), 2.0) + pow((c[b][1] - c[a][1]), 2.0) +
-                            pow((c[b][2] - c[a][2]), 2.0)));
+        dist[i] = fabs(sqrt(orc_pow2(c[b][0] - c[a][0]) + orc_pow2(c[b][1] - c[a][1]) +
+                            orc_pow2(c[b][2] - c[a][2])));
         b++;
         a++;
         if (b > 7) {
@@ -590,8 +628,8 @@ static void get_force_sgh(orc_sim* s, const orc_params* p) {
     }
     double phi = 1.0 - fmax(0.0, r_min);
     phi = pow(phi, n_coef);
-    double omega = 20.0, third = 1.0 / 3.0;
-    double c_length = pow(vol, third);
+    double omega = 20.0;
+    double c_length = orc_pow_third(vol);
     double alpha = fmin(1.0, omega * (c_length * fabs(div)) / (s->sspd[e] + fuzz));
     phi = alpha * phi;
     for (int l = 0; l < 8; ++l) {

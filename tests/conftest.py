@@ -1,0 +1,63 @@
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+REFERENCE_MESHES = "/root/reference/Explicit-Lagrange/meshes"
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the libfierro_sgh kernels)")
+
+
+def field_error(got: np.ndarray, ref: np.ndarray, floor: float = 1e-3) -> float:
+    """Pointwise relative error with an absolute floor for near-zero values:
+    max |got - ref| / max(|ref|, floor * max|ref|).  Values smaller than `floor`
+    times the field's peak magnitude are compared at that scale."""
+    got = np.asarray(got, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    scale = float(np.max(np.abs(ref))) if ref.size else 0.0
+    if scale == 0.0:
+        return float(np.max(np.abs(got))) if got.size else 0.0
+    return float(np.max(np.abs(got - ref) / np.maximum(np.abs(ref), floor * scale)))
+
+
+def assert_fields(got: dict, ref: dict, tol: float, keys=("coords", "vel", "den", "pres", "sie"),
+                  floor: float = 1e-3, label: str = ""):
+    bad = {}
+    for k in keys:
+        e = field_error(got[k], ref[k], floor)
+        if not e <= tol:
+            bad[k] = e
+    assert not bad, "%s: fields over tolerance %g: %s" % (label, tol, bad)
+
+
+def assert_bitwise(got: dict, ref: dict, keys, label: str = ""):
+    bad = {k: int(np.sum(np.asarray(got[k]) != np.asarray(ref[k]))) for k in keys}
+    bad = {k: v for k, v in bad.items() if v}
+    assert not bad, "%s: values differing bit-for-bit: %s" % (label, bad)
+
+
+def load_golden(name: str) -> dict:
+    with np.load(os.path.join(GOLDEN, name + ".npz")) as z:
+        return {k: z[k] for k in z.files}
+
+
+@pytest.fixture(scope="session")
+def oracle_built():
+    from oracle import build_ref
+    build_ref.build_oracle_lib()
+    return True
+
+
+@pytest.fixture(scope="session")
+def lib_built():
+    from fierro_gb300 import build
+    build.build()
+    return True

@@ -1,0 +1,135 @@
+"""GPU checks of the C ABI's behaviour: one-shot sgh_solve equals the handle path,
+graph replay equals stage stepping and event-timed runs, state round trips,
+stopping at time_final, and error reporting (including a device-detected
+inverted element, after which the context stays usable)."""
+import numpy as np
+import pytest
+
+from conftest import assert_bitwise
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("coords", "vel", "den", "pres", "sie", "sspd", "vol")
+
+
+def _prob():
+    from fierro_gb300 import problems
+    return problems.sedov(10, jitter=0.1, seed=4, permute=True, cycles=25)
+
+
+def test_set_get_roundtrip(lib_built):
+    from fierro_gb300 import sgh
+    prob = _prob()
+    st = sgh.setup(prob)
+    with sgh.SGHSolver(prob) as s:
+        s.set_state(st)
+        back = s.get_state()
+    for k in ("node_coords", "node_vel", "node_mass", "elem_den", "elem_pres", "elem_sspd", "elem_sie",
+              "elem_vol", "elem_mass"):
+        assert np.array_equal(back[k], st[k]), k
+
+
+def test_one_shot_solve_equals_handle(lib_built):
+    from fierro_gb300 import sgh
+    prob = _prob()
+    st = sgh.setup(prob)
+    one = {k: v.copy() for k, v in st.items()}
+    info = sgh.sgh_solve(prob, one, cycle_stop=25)
+    with sgh.SGHSolver(prob) as s:
+        s.set_state(st)
+        assert s.run(25) == 25
+        h = s.get_state()
+        t = s.time()
+    assert info["cycles"] == 25 and info["time_value"] == t[0]
+    a, b = sgh.compared_fields(one), sgh.compared_fields(h)
+    assert_bitwise(a, b, FIELDS)
+    assert np.array_equal(one["corner_force"], h["corner_force"])
+
+
+def test_graph_stage_and_timed_paths_agree(lib_built):
+    from fierro_gb300 import sgh
+    prob = _prob()
+    st = sgh.setup(prob)
+    outs = []
+    for how in ("graph", "stages", "timed"):
+        with sgh.SGHSolver(prob) as s:
+            s.set_state(st)
+            if how == "graph":
+                s.run(7)
+            elif how == "stages":
+                s.run_stages(14)
+            else:
+                ran, tot, kms = s.run_timed(7)
+                assert ran == 7 and tot > 0 and len(kms) == s.launches_per_cycle
+            outs.append(sgh.compared_fields(s.get_state()))
+            assert s.time()[3] == 7
+    assert_bitwise(outs[0], outs[1], FIELDS, "graph vs stages")
+    assert_bitwise(outs[0], outs[2], FIELDS, "graph vs timed")
+
+
+def test_stops_at_time_final(lib_built, oracle_built):
+    from fierro_gb300 import problems, sgh
+    from oracle import orc
+    prob = problems.noh(8, cycles=10 ** 6)
+    prob.params.time_final = 0.05
+    st = sgh.setup(prob)
+    with sgh.SGHSolver(prob) as s:
+        s.set_state(st)
+        ran = s.run(2000)
+        t = s.time()
+        out = sgh.compared_fields(s.get_state())
+    o = orc.Oracle(prob, variant="crpow")
+    n = o.run_cycles(2000)
+    assert ran == n and t[0] == 0.05 == o.time()[0]
+    assert_bitwise(out, o.state(), FIELDS, "noh8 to time_final")
+
+
+def test_error_codes(lib_built):
+    from fierro_gb300 import sgh
+    prob = _prob()
+    st = sgh.setup(prob)
+    with sgh.SGHSolver(prob) as s:
+        with pytest.raises(sgh.FierroError) as ei:
+            s.run(1)  # before set_state
+        assert ei.value.code == sgh.FIERRO_EINVAL
+        bad = {k: v.copy() for k, v in st.items()}
+        bad["elem_vol"][3] = -1.0
+        with pytest.raises(sgh.FierroError) as ei:
+            s.set_state(bad)
+        assert ei.value.code == sgh.FIERRO_ENUMERIC
+        bad = {k: v.copy() for k, v in st.items()}
+        bad["elem_stress"][1, 2, 0, 1] = 1.0
+        with pytest.raises(sgh.FierroError) as ei:
+            s.set_state(bad)
+        assert ei.value.code == sgh.FIERRO_ENOTSUP
+        bad = {k: v.copy() for k, v in st.items()}
+        bad["elem_mat_id"][0] = 7
+        with pytest.raises(sgh.FierroError) as ei:
+            s.set_state(bad)
+        assert ei.value.code == sgh.FIERRO_EINVAL
+
+
+def test_device_detects_inverted_element_and_recovers(lib_built):
+    """A velocity field that crushes one element inverts it within a cycle: the
+    element kernel flags it, run() returns ENUMERIC, and the same handle then
+    runs a valid state normally (the status is a flag, never a trap)."""
+    from fierro_gb300 import sgh
+    prob = _prob()
+    prob.params.dt_start = 1e-2
+    prob.params.dt_min = 1e-2
+    st = sgh.setup(prob)
+    bad = {k: v.copy() for k, v in st.items()}
+    e = 200
+    nodes = prob.mesh.nodes_in_elem[e]
+    cen = prob.mesh.coords[nodes].mean(axis=0)
+    for n in nodes:
+        bad["node_vel"][1, n] = -500.0 * (prob.mesh.coords[n] - cen)
+    with sgh.SGHSolver(prob) as s:
+        s.set_state(bad)
+        with pytest.raises(sgh.FierroError) as ei:
+            s.run(3)
+        assert ei.value.code == sgh.FIERRO_ENUMERIC
+        s.set_state(st)
+        assert s.run(2) == 2
+        out = s.get_state()
+        assert np.all(out["elem_vol"] > 0)
