@@ -5,7 +5,7 @@ U(-0.1h, 0.1h) per axis from a seed, element and node ids randomly permuted,
 gamma = 1.4, origin-corner energy 0.2467, CFL 0.4).  A step is one SGH cycle
 (two RK stages) over the whole mesh.
 
-Prints one JSON line (see the design doc for every key).  Default: 1 GPU, 20 timed
+Prints one JSON line.  Default: 1 GPU, 20 timed
 cycles after 3 warm-up cycles.  Under torchrun (N > 1) every rank advances its own
 replica (the path is run as independent replicas, no collective in the data
 path); value = all ranks' element-cycles / max-over-ranks time.

@@ -45,7 +45,8 @@ struct fierro_sgh {
   double* d_x[2][3] = {};
   double* d_v[2][3] = {};
   double* d_h[3] = {};
-  double *d_den = nullptr, *d_pres = nullptr, *d_sspd = nullptr, *d_vol = nullptr, *d_div = nullptr;
+  double *d_den = nullptr, *d_pres = nullptr, *d_sspd = nullptr, *d_vol = nullptr;
+  double* d_div[2] = {};  // see sgh_device.h: read by stage parity q, written at q^1
   double* d_sie[2] = {};
   double *d_bmat = nullptr, *d_force = nullptr;
   long long* d_cfl = nullptr;
@@ -131,7 +132,7 @@ int check_status(fierro_sgh* h) {
 // Bins at a cycle boundary after `done` executed cycles: state bin and start bin.
 int bin_now(const fierro_sgh* h, long long cycles_done) { return (int)((h->base + cycles_done) & 1); }
 
-ForceArgs force_args(fierro_sgh* h, int rb) {
+ForceArgs force_args(fierro_sgh* h, int rb, int q) {
   ForceArgs a{};
   a.ne = (int)h->ne;
   a.nie = h->d_nie;
@@ -147,7 +148,7 @@ ForceArgs force_args(fierro_sgh* h, int rb) {
   a.pres = h->d_pres;
   a.sspd = h->d_sspd;
   a.vol = h->d_vol;
-  a.div = h->d_div;
+  a.div = h->d_div[q];
   a.force = h->d_force;
   a.ctrl = h->d_ctrl;
   a.fuzz = h->lp.fuzz;
@@ -184,7 +185,7 @@ NodeArgs node_args(fierro_sgh* h, int c, double alpha) {
   return a;
 }
 
-ElemArgs elem_args(fierro_sgh* h, int cur_bin, int c, double alpha) {
+ElemArgs elem_args(fierro_sgh* h, int cur_bin, int c, double alpha, int div_out) {
   ElemArgs a{};
   a.ne = (int)h->ne;
   a.nie = h->d_nie;
@@ -207,7 +208,7 @@ ElemArgs elem_args(fierro_sgh* h, int cur_bin, int c, double alpha) {
   a.pres = h->d_pres;
   a.sspd = h->d_sspd;
   a.vol = h->d_vol;
-  a.div = h->d_div;
+  a.div = h->d_div[div_out];
   a.bmat = h->d_bmat;
   a.cfl_part = h->d_cfl;
   a.ctrl = h->d_ctrl;
@@ -221,13 +222,18 @@ double stage_alpha(const fierro_sgh* h, int s) {
   return 1.0 / ((double)h->rk_num_stages - (double)s);  // sgh_solve.cpp:353
 }
 
+// Divergence buffer a stage reads: the parity of the number of stages run since
+// set_state, which for stage s of a cycle with bin parity c is (c*S + s) & 1.
+int div_parity(const fierro_sgh* h, int c, int s) { return (c * h->rk_num_stages + s) & 1; }
+
 // Stage s of a cycle whose start state is in bin c.
 void enqueue_stage(fierro_sgh* h, int c, int s) {
   const double alpha = stage_alpha(h, s);
   const int rb = (s == 0) ? c : (c ^ 1);
-  h->ks->force(force_args(h, rb), h->stream);
+  const int q = div_parity(h, c, s);
+  h->ks->force(force_args(h, rb, q), h->stream);
   h->ks->node(node_args(h, c, alpha), h->stream);
-  h->ks->elem(elem_args(h, c ^ 1, c, alpha), (s == h->rk_num_stages - 1) ? 1 : 0, h->stream);
+  h->ks->elem(elem_args(h, c ^ 1, c, alpha, q ^ 1), (s == h->rk_num_stages - 1) ? 1 : 0, h->stream);
 }
 
 void enqueue_dt(fierro_sgh* h) {
@@ -339,7 +345,8 @@ static int create_impl(fierro_sgh* h, const fierro_mesh* mesh, const fierro_mate
   TRY(dalloc(h, &h->d_pres, ne));
   TRY(dalloc(h, &h->d_sspd, ne));
   TRY(dalloc(h, &h->d_vol, ne));
-  TRY(dalloc(h, &h->d_div, ne));
+  TRY(dalloc(h, &h->d_div[0], ne));
+  TRY(dalloc(h, &h->d_div[1], ne));
   TRY(dalloc(h, &h->d_sie[0], ne));
   TRY(dalloc(h, &h->d_sie[1], ne));
   TRY(dalloc(h, &h->d_bmat, ne * 24));
@@ -438,7 +445,9 @@ static int set_state_impl(fierro_sgh* h, const fierro_sgh_state* s, double time_
   std::vector<int32_t> mat((size_t)ne);
   for (int64_t e = 0; e < ne; ++e) mat[e] = (int32_t)s->elem_mat_id[t.elem_int2ext[e]];
   TRY(upload_raw(h, h->d_mat, mat.data(), sizeof(int32_t) * (size_t)ne));
-  if (s->elem_div) TRY(upload_gather(h, h->d_div, s->elem_div, t.elem_int2ext, 1, 0, &slot));
+  // the caller's elem_div is what the reference shows before any stage runs
+  if (s->elem_div) TRY(upload_gather(h, h->d_div[1], s->elem_div, t.elem_int2ext, 1, 0, &slot));
+  else CUDA_TRY(cudaMemsetAsync(h->d_div[1], 0, sizeof(double) * (size_t)ne, h->stream));
   Ctrl c{};
   c.dt = dt;
   c.time_value = time_value;
@@ -448,7 +457,7 @@ static int set_state_impl(fierro_sgh* h, const fierro_sgh_state* s, double time_
   h->enq_cycles = 0;
   h->stage = 0;
   // prime: corner normals, divergence and CFL partials of the uploaded state
-  h->ks->elem(elem_args(h, 0, 0, 1.0), 2, h->stream);
+  h->ks->elem(elem_args(h, 0, 0, 1.0, 0), 2, h->stream);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   h->has_state = true;
@@ -497,7 +506,12 @@ extern "C" int fierro_sgh_get_state(fierro_sgh* h, fierro_sgh_state* s) {
   if (s->elem_pres) TRY(download_scatter(h, s->elem_pres, h->d_pres, t.elem_int2ext, 1, 0));
   if (s->elem_sspd) TRY(download_scatter(h, s->elem_sspd, h->d_sspd, t.elem_int2ext, 1, 0));
   if (s->elem_vol) TRY(download_scatter(h, s->elem_vol, h->d_vol, t.elem_int2ext, 1, 0));
-  if (s->elem_div) TRY(download_scatter(h, s->elem_div, h->d_div, t.elem_int2ext, 1, 0));
+  if (s->elem_div) {
+    // the divergence the last executed stage used (reference elem_div)
+    const long long stages_done = cyc * h->rk_num_stages + h->stage;
+    const int qb = stages_done == 0 ? 1 : (int)((stages_done - 1) & 1);
+    TRY(download_scatter(h, s->elem_div, h->d_div[qb], t.elem_int2ext, 1, 0));
+  }
   if (s->elem_mass) TRY(download_scatter(h, s->elem_mass, h->d_elem_mass, t.elem_int2ext, 1, 0));
   if (s->elem_stress) std::memset(s->elem_stress, 0, sizeof(double) * (size_t)ne * 18);
   if (s->corner_force) {
@@ -590,11 +604,12 @@ extern "C" int fierro_sgh_run_timed(fierro_sgh* h, int64_t cycles, float* kernel
     for (int s = 0; s < h->rk_num_stages; ++s) {
       const double alpha = stage_alpha(h, s);
       const int rb = (s == 0) ? c : (c ^ 1);
-      h->ks->force(force_args(h, rb), h->stream);
+      const int q = div_parity(h, c, s);
+      h->ks->force(force_args(h, rb, q), h->stream);
       CUDA_TRY(cudaEventRecord(ev[k++], h->stream));
       h->ks->node(node_args(h, c, alpha), h->stream);
       CUDA_TRY(cudaEventRecord(ev[k++], h->stream));
-      h->ks->elem(elem_args(h, c ^ 1, c, alpha), (s == h->rk_num_stages - 1) ? 1 : 0, h->stream);
+      h->ks->elem(elem_args(h, c ^ 1, c, alpha, q ^ 1), (s == h->rk_num_stages - 1) ? 1 : 0, h->stream);
       CUDA_TRY(cudaEventRecord(ev[k++], h->stream));
     }
     h->ks->end(h->d_ctrl, h->lp, h->stream);

@@ -10,6 +10,9 @@
 //            geometry (row lid*3+dim), written by the element kernel and read by
 //            the next stage's force kernel
 //   force    [24][ne]  corner forces, row lid*3+dim
+//   div      two buffers: the force pass of a stage reads one, the element pass
+//            writes the next stage's into the other (so the reference-visible
+//            elem_div, the one the last stage used, survives)
 //   corner CSR per node (int32 corner id e*8+lid, reference summation order),
 //   neighbour CSR per element (int32)
 #ifndef FIERRO_SGH_DEVICE_H
@@ -50,7 +53,8 @@ struct ForceArgs {
   const double* qtab;  // [nmat][4] = q1, q1ex, q2, q2ex
   const double* bmat;
   const double *u, *v, *w;  // current velocity (reference bin 1)
-  const double *den, *pres, *sspd, *vol, *div;
+  const double *den, *pres, *sspd, *vol;
+  const double* div;  // divergence of this stage (written by the previous element pass)
   double* force;
   const Ctrl* ctrl;
   double fuzz, small;
@@ -83,7 +87,8 @@ struct ElemArgs {
   const double* sie0;
   double* sie1;
   const double *gamma, *csmin;
-  double *den, *pres, *sspd, *vol, *div;
+  double *den, *pres, *sspd, *vol;
+  double* div;  // divergence for the next stage
   double* bmat;
   long long* cfl_part;  // per-block minimum of the element time steps (order keys)
   Ctrl* ctrl;

@@ -9,7 +9,6 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REFERENCE_MESHES = "/root/reference/Explicit-Lagrange/meshes"
 
 
 def pytest_configure(config):
