@@ -179,6 +179,21 @@ int64_t fierro_sgh_launches_per_cycle(const fierro_sgh* h);
 /* Bytes of device memory the handle holds. */
 int64_t fierro_sgh_device_bytes(const fierro_sgh* h);
 
+/* Energy tallies IE = sum elem_mass*elem_sie and KE = 1/2 sum node_mass*|v|^2
+ * over device arrays the caller owns, enqueued on `stream` (NULL = default
+ * stream), written as two doubles to the DEVICE pointer ie_ke.  No counterpart in
+ * the reference: it exists for callers that cannot call cudaMalloc when they
+ * need the tallies (for example while capturing a CUDA graph, or when all device
+ * memory belongs to the caller's own arena), and it allocates nothing.  Its
+ * scratch is an 8 KiB array held by every GPU that loads the library until the
+ * process exits; at most 2^30 elements and 2^30 nodes per call (EINVAL beyond).
+ * The first call on each device looks up that array's device address, so make
+ * the first call before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU race on it. */
+int fierro_energy_tally_noalloc(const double* elem_mass, const double* elem_sie, int64_t num_elems,
+                                const double* node_mass, const double* node_u, const double* node_v,
+                                const double* node_w, int64_t num_nodes, double* ie_ke, void* stream);
+
 /* FP64 roof calibration on the current device: dependent-chain-free DFMA
  * throughput, in fused multiply-adds per second (one FMA = 2 FLOP). */
 int fierro_measure_fp64_rate(double* dfma_per_second);
