@@ -150,6 +150,17 @@ def alg_bytes(kind: str, nn: int, ne: int, nnz: int) -> float:
     return 0.0
 
 
+# Per-unit figures of the exact-mode kernels from the ncu capture summarised in
+# profiles/sgh_kernels_sedov64_ncu_full.md (64^3 case, above L2; per-element
+# DRAM bytes scale with the elements processed): FP64 thread instructions and
+# dram__bytes_read + dram__bytes_write per element of one launch.  k_elem is the
+# mean of its first-stage and last-stage (CFL) launches.
+NCU_PER_ELEM = {
+    "k_force": {"fp64_ops": 528.0, "dram_bytes": (104.547840e6 + 22.322176e6) / 262144},
+    "k_elem": {"fp64_ops": (603.0 + 811.0) / 2, "dram_bytes": (87.241472e6 + 26.444544e6 + 87.148800e6 + 26.663424e6) / 2 / 262144},
+}
+
+
 def measure_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -296,11 +307,17 @@ def ours(args):
         "e2e": e2e,
         "roofline": {
             "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-            "frac": achieved / hbm_peak, "traffic": None, "peak_kind": peak_kind,
-            "alg_bytes_per_launch": ab, "avg_launch_ms": dom_ms,
-            "binding_pipe": "fp64",
-            "fp64_peak_dfma_per_s": fp64_rate,
+            "frac": achieved / hbm_peak,
+            "traffic": NCU_PER_ELEM[dom]["dram_bytes"] * ne if dom in NCU_PER_ELEM else None,
+            "peak_kind": peak_kind, "alg_bytes_per_launch": ab, "avg_launch_ms": dom_ms,
             "cycle_alg_bytes": cycle_bytes, "cycle_hbm_gbs": cycle_bytes / (cycle_ms * 1e-3) / 1e9,
+            "binding_pipe": "fp64",
+            "fp64": None if dom not in NCU_PER_ELEM or args.fp_mode != "exact" else {
+                "achieved": NCU_PER_ELEM[dom]["fp64_ops"] * ne / (dom_ms * 1e-3) / 1e9,
+                "peak": fp64_rate / 1e9, "unit": "G FP64 thread-instructions/s",
+                "frac": NCU_PER_ELEM[dom]["fp64_ops"] * ne / (dom_ms * 1e-3) / fp64_rate,
+                "peak_kind": "measured DFMA rate on this GPU (fierro_measure_fp64_rate)",
+                "ops_per_elem": NCU_PER_ELEM[dom]["fp64_ops"]},
         },
         "kernels": {nm: {"launches": launches[nm], "ms": per[nm], "share": share[nm]} for nm in sorted(per)},
         "cpu_baseline": None if cpu is None else {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
