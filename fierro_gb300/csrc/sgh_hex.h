@@ -51,11 +51,6 @@ constexpr int VJ[8][6] = {
 constexpr int PATCH[6][4] = {
     {0, 4, 7, 3}, {1, 2, 6, 5}, {0, 1, 5, 4}, {2, 3, 7, 6}, {0, 3, 2, 1}, {4, 5, 6, 7},
 };
-// Node pairs of get_timestep's 28 distances (time_integration.cpp:93-121),
-// in the reference's visiting order.
-constexpr int PAIR_A[28] = {0, 1, 2, 3, 4, 5, 6, 0, 1, 2, 3, 4, 5, 0, 1, 2, 3, 4, 0, 1, 2, 3, 0, 1, 2, 0, 1, 0};
-constexpr int PAIR_B[28] = {1, 2, 3, 4, 5, 6, 7, 2, 3, 4, 5, 6, 7, 3, 4, 5, 6, 7, 4, 5, 6, 7, 5, 6, 7, 6, 7, 7};
-
 // Position t of neighbour j in row p of J (compile-time).
 constexpr int slot(int p, int j) {
   return J[p][0] == j ? 0 : J[p][1] == j ? 1 : J[p][2] == j ? 2 : J[p][3] == j ? 3 : J[p][4] == j ? 4 : 5;

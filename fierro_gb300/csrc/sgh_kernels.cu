@@ -57,6 +57,7 @@ __device__ __forceinline__ double okey_decode(long long k) {
 }
 
 #include "sgh_hex_geometry.cuh"
+#include "sgh_cfl.cuh"
 
 // pow(v, 1.0/3.0) as the reference computes it (force_sgh.cpp:319-320).
 // The exponent is fl(1/3) = 1/3 - d, d = 2^-54/3, so the target is
@@ -309,8 +310,8 @@ __global__ void __launch_bounds__(kElemBlock) k_elem(const ElemArgs a) {
       sie1 = a.sie0[e] - adt / a.mass[e] * power;
       a.sie1[e] = sie1;
     }
-    double vol_geo, Sx, Sy, Sz, d2min;
-    hex_geometry<KIND != 0>(x, y, z, u, v, w, a.bmat, ne, e, vol_geo, Sx, Sy, Sz, d2min);
+    double vol_geo, Sx, Sy, Sz;
+    hex_geometry(x, y, z, u, v, w, a.bmat, ne, e, vol_geo, Sx, Sy, Sz);
     // the priming pass keeps the uploaded volume, as get_divergence reads elem_vol
     const double vol = (KIND == 2) ? a.vol[e] : vol_geo;
     // divergence for the next stage (momentum.cpp:265-286), with this geometry
@@ -339,7 +340,18 @@ __global__ void __launch_bounds__(kElemBlock) k_elem(const ElemArgs a) {
     }
     if (KIND != 0) {
       // element CFL step dt_cfl * min distance / (c + fuzz) (time_integration.cpp:124-131);
-      // min of the square roots == square root of the min (sqrt is monotone, exact)
+      // min of the square roots == square root of the min (sqrt is monotone, exact).
+      // The coordinates go to this thread's column of shared memory for the exact
+      // re-evaluation of the screened pairs (no other thread reads them).
+      __shared__ double s_xyz[24][kElemBlock];
+#pragma unroll
+      for (int l = 0; l < 8; ++l) {
+        s_xyz[l][threadIdx.x] = x[l];
+        s_xyz[8 + l][threadIdx.x] = y[l];
+        s_xyz[16 + l][threadIdx.x] = z[l];
+      }
+      const double d2min = cfl::min_d2(x, y, z, &s_xyz[0][threadIdx.x], &s_xyz[8][threadIdx.x],
+                                       &s_xyz[16][threadIdx.x], kElemBlock);
       const double dist_min = sqrt(d2min);
       const double dt_l = a.dt_cfl * dist_min / (sspd + a.fuzz);
       dkey = isnan(dt_l) ? 0x7FFFFFFFFFFFFFFFLL : okey(dt_l);

@@ -1,10 +1,10 @@
 """The generated straight-line hex geometry (fierro_gb300/csrc/sgh_hex_geometry.cuh,
 used by the element kernel) compiled as host C++ without contraction equals the
-oracle's table-driven B matrix and volume bit for bit, and its divergence sums
-and CFL minimum equal the reference's formulas evaluated term by term (with the
-IEEE square d*d for the reference's pow(d, 2.0))."""
+oracle's table-driven B matrix and volume bit for bit and its divergence sums
+equal the reference's formulas evaluated term by term; the screened CFL minimum
+(sgh_cfl.cuh) equals the exhaustive FP64 minimum of the reference's squared
+distances (with the IEEE square d*d for the reference's pow(d, 2.0))."""
 import ctypes as C
-import math
 import os
 import subprocess
 
@@ -14,16 +14,26 @@ import pytest
 from conftest import ROOT
 
 SHIM = r'''
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #define __device__
 #define __forceinline__ inline
-static inline long long okey(double d) { long long b; std::memcpy(&b, &d, 8); return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL); }
-static inline double okey_decode(long long k) { long long b = k ^ ((k >> 63) & 0x7FFFFFFFFFFFFFFFLL); double d; std::memcpy(&d, &b, 8); return d; }
+static inline long long __double_as_longlong(double d) { long long b; std::memcpy(&b, &d, 8); return b; }
+static inline double __longlong_as_double(long long b) { double d; std::memcpy(&d, &b, 8); return d; }
+static inline float __uint_as_float(unsigned u) { float f; std::memcpy(&f, &u, 4); return f; }
+static inline int __ffs(int v) { return __builtin_ffs(v); }
+using std::fabs; using std::sqrt;
 #include "sgh_hex_geometry.cuh"
+#include "sgh_cfl.cuh"
 extern "C" void geom(const double* x, const double* y, const double* z, const double* u, const double* v,
                      const double* w, double* bmat, double* out) {
-  hex_geometry<true>(x, y, z, u, v, w, bmat, 1, 0, out[0], out[1], out[2], out[3], out[4]);
+  hex_geometry(x, y, z, u, v, w, bmat, 1, 0, out[0], out[1], out[2], out[3]);
+}
+extern "C" double cfl_min(const double* x, const double* y, const double* z) {
+  double sx[8], sy[8], sz[8];
+  for (int l = 0; l < 8; ++l) { sx[l] = x[l]; sy[l] = y[l]; sz[l] = z[l]; }
+  return cfl::min_d2(x, y, z, sx, sy, sz, 1);
 }
 '''
 
@@ -38,6 +48,8 @@ def geomlib(tmp_path_factory):
                     os.path.join(ROOT, "fierro_gb300", "csrc"), str(src), "-o", str(so)], check=True)
     lib = C.CDLL(str(so))
     lib.geom.argtypes = [C.c_void_p] * 8
+    lib.cfl_min.argtypes = [C.c_void_p] * 3
+    lib.cfl_min.restype = C.c_double
     return lib
 
 
@@ -66,7 +78,7 @@ def test_generated_geometry_bitwise(geomlib, oracle_built):
         x, y, z = (np.ascontiguousarray(h[:, d]) for d in range(3))
         u, v, w = (np.ascontiguousarray(vel[:, d]) for d in range(3))
         bm = np.zeros(24)
-        out = np.zeros(5)
+        out = np.zeros(4)
         geomlib.geom(*(a.ctypes.data for a in (x, y, z, u, v, w, bm, out)))
         B = orc.bmatrix(x, y, z)
         assert np.array_equal(bm.reshape(8, 3), B)
@@ -76,9 +88,49 @@ def test_generated_geometry_bitwise(geomlib, oracle_built):
             for p in range(1, 8):
                 s = s + vv[p] * B[p, c]
             assert out[1 + c] == s
-        dist = []
-        for a, b in pairs:
-            dx, dy, dz = h[b, 0] - h[a, 0], h[b, 1] - h[a, 1], h[b, 2] - h[a, 2]
-            dist.append(abs(math.sqrt((dx * dx + dy * dy) + dz * dz)))
-        assert len(dist) == 28
-        assert math.sqrt(out[4]) == min(dist)
+
+
+PAIRS = [(a, b) for gap in range(1, 8) for a in range(0, 8 - gap) for b in [a + gap]]
+
+
+def exact_min_d2(h):
+    best = None
+    for a, b in PAIRS:
+        dx, dy, dz = h[b, 0] - h[a, 0], h[b, 1] - h[a, 1], h[b, 2] - h[a, 2]
+        d2 = (dx * dx + dy * dy) + dz * dz
+        best = d2 if best is None else min(best, d2)
+    return best
+
+
+def _cfl(lib, h):
+    x, y, z = (np.ascontiguousarray(h[:, d]) for d in range(3))
+    return lib.cfl_min(x.ctypes.data, y.ctypes.data, z.ctypes.data)
+
+
+def test_cfl_screening_is_exact(geomlib):
+    """The FP32-screened CFL minimum equals the exhaustive FP64 minimum bit for bit:
+    jittered hexes over many scales and offsets, exact cubes (12 tied edges) far
+    from the origin, near-ties, coincident nodes, and coordinates outside the
+    screening's range (full FP64 path)."""
+    rng = np.random.default_rng(11)
+    base = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], float)
+    cases = []
+    for _ in range(3000):
+        scale = 10 ** rng.uniform(-6, 3)
+        off = rng.uniform(-1, 1, 3) * 10 ** rng.uniform(-3, 4)
+        cases.append((base + rng.uniform(-0.2, 0.2, base.shape)) * scale + off)
+    for _ in range(500):
+        h = 10 ** rng.uniform(-4, 0)
+        cases.append(base * h + rng.uniform(0, 1e3, 3))        # exact ties, large offset
+        k = base.copy() * h + rng.uniform(0, 2, 3)
+        k[1, 0] = np.nextafter(k[1, 0], np.inf)                 # 1-ulp near-tie
+        cases.append(k)
+        k = base.copy() * h
+        k[6] = k[5]                                             # coincident nodes
+        cases.append(k)
+    cases.append(base * 2.0 ** 70)                              # outside [2^-60, 2^60]
+    cases.append(base * 2.0 ** -70)
+    cases.append(base * 1e-7)                                   # M < 2^-20
+    for h in cases:
+        got = _cfl(geomlib, h)
+        assert got == exact_min_d2(h), h
