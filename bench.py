@@ -44,6 +44,10 @@ def parse(argv=None):
     ap.add_argument("--cpu-cycles", type=int, default=6, help="timed cycles of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--batch", action="store_true",
+                    help="run the batched-ensemble benchmark instead (instances/s vs looping the plain solver)")
+    ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--batch-cycles", type=int, default=100)
     return ap.parse_args(argv)
 
 
@@ -340,8 +344,76 @@ def solver_neighbor_count(prob) -> int:
     return per_axis_sum ** 3 - m.num_elems
 
 
+def batch_workload(n_inst: int, seed: int, cycles: int):
+    """The ensemble: instance i is Sedov or Noh with probability 1/2, a uniform
+    n^3 box with n ~ U{8..48}, gamma ~ U[1.2, 1.8]; Sedov deposits E ~ logU[0.05, 5]
+    in the origin element, Noh flows in at speed ~ U[0.5, 2].  Seeded through the
+    counter-based generator of fierro_gb300.mesh."""
+    import math
+    from fierro_gb300 import mesh, problems
+    out = []
+    for i in range(n_inst):
+        u = mesh.uniform01(seed, 1000 + i, 5)
+        n = 8 + min(40, int(u[1] * 41))
+        gamma = 1.2 + 0.6 * float(u[2])
+        if u[0] < 0.5:
+            energy = math.exp(math.log(0.05) + float(u[3]) * (math.log(5.0) - math.log(0.05)))
+            out.append(problems.sedov(n, energy=energy, gamma=gamma, cycles=cycles))
+        else:
+            speed = 0.5 + 1.5 * float(u[4])
+            out.append(problems.noh(n, speed=-speed, gamma=gamma, cycles=cycles))
+    return out
+
+
+def batch_bench(args):
+    import torch
+    from fierro_gb300 import sgh
+    torch.cuda.set_device(0)
+    probs = batch_workload(args.instances, args.seed, args.batch_cycles)
+    states = [sgh.setup(p) for p in probs]
+    ne_tot = sum(p.mesh.num_elems for p in probs)
+    with sgh.Batch(probs[:2]) as w:  # load the batch kernels
+        w.set_state(0, states[0])
+        w.set_state(1, states[1])
+        w.run(3)
+    stream = torch.cuda.Stream()
+    b = sgh.Batch(probs, stream=stream.cuda_stream)
+    for i, st in enumerate(states):
+        b.set_state(i, st)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.run(args.batch_cycles)
+    t_batch = time.perf_counter() - t0
+    cycles_done = [b.time(i)[2] for i in range(len(probs))]
+    b.close()
+    # the same instances one after another through the single-problem solver
+    t_loop = 0.0
+    for p, st in zip(probs, states):
+        with sgh.SGHSolver(p) as s:
+            s.set_state(st)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            s.run(args.batch_cycles)
+            t_loop += time.perf_counter() - t1
+    n = len(probs)
+    line = {"metric": "batched SGH ensemble instances/s (%d Sedov/Noh instances, n~U{8..48}, %d cycles each)"
+                      % (n, args.batch_cycles),
+            "value": n / t_batch, "unit": "instances/s", "higher_is_better": True, "dtype": "f64",
+            "data": "synthetic", "loop_value": n / t_loop, "speedup_vs_loop": t_loop / t_batch,
+            "batch_seconds": t_batch, "loop_seconds": t_loop, "elements_total": ne_tot,
+            "element_cycles_per_s": sum(p.mesh.num_elems * c for p, c in zip(probs, cycles_done)) / t_batch,
+            "instances_stopped_early": int(sum(c < args.batch_cycles for c in cycles_done)),
+            "config": {"workload": "ensemble", "instances": n, "cycles": args.batch_cycles, "seed": args.seed,
+                       "launches_per_cycle": 8, "timing": "host wall clock around fierro_batch_run / "
+                       "fierro_sgh_run (each synchronises)"}}
+    print(json.dumps(line))
+
+
 def main(argv=None):
     args = parse(argv)
+    if args.batch:
+        batch_bench(args)
+        return
     if args.impl == "reference":
         reference_arm(args)
     else:

@@ -6,6 +6,7 @@ Translation units:
   csrc/sgh_host.cpp    mesh topology, Morton renumbering, set-up (g++, OpenMP,
                        -ffp-contract=off so set-up doubles are uncontracted)
   csrc/sgh_capi.cpp    the C ABI (g++)
+  csrc/sgh_batch.cpp   the batched-ensemble C ABI (g++)
   csrc/sgh_calib.cu    FP64 throughput calibration for the roofline
   csrc/sgh_noalloc.cu  energy tallies with static scratch (no allocation)
 All compile in parallel; a unit is rebuilt only when it or a header changed.
@@ -64,7 +65,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     units.append((os.path.join(OBJ, "sgh_noalloc.o"), nvcc_common + ["-c", noalloc], [noalloc]))
     gxx = ["g++", "-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wall", "-Wno-unknown-pragmas",
            "-I", os.path.join(CUDA_HOME, "include")] + inc
-    for name in ("sgh_host.cpp", "sgh_capi.cpp"):
+    for name in ("sgh_host.cpp", "sgh_capi.cpp", "sgh_batch.cpp"):
         src = os.path.join(CSRC, name)
         units.append((os.path.join(OBJ, name.replace(".cpp", ".o")), gxx + ["-c", src], [src]))
     jobs = []

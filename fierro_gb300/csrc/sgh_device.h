@@ -56,7 +56,8 @@ struct ForceArgs {
   const double *den, *pres, *sspd, *vol;
   const double* div;  // divergence of this stage (written by the previous element pass)
   double* force;
-  const Ctrl* ctrl;
+  const Ctrl* ctrl;   // plain: the solver's control block; batch: one per instance
+  const int* inst;    // batch only: instance of each element (negative = padding)
   double fuzz, small;
 };
 
@@ -71,6 +72,7 @@ struct NodeArgs {
   double *u1, *v1, *w1, *x1, *y1, *z1;        // updated (reference bin 1)
   double *hx, *hy, *hz;                       // half velocity (v1 + v0) / 2
   const Ctrl* ctrl;
+  const int* inst;  // batch only: instance of each node
   double rk_alpha;
 };
 
@@ -92,6 +94,8 @@ struct ElemArgs {
   double* bmat;
   long long* cfl_part;  // per-block minimum of the element time steps (order keys)
   Ctrl* ctrl;
+  const int* inst;            // batch only: instance of each element (negative = padding)
+  const double* dt_cfl_tab;   // batch only: CFL number per instance
   double rk_alpha, dt_cfl, fuzz;
 };
 
@@ -100,6 +104,10 @@ struct DtArgs {
   int nparts;
   Ctrl* ctrl;
   LoopParams lp;
+  // batch only: instance i owns cfl_part[part_start[i] .. part_start[i+1])
+  const int* part_start;
+  const LoopParams* lps;
+  int ninst;
 };
 
 struct EnergyArgs {
@@ -118,6 +126,7 @@ struct KernelSet {
   void (*dt)(const DtArgs&, cudaStream_t);
   void (*end)(Ctrl*, const LoopParams&, cudaStream_t);
   void (*energy)(const EnergyArgs&, cudaStream_t);
+  void (*end_batch)(Ctrl*, const LoopParams*, int, cudaStream_t);
   const char* name;
 };
 

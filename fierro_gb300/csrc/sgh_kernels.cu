@@ -118,10 +118,12 @@ __device__ __forceinline__ long long block_min_key(long long k) {
 // (use_shock_dir = 0 at :227, phi_curl unused at :331) and are not computed.
 // Stress is zero for strength-free materials, so tau = -p I and the force's
 // stress term a_k tau(k,d) reduces exactly to B(d) p (two negations).
+template <bool BATCH>
 __global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
-  if (!a.ctrl->active) return;
+  if (!BATCH && !a.ctrl->active) return;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= a.ne) return;
+  if (BATCH && (a.inst[e] < 0 || !a.ctrl[a.inst[e]].active)) return;
   const int ne = a.ne;
   const int4 n03 = __ldg(reinterpret_cast<const int4*>(a.nie) + 2 * e);
   const int4 n47 = __ldg(reinterpret_cast<const int4*>(a.nie) + 2 * e + 1);
@@ -229,10 +231,13 @@ __global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
 // ---------------------------------------------------------------------------
 // Node update: corner-force gather in the reference's summation order, velocity,
 // boundary conditions, half velocity and position.
+template <bool BATCH>
 __global__ void __launch_bounds__(kNodeBlock) k_node(const NodeArgs a) {
-  if (!a.ctrl->active) return;
+  if (!BATCH && !a.ctrl->active) return;
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= a.nn) return;
+  const Ctrl* ctrl = BATCH ? a.ctrl + a.inst[n] : a.ctrl;
+  if (BATCH && !ctrl->active) return;
   const size_t ne = (size_t)a.ne;
   double f0 = 0.0, f1 = 0.0, f2 = 0.0;
   const int c0 = a.cin_start[n], c1 = a.cin_start[n + 1];
@@ -243,7 +248,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_node(const NodeArgs a) {
     f1 = f1 + __ldg(a.force + (size_t)(l * 3 + 1) * ne + e);
     f2 = f2 + __ldg(a.force + (size_t)(l * 3 + 2) * ne + e);
   }
-  const double adt = a.rk_alpha * a.ctrl->dt;
+  const double adt = a.rk_alpha * ctrl->dt;
   const double m = a.node_mass[n];
   const double u0 = a.u0[n], v0 = a.v0[n], w0 = a.w0[n];
 #if FIERRO_FMA
@@ -275,11 +280,17 @@ __global__ void __launch_bounds__(kNodeBlock) k_node(const NodeArgs a) {
 // ---------------------------------------------------------------------------
 // Element update.  KIND 0: stage; 1: last stage (adds the CFL partials);
 // 2: prime (corner normals, divergence and CFL of an uploaded state).
-template <int KIND>
+// In a batch every block lies inside one instance (instances' element ranges are
+// padded to whole blocks, padding marked by a negative instance id), so the
+// activity test and the CFL partial are per block.
+template <int KIND, bool BATCH>
 __global__ void __launch_bounds__(kElemBlock) k_elem(const ElemArgs a) {
-  if (KIND != 2 && !a.ctrl->active) return;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool live = e < a.ne;
+  const int ib = BATCH ? a.inst[blockIdx.x * kElemBlock] : 0;
+  Ctrl* ctrl = a.ctrl + ib;
+  if (KIND != 2 && !ctrl->active) return;
+  const bool live = e < a.ne && (!BATCH || a.inst[e] >= 0);
+  const double dt_cfl = BATCH ? a.dt_cfl_tab[ib] : a.dt_cfl;
   long long dkey = 0x7FFFFFFFFFFFFFFFLL;
   if (live) {
     const int ne = a.ne;
@@ -306,7 +317,7 @@ __global__ void __launch_bounds__(kElemBlock) k_elem(const ElemArgs a) {
         power = power + a.force[(size_t)(l * 3 + 1) * ne + e] * __ldg(a.hy + nid[l]);
         power = power + a.force[(size_t)(l * 3 + 2) * ne + e] * __ldg(a.hz + nid[l]);
       }
-      const double adt = a.rk_alpha * a.ctrl->dt;
+      const double adt = a.rk_alpha * ctrl->dt;
       sie1 = a.sie0[e] - adt / a.mass[e] * power;
       a.sie1[e] = sie1;
     }
@@ -333,8 +344,8 @@ __global__ void __launch_bounds__(kElemBlock) k_elem(const ElemArgs a) {
       a.den[e] = den;
       a.pres[e] = pres;
       a.sspd[e] = sspd;
-      if (!(vol > 0.0) || !isfinite(vol)) atomicOr(&a.ctrl->status, FIERRO_STATUS_BAD_VOLUME);
-      if (!isfinite(sie1) || !isfinite(pres)) atomicOr(&a.ctrl->status, FIERRO_STATUS_BAD_STATE);
+      if (!(vol > 0.0) || !isfinite(vol)) atomicOr(&ctrl->status, FIERRO_STATUS_BAD_VOLUME);
+      if (!isfinite(sie1) || !isfinite(pres)) atomicOr(&ctrl->status, FIERRO_STATUS_BAD_STATE);
     } else {
       sspd = a.sspd[e];
     }
@@ -353,7 +364,7 @@ __global__ void __launch_bounds__(kElemBlock) k_elem(const ElemArgs a) {
       const double d2min = cfl::min_d2(x, y, z, &s_xyz[0][threadIdx.x], &s_xyz[8][threadIdx.x],
                                        &s_xyz[16][threadIdx.x], kElemBlock);
       const double dist_min = sqrt(d2min);
-      const double dt_l = a.dt_cfl * dist_min / (sspd + a.fuzz);
+      const double dt_l = dt_cfl * dist_min / (sspd + a.fuzz);
       dkey = isnan(dt_l) ? 0x7FFFFFFFFFFFFFFFLL : okey(dt_l);
     }
   }
@@ -367,6 +378,22 @@ __global__ void __launch_bounds__(kElemBlock) k_elem(const ElemArgs a) {
 // get_timestep's scalar part (time_integration.cpp:69-150) on the device.  The
 // per-element clamp to [dt_min, dt_max] commutes with the minimum (it is
 // monotone), so it is applied once to the minimum.
+__device__ __forceinline__ void dt_update(Ctrl* c, long long k, const LoopParams& lp) {
+  if (c->stopped) {
+    c->active = 0;
+    return;
+  }
+  double dt = c->dt * 1.1;
+  double min_dt_calc = (k == 0x7FFFFFFFFFFFFFFFLL) ? 1.7976931348623157e308 : okey_decode(k);
+  min_dt_calc = fmin(min_dt_calc, lp.dt_max);
+  min_dt_calc = fmax(min_dt_calc, lp.dt_min);
+  if (min_dt_calc < dt) dt = min_dt_calc;
+  dt = fmin(dt, (c->graphics_time - c->time_value) + lp.fuzz);
+  dt = fmin(dt, lp.time_final - c->time_value);
+  c->dt = dt;
+  c->active = 1;
+}
+
 __global__ void __launch_bounds__(1024) k_dt(const DtArgs a) {
   long long k = 0x7FFFFFFFFFFFFFFFLL;
   for (int i = threadIdx.x; i < a.nparts; i += blockDim.x) {
@@ -374,25 +401,24 @@ __global__ void __launch_bounds__(1024) k_dt(const DtArgs a) {
     k = t < k ? t : k;
   }
   k = block_min_key(k);
-  if (threadIdx.x != 0) return;
-  Ctrl* c = a.ctrl;
-  if (c->stopped) {
-    c->active = 0;
-    return;
+  if (threadIdx.x == 0) dt_update(a.ctrl, k, a.lp);
+}
+
+// One block per instance: instance i's CFL partials are cfl_part[part_start[i] ..
+// part_start[i+1]).
+__global__ void __launch_bounds__(256) k_dt_batch(const DtArgs a) {
+  const int i = blockIdx.x;
+  long long k = 0x7FFFFFFFFFFFFFFFLL;
+  for (int j = a.part_start[i] + threadIdx.x; j < a.part_start[i + 1]; j += blockDim.x) {
+    const long long t = a.cfl_part[j];
+    k = t < k ? t : k;
   }
-  double dt = c->dt * 1.1;
-  double min_dt_calc = (k == 0x7FFFFFFFFFFFFFFFLL) ? 1.7976931348623157e308 : okey_decode(k);
-  min_dt_calc = fmin(min_dt_calc, a.lp.dt_max);
-  min_dt_calc = fmax(min_dt_calc, a.lp.dt_min);
-  if (min_dt_calc < dt) dt = min_dt_calc;
-  dt = fmin(dt, (c->graphics_time - c->time_value) + a.lp.fuzz);
-  dt = fmin(dt, a.lp.time_final - c->time_value);
-  c->dt = dt;
-  c->active = 1;
+  k = block_min_key(k);
+  if (threadIdx.x == 0) dt_update(a.ctrl + i, k, a.lps[i]);
 }
 
 // End of a cycle (sgh_solve.cpp:590-632).
-__global__ void k_end(Ctrl* c, const LoopParams lp) {
+__device__ __forceinline__ void end_update(Ctrl* c, const LoopParams& lp) {
   if (!c->active) return;
   c->time_value += c->dt;
   const long long cycle = c->cycle;
@@ -404,6 +430,13 @@ __global__ void k_end(Ctrl* c, const LoopParams lp) {
   if (c->time_value >= lp.time_final) c->stopped = 1;
   c->cycle = cycle + 1;
   c->active = 0;
+}
+
+__global__ void k_end(Ctrl* c, const LoopParams lp) { end_update(c, lp); }
+
+__global__ void k_end_batch(Ctrl* c, const LoopParams* lps, int ninst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < ninst) end_update(c + i, lps[i]);
 }
 
 // Energy tallies (sgh_solve.cpp:77-101): fixed-shape two-pass sums.
@@ -450,19 +483,32 @@ __global__ void k_energy_final(const EnergyArgs a, int nblocks) {
 static unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 static void launch_force(const ForceArgs& a, cudaStream_t s) {
-  k_force<<<blocks_for(a.ne, kForceBlock), kForceBlock, 0, s>>>(a);
+  if (a.inst) k_force<true><<<blocks_for(a.ne, kForceBlock), kForceBlock, 0, s>>>(a);
+  else k_force<false><<<blocks_for(a.ne, kForceBlock), kForceBlock, 0, s>>>(a);
 }
 static void launch_node(const NodeArgs& a, cudaStream_t s) {
-  k_node<<<blocks_for(a.nn, kNodeBlock), kNodeBlock, 0, s>>>(a);
+  if (a.inst) k_node<true><<<blocks_for(a.nn, kNodeBlock), kNodeBlock, 0, s>>>(a);
+  else k_node<false><<<blocks_for(a.nn, kNodeBlock), kNodeBlock, 0, s>>>(a);
+}
+template <bool B>
+static void launch_elem_t(const ElemArgs& a, int kind, cudaStream_t s) {
+  const unsigned g = blocks_for(a.ne, kElemBlock);
+  if (kind == 0) k_elem<0, B><<<g, kElemBlock, 0, s>>>(a);
+  else if (kind == 1) k_elem<1, B><<<g, kElemBlock, 0, s>>>(a);
+  else k_elem<2, B><<<g, kElemBlock, 0, s>>>(a);
 }
 static void launch_elem(const ElemArgs& a, int kind, cudaStream_t s) {
-  const unsigned g = blocks_for(a.ne, kElemBlock);
-  if (kind == 0) k_elem<0><<<g, kElemBlock, 0, s>>>(a);
-  else if (kind == 1) k_elem<1><<<g, kElemBlock, 0, s>>>(a);
-  else k_elem<2><<<g, kElemBlock, 0, s>>>(a);
+  if (a.inst) launch_elem_t<true>(a, kind, s);
+  else launch_elem_t<false>(a, kind, s);
 }
-static void launch_dt(const DtArgs& a, cudaStream_t s) { k_dt<<<1, 1024, 0, s>>>(a); }
+static void launch_dt(const DtArgs& a, cudaStream_t s) {
+  if (a.part_start) k_dt_batch<<<a.ninst, 256, 0, s>>>(a);
+  else k_dt<<<1, 1024, 0, s>>>(a);
+}
 static void launch_end(Ctrl* c, const LoopParams& lp, cudaStream_t s) { k_end<<<1, 1, 0, s>>>(c, lp); }
+static void launch_end_batch(Ctrl* c, const LoopParams* lps, int ninst, cudaStream_t s) {
+  k_end_batch<<<blocks_for(ninst, 128), 128, 0, s>>>(c, lps, ninst);
+}
 static void launch_energy(const EnergyArgs& a, cudaStream_t s) {
   const int nb = 512;
   k_energy_part<<<nb, kEnergyBlock, 0, s>>>(a);
@@ -474,14 +520,15 @@ static void launch_energy(const EnergyArgs& a, cudaStream_t s) {
 #if FIERRO_FMA
 const KernelSet& kernels_fma() {
   static const KernelSet k = {fma_impl::launch_force, fma_impl::launch_node, fma_impl::launch_elem,
-                              fma_impl::launch_dt, fma_impl::launch_end, fma_impl::launch_energy, "fma"};
+                              fma_impl::launch_dt, fma_impl::launch_end, fma_impl::launch_energy,
+                              fma_impl::launch_end_batch, "fma"};
   return k;
 }
 #else
 const KernelSet& kernels_exact() {
   static const KernelSet k = {exact_impl::launch_force, exact_impl::launch_node, exact_impl::launch_elem,
                               exact_impl::launch_dt, exact_impl::launch_end, exact_impl::launch_energy,
-                              "exact"};
+                              exact_impl::launch_end_batch, "exact"};
   return k;
 }
 #endif

@@ -95,6 +95,16 @@ def _load():
     lib.fierro_sgh_device_bytes.restype = i64
     lib.fierro_sgh_run_timed.argtypes = [vp, i64, vp, C.POINTER(C.c_float), C.POINTER(i64)]
     lib.fierro_measure_fp64_rate.argtypes = [C.POINTER(dbl)]
+    lib.fierro_batch_create.argtypes = [vp, i64, C.c_int, vp, C.POINTER(vp)]
+    lib.fierro_batch_destroy.argtypes = [vp]
+    lib.fierro_batch_set_state.argtypes = [vp, i64, vp]
+    lib.fierro_batch_get_state.argtypes = [vp, i64, vp]
+    lib.fierro_batch_run.argtypes = [vp, i64]
+    lib.fierro_batch_time.argtypes = [vp, i64, C.POINTER(dbl), C.POINTER(dbl), C.POINTER(i64)]
+    lib.fierro_batch_num_instances.argtypes = [vp]
+    lib.fierro_batch_num_instances.restype = i64
+    lib.fierro_batch_device_bytes.argtypes = [vp]
+    lib.fierro_batch_device_bytes.restype = i64
     return lib
 
 
@@ -281,6 +291,70 @@ class SGHSolver:
     @property
     def device_bytes(self) -> int:
         return int(_lib.fierro_sgh_device_bytes(self.h))
+
+
+class BatchInstance(C.Structure):
+    _fields_ = [("mesh", Mesh), ("materials", C.c_void_p), ("num_materials", C.c_int64), ("boundaries", C.c_void_p),
+                ("num_bcs", C.c_int64), ("params", Params)]
+
+
+class Batch:
+    """Batched ensemble: many independent problems advanced together, one launch
+    per kernel per cycle for all of them (fierro_batch_* in the C ABI)."""
+
+    def __init__(self, problems, fp_mode: int = FP_EXACT, stream: int | None = None):
+        self.problems = list(problems)
+        n = len(self.problems)
+        self._keep = []
+        arr = (BatchInstance * n)()
+        for i, p in enumerate(self.problems):
+            m, keep = c_mesh(p.mesh)
+            mats, bcs = c_materials(p), c_boundaries(p)
+            self._keep += [keep, mats, bcs]
+            arr[i] = BatchInstance(m, C.cast(mats, C.c_void_p), len(p.materials), C.cast(bcs, C.c_void_p),
+                                   len(p.boundaries), c_params(p))
+        self._arr = arr
+        h = C.c_void_p()
+        _check(_lib.fierro_batch_create(arr, n, fp_mode, C.c_void_p(stream) if stream else None, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            _lib.fierro_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __len__(self):
+        return len(self.problems)
+
+    def set_state(self, i: int, st: Dict[str, np.ndarray]):
+        _check(_lib.fierro_batch_set_state(self.h, i, C.byref(c_state(st))))
+
+    def get_state(self, i: int) -> Dict[str, np.ndarray]:
+        p = self.problems[i]
+        st = empty_state(p.mesh.num_nodes, p.mesh.num_elems, p.num_state_vars)
+        _check(_lib.fierro_batch_get_state(self.h, i, C.byref(c_state(st))))
+        return st
+
+    def run(self, cycles: int):
+        _check(_lib.fierro_batch_run(self.h, cycles))
+
+    def time(self, i: int):
+        t, dt, cyc = C.c_double(), C.c_double(), C.c_int64()
+        _check(_lib.fierro_batch_time(self.h, i, C.byref(t), C.byref(dt), C.byref(cyc)))
+        return t.value, dt.value, cyc.value
+
+    @property
+    def device_bytes(self) -> int:
+        return int(_lib.fierro_batch_device_bytes(self.h))
 
 
 def measure_fp64_rate() -> float:

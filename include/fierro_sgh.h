@@ -179,6 +179,38 @@ int64_t fierro_sgh_launches_per_cycle(const fierro_sgh* h);
 /* Bytes of device memory the handle holds. */
 int64_t fierro_sgh_device_bytes(const fierro_sgh* h);
 
+/* ---- batched ensemble: many independent problems advanced together ---------
+ * All instances' meshes and states live in one device layout and every kernel
+ * of a cycle covers all of them in one launch; each instance keeps its own dt,
+ * time, CFL number, materials, boundaries and stop time.  Results per instance
+ * equal those of a separate fierro_sgh handle bit for bit.  rk_num_stages, fuzz,
+ * tiny and small must be equal across instances.  No counterpart in the
+ * reference (it runs one problem per process). */
+typedef struct {
+  fierro_mesh mesh;
+  const fierro_material* materials;
+  int64_t num_materials;
+  const fierro_boundary* boundaries;
+  int64_t num_bcs;
+  fierro_sgh_params params;
+} fierro_batch_instance;
+
+typedef struct fierro_batch fierro_batch;
+
+int fierro_batch_create(const fierro_batch_instance* instances, int64_t num_instances, int fp_mode, void* stream,
+                        fierro_batch** out);
+int fierro_batch_destroy(fierro_batch* b);
+/* Upload instance i's initial state (reference layouts).  Every instance needs a
+ * state before the first fierro_batch_run; states cannot be replaced after it. */
+int fierro_batch_set_state(fierro_batch* b, int64_t instance, const fierro_sgh_state* state);
+int fierro_batch_get_state(fierro_batch* b, int64_t instance, fierro_sgh_state* state);
+/* Run `cycles` cycles of every instance (one CUDA graph launch per cycle) and
+ * wait; instances that reach their time_final stop by themselves. */
+int fierro_batch_run(fierro_batch* b, int64_t cycles);
+int fierro_batch_time(fierro_batch* b, int64_t instance, double* time_value, double* dt, int64_t* cycle);
+int64_t fierro_batch_num_instances(const fierro_batch* b);
+int64_t fierro_batch_device_bytes(const fierro_batch* b);
+
 /* Energy tallies IE = sum elem_mass*elem_sie and KE = 1/2 sum node_mass*|v|^2
  * over device arrays the caller owns, enqueued on `stream` (NULL = default
  * stream), written as two doubles to the DEVICE pointer ie_ke.  No counterpart in
