@@ -7,6 +7,8 @@ Translation units:
                        -ffp-contract=off so set-up doubles are uncontracted)
   csrc/sgh_capi.cpp    the C ABI (g++)
   csrc/sgh_batch.cpp   the batched-ensemble C ABI (g++)
+  csrc/sgh_adjoint.cu  discrete-adjoint kernels (--fmad=false, like the exact mode)
+  csrc/sgh_adjoint.cpp the adjoint's checkpointing, replay and reverse schedule (g++)
   csrc/sgh_calib.cu    FP64 throughput calibration for the roofline
   csrc/sgh_noalloc.cu  energy tallies with static scratch (no allocation)
 All compile in parallel; a unit is rebuilt only when it or a header changed.
@@ -61,11 +63,13 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     ]
     calib = os.path.join(CSRC, "sgh_calib.cu")
     units.append((os.path.join(OBJ, "sgh_calib.o"), nvcc_common + ["-c", calib], [calib]))
+    adjk = os.path.join(CSRC, "sgh_adjoint.cu")
+    units.append((os.path.join(OBJ, "sgh_adjoint_k.o"), nvcc_common + ["--fmad=false", "-c", adjk], [adjk]))
     noalloc = os.path.join(CSRC, "sgh_noalloc.cu")
     units.append((os.path.join(OBJ, "sgh_noalloc.o"), nvcc_common + ["-c", noalloc], [noalloc]))
     gxx = ["g++", "-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wall", "-Wno-unknown-pragmas",
            "-I", os.path.join(CUDA_HOME, "include")] + inc
-    for name in ("sgh_host.cpp", "sgh_capi.cpp", "sgh_batch.cpp"):
+    for name in ("sgh_host.cpp", "sgh_capi.cpp", "sgh_batch.cpp", "sgh_adjoint.cpp"):
         src = os.path.join(CSRC, name)
         units.append((os.path.join(OBJ, name.replace(".cpp", ".o")), gxx + ["-c", src], [src]))
     jobs = []

@@ -113,6 +113,37 @@ def main():
                 w("    %s = %s + %s[%d] * b%d;" % (S, S, vel[c], p, p))
         w("  }")
     w("}")
+    w("")
+    w("// Reverse mode of the corner normals: given Bbar[lid*3+dim] (the adjoint of")
+    w("// B(lid, dim)), accumulate the coordinate adjoints xbar, ybar, zbar[8].  B is")
+    w("// bilinear, B(p,c) = sum_t O[j_t] comb_t(I) / 12, and each unordered pair (p, j)")
+    w("// enters B(p) as O[j] cm and B(j) as -O[p] cm with one shared combo cm, so")
+    w("//   Obar[j] += g_p cm,  Obar[p] -= g_j cm,  Ibar[terms of cm] +-= g_p O[j] - g_j O[p]")
+    w("// with g = Bbar / 12 (multiply-adds fused: the adjoint has no parity target).")
+    w("__device__ __forceinline__ void hex_bmatrix_adjoint(const double* __restrict__ x, const double* __restrict__ y,")
+    w("    const double* __restrict__ z, const double* __restrict__ Bbar, double* __restrict__ xbar,")
+    w("    double* __restrict__ ybar, double* __restrict__ zbar) {")
+    w("  const double twelth = 1. / 12.;")
+    bar = {"x": "xbar", "y": "ybar", "z": "zbar"}
+    for c, (O, I) in enumerate(comps):
+        w("  {  // component %d: O = %s, I = %s" % (c, O, I))
+        for p_ in range(8):
+            w("    const double g%d = Bbar[%d] * twelth;" % (p_, p_ * 3 + c))
+        for k, (p_, t, j) in enumerate(pairs):
+            terms = [v for v in T[p_][t] if v]
+            expr = ("-" if terms[0] < 0 else "") + "%s[%d]" % (I, abs(terms[0]) - 1)
+            for v_ in terms[1:]:
+                expr = "(%s %s %s[%d])" % (expr, "+" if v_ > 0 else "-", I, abs(v_) - 1)
+            w("    {  // pair (%d,%d)" % (p_, j))
+            w("      const double cm = %s;" % expr)
+            w("      %s[%d] = fma(g%d, cm, %s[%d]);" % (bar[O], j, p_, bar[O], j))
+            w("      %s[%d] = fma(-g%d, cm, %s[%d]);" % (bar[O], p_, j, bar[O], p_))
+            w("      const double wk = fma(g%d, %s[%d], -(g%d * %s[%d]));" % (p_, O, j, j, O, p_))
+            for v_ in terms:
+                w("      %s[%d] %s= wk;" % (bar[I], abs(v_) - 1, "+" if v_ > 0 else "-"))
+            w("    }")
+        w("  }")
+    w("}")
     out = os.path.join(HERE, "sgh_hex_geometry.cuh")
     with open(out, "w") as f:
         f.write("\n".join(L) + "\n")

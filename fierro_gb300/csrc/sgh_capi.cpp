@@ -8,83 +8,12 @@
 
 #include <cuda_runtime.h>
 
-#include "fierro_sgh.h"
-#include "sgh_device.h"
-#include "sgh_internal.h"
+#include "sgh_handle.h"
 
 using namespace fierro;
 
-#define CUDA_TRY(expr)                                                                            \
-  do {                                                                                            \
-    cudaError_t err_ = (expr);                                                                    \
-    if (err_ != cudaSuccess)                                                                      \
-      return set_error(err_ == cudaErrorMemoryAllocation ? FIERRO_ENOMEM : FIERRO_ECUDA, "%s: %s", \
-                       #expr, cudaGetErrorString(err_));                                          \
-  } while (0)
-
-struct fierro_sgh {
-  HostTopo topo;
-  int64_t nn = 0, ne = 0;
-  int nmat = 0;
-  int fp_mode = FIERRO_FP_EXACT;
-  const KernelSet* ks = nullptr;
-  LoopParams lp{};
-  int rk_num_stages = 2;
-  double dt_start = 1e-5;
-  cudaStream_t stream = nullptr;
-  bool own_stream = false;
-  std::vector<void*> allocations;
-  size_t dev_bytes = 0;
-  // mesh
-  int *d_nie = nullptr, *d_cin_start = nullptr, *d_cin = nullptr, *d_eie_start = nullptr, *d_eie = nullptr;
-  int* d_mat = nullptr;
-  unsigned char* d_bc = nullptr;
-  double* d_qtab = nullptr;
-  // state
-  double *d_node_mass = nullptr, *d_elem_mass = nullptr, *d_gamma = nullptr, *d_csmin = nullptr;
-  double* d_x[2][3] = {};
-  double* d_v[2][3] = {};
-  double* d_h[3] = {};
-  double *d_den = nullptr, *d_pres = nullptr, *d_sspd = nullptr, *d_vol = nullptr;
-  double* d_div[2] = {};  // see sgh_device.h: read by stage parity q, written at q^1
-  double* d_sie[2] = {};
-  double *d_bmat = nullptr, *d_force = nullptr;
-  long long* d_cfl = nullptr;
-  int ncfl = 0;
-  Ctrl* d_ctrl = nullptr;
-  double *d_energy_part = nullptr, *d_energy_out = nullptr;
-  // pinned double buffer for permuted transfers
-  double* h_stage[2] = {};
-  cudaEvent_t stage_ev[2] = {};
-  size_t stage_elems = 0;
-  // loop position
-  int base = 0;          // bin holding the state uploaded by set_state
-  long long enq_cycles = 0;  // cycles enqueued since set_state
-  int stage = 0;         // next RK stage of the current cycle (stage stepping)
-  bool has_state = false;
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};
-};
-
-namespace {
-
-template <typename T>
-int dalloc(fierro_sgh* h, T** p, size_t count) {
-  void* q = nullptr;
-  size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
-  cudaError_t err = cudaMalloc(&q, bytes);
-  if (err != cudaSuccess)
-    return set_error(FIERRO_ENOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(err));
-  h->allocations.push_back(q);
-  h->dev_bytes += bytes;
-  *p = static_cast<T*>(q);
-  return FIERRO_OK;
-}
-
-#define TRY(expr)          \
-  do {                     \
-    int rc_ = (expr);      \
-    if (rc_) return rc_;   \
-  } while (0)
+namespace fierro {
+namespace hd {
 
 int upload_raw(fierro_sgh* h, void* dst, const void* src, size_t bytes) {
   CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
@@ -128,9 +57,6 @@ int check_status(fierro_sgh* h) {
     return set_error(FIERRO_ENUMERIC, "non-finite energy or pressure at cycle %lld", c.cycle);
   return FIERRO_OK;
 }
-
-// Bins at a cycle boundary after `done` executed cycles: state bin and start bin.
-int bin_now(const fierro_sgh* h, long long cycles_done) { return (int)((h->base + cycles_done) & 1); }
 
 ForceArgs force_args(fierro_sgh* h, int rb, int q) {
   ForceArgs a{};
@@ -218,13 +144,20 @@ ElemArgs elem_args(fierro_sgh* h, int cur_bin, int c, double alpha, int div_out)
   return a;
 }
 
-double stage_alpha(const fierro_sgh* h, int s) {
-  return 1.0 / ((double)h->rk_num_stages - (double)s);  // sgh_solve.cpp:353
+int cycles_done(fierro_sgh* h, long long* cyc) {
+  Ctrl c;
+  CUDA_TRY(cudaMemcpyAsync(&c, h->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  *cyc = c.cycle;
+  return FIERRO_OK;
 }
 
-// Divergence buffer a stage reads: the parity of the number of stages run since
-// set_state, which for stage s of a cycle with bin parity c is (c*S + s) & 1.
-int div_parity(const fierro_sgh* h, int c, int s) { return (c * h->rk_num_stages + s) & 1; }
+}  // namespace hd
+}  // namespace fierro
+
+using namespace fierro::hd;
+
+namespace {
 
 // Stage s of a cycle whose start state is in bin c.
 void enqueue_stage(fierro_sgh* h, int c, int s) {
@@ -279,6 +212,7 @@ int validate_params(const fierro_sgh_params* p) {
 extern "C" int fierro_sgh_destroy(fierro_sgh* h) {
   if (!h) return FIERRO_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
+  adj_release(h);
   for (int c = 0; c < 2; ++c)
     if (h->graph[c]) cudaGraphExecDestroy(h->graph[c]);
   for (void* p : h->allocations) cudaFree(p);
@@ -468,14 +402,6 @@ extern "C" int fierro_sgh_set_state(fierro_sgh* h, const fierro_sgh_state* s) {
   clear_error();
   if (!h) return set_error(FIERRO_EINVAL, "handle is NULL");
   return set_state_impl(h, s, 0.0, h->lp.graphics_dt_ival, h->dt_start);
-}
-
-static int cycles_done(fierro_sgh* h, long long* cyc) {
-  Ctrl c;
-  CUDA_TRY(cudaMemcpyAsync(&c, h->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
-  CUDA_TRY(cudaStreamSynchronize(h->stream));
-  *cyc = c.cycle;
-  return FIERRO_OK;
 }
 
 extern "C" int fierro_sgh_get_state(fierro_sgh* h, fierro_sgh_state* s) {

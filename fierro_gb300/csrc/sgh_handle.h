@@ -1,0 +1,123 @@
+// The persistent solver handle and the helpers that build per-launch argument
+// records from it; shared by the C ABI (sgh_capi.cpp) and the discrete adjoint
+// (sgh_adjoint.cpp).  Internal, not part of include/fierro_sgh.h.
+#ifndef FIERRO_SGH_HANDLE_H
+#define FIERRO_SGH_HANDLE_H
+
+#include <algorithm>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "fierro_sgh.h"
+#include "sgh_device.h"
+#include "sgh_internal.h"
+
+#define CUDA_TRY(expr)                                                                            \
+  do {                                                                                            \
+    cudaError_t err_ = (expr);                                                                    \
+    if (err_ != cudaSuccess)                                                                      \
+      return set_error(err_ == cudaErrorMemoryAllocation ? FIERRO_ENOMEM : FIERRO_ECUDA, "%s: %s", \
+                       #expr, cudaGetErrorString(err_));                                          \
+  } while (0)
+
+#define TRY(expr)          \
+  do {                     \
+    int rc_ = (expr);      \
+    if (rc_) return rc_;   \
+  } while (0)
+
+namespace fierro {
+struct AdjState;
+}
+
+struct fierro_sgh {
+  fierro::HostTopo topo;
+  int64_t nn = 0, ne = 0;
+  int nmat = 0;
+  int fp_mode = FIERRO_FP_EXACT;
+  const fierro::KernelSet* ks = nullptr;
+  fierro::LoopParams lp{};
+  int rk_num_stages = 2;
+  double dt_start = 1e-5;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::vector<void*> allocations;
+  size_t dev_bytes = 0;
+  // mesh
+  int *d_nie = nullptr, *d_cin_start = nullptr, *d_cin = nullptr, *d_eie_start = nullptr, *d_eie = nullptr;
+  int* d_mat = nullptr;
+  unsigned char* d_bc = nullptr;
+  double* d_qtab = nullptr;
+  // state
+  double *d_node_mass = nullptr, *d_elem_mass = nullptr, *d_gamma = nullptr, *d_csmin = nullptr;
+  double* d_x[2][3] = {};
+  double* d_v[2][3] = {};
+  double* d_h[3] = {};
+  double *d_den = nullptr, *d_pres = nullptr, *d_sspd = nullptr, *d_vol = nullptr;
+  double* d_div[2] = {};  // see sgh_device.h: read by stage parity q, written at q^1
+  double* d_sie[2] = {};
+  double *d_bmat = nullptr, *d_force = nullptr;
+  long long* d_cfl = nullptr;
+  int ncfl = 0;
+  fierro::Ctrl* d_ctrl = nullptr;
+  double *d_energy_part = nullptr, *d_energy_out = nullptr;
+  // pinned double buffer for permuted transfers
+  double* h_stage[2] = {};
+  cudaEvent_t stage_ev[2] = {};
+  size_t stage_elems = 0;
+  // loop position
+  int base = 0;          // bin holding the state uploaded by set_state
+  long long enq_cycles = 0;  // cycles enqueued since set_state
+  int stage = 0;         // next RK stage of the current cycle (stage stepping)
+  bool has_state = false;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  fierro::AdjState* adj = nullptr;  // discrete-adjoint tape and checkpoints (sgh_adjoint.cpp)
+};
+
+namespace fierro {
+namespace hd {
+
+template <typename T>
+int dalloc(fierro_sgh* h, T** p, size_t count) {
+  void* q = nullptr;
+  size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+  cudaError_t err = cudaMalloc(&q, bytes);
+  if (err != cudaSuccess)
+    return set_error(FIERRO_ENOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(err));
+  h->allocations.push_back(q);
+  h->dev_bytes += bytes;
+  *p = static_cast<T*>(q);
+  return FIERRO_OK;
+}
+
+int upload_raw(fierro_sgh* h, void* dst, const void* src, size_t bytes);
+// Permuted upload through the pinned double buffer: dst[i] = src[map[i]*stride + off].
+int upload_gather(fierro_sgh* h, double* dst, const double* src, const std::vector<int64_t>& map,
+                  size_t stride, size_t off, int* slot);
+// Permuted download: out[map[i]*stride + off] = src[i].
+int download_scatter(fierro_sgh* h, double* out, const double* src, const std::vector<int64_t>& map,
+                     size_t stride, size_t off);
+int check_status(fierro_sgh* h);
+int cycles_done(fierro_sgh* h, long long* cyc);
+ForceArgs force_args(fierro_sgh* h, int rb, int q);
+NodeArgs node_args(fierro_sgh* h, int c, double alpha);
+ElemArgs elem_args(fierro_sgh* h, int cur_bin, int c, double alpha, int div_out);
+
+// Bins at a cycle boundary after `done` executed cycles: state bin and start bin.
+inline int bin_now(const fierro_sgh* h, long long cycles_done) { return (int)((h->base + cycles_done) & 1); }
+inline double stage_alpha(const fierro_sgh* h, int s) {
+  return 1.0 / ((double)h->rk_num_stages - (double)s);  // sgh_solve.cpp:353
+}
+// Divergence buffer a stage reads: the parity of the number of stages run since
+// set_state, which for stage s of a cycle with bin parity c is (c*S + s) & 1.
+inline int div_parity(const fierro_sgh* h, int c, int s) { return (c * h->rk_num_stages + s) & 1; }
+
+}  // namespace hd
+
+// Frees the adjoint's device memory (no-op without one).
+void adj_release(fierro_sgh* h);
+
+}  // namespace fierro
+
+#endif

@@ -313,3 +313,693 @@ __device__ __forceinline__ void hex_geometry(const double* __restrict__ x, const
     Sz = Sz + w[7] * b7;
   }
 }
+
+// Reverse mode of the corner normals: given Bbar[lid*3+dim] (the adjoint of
+// B(lid, dim)), accumulate the coordinate adjoints xbar, ybar, zbar[8].  B is
+// bilinear, B(p,c) = sum_t O[j_t] comb_t(I) / 12, and each unordered pair (p, j)
+// enters B(p) as O[j] cm and B(j) as -O[p] cm with one shared combo cm, so
+//   Obar[j] += g_p cm,  Obar[p] -= g_j cm,  Ibar[terms of cm] +-= g_p O[j] - g_j O[p]
+// with g = Bbar / 12 (multiply-adds fused: the adjoint has no parity target).
+__device__ __forceinline__ void hex_bmatrix_adjoint(const double* __restrict__ x, const double* __restrict__ y,
+    const double* __restrict__ z, const double* __restrict__ Bbar, double* __restrict__ xbar,
+    double* __restrict__ ybar, double* __restrict__ zbar) {
+  const double twelth = 1. / 12.;
+  {  // component 0: O = y, I = z
+    const double g0 = Bbar[0] * twelth;
+    const double g1 = Bbar[3] * twelth;
+    const double g2 = Bbar[6] * twelth;
+    const double g3 = Bbar[9] * twelth;
+    const double g4 = Bbar[12] * twelth;
+    const double g5 = Bbar[15] * twelth;
+    const double g6 = Bbar[18] * twelth;
+    const double g7 = Bbar[21] * twelth;
+    {  // pair (0,1)
+      const double cm = (((-z[2] - z[3]) + z[4]) + z[5]);
+      ybar[1] = fma(g0, cm, ybar[1]);
+      ybar[0] = fma(-g1, cm, ybar[0]);
+      const double wk = fma(g0, y[1], -(g1 * y[0]));
+      zbar[2] -= wk;
+      zbar[3] -= wk;
+      zbar[4] += wk;
+      zbar[5] += wk;
+    }
+    {  // pair (0,2)
+      const double cm = (z[1] - z[3]);
+      ybar[2] = fma(g0, cm, ybar[2]);
+      ybar[0] = fma(-g2, cm, ybar[0]);
+      const double wk = fma(g0, y[2], -(g2 * y[0]));
+      zbar[1] += wk;
+      zbar[3] -= wk;
+    }
+    {  // pair (0,3)
+      const double cm = (((z[1] + z[2]) - z[4]) - z[7]);
+      ybar[3] = fma(g0, cm, ybar[3]);
+      ybar[0] = fma(-g3, cm, ybar[0]);
+      const double wk = fma(g0, y[3], -(g3 * y[0]));
+      zbar[1] += wk;
+      zbar[2] += wk;
+      zbar[4] -= wk;
+      zbar[7] -= wk;
+    }
+    {  // pair (0,4)
+      const double cm = (((-z[1] + z[3]) - z[5]) + z[7]);
+      ybar[4] = fma(g0, cm, ybar[4]);
+      ybar[0] = fma(-g4, cm, ybar[0]);
+      const double wk = fma(g0, y[4], -(g4 * y[0]));
+      zbar[1] -= wk;
+      zbar[3] += wk;
+      zbar[5] -= wk;
+      zbar[7] += wk;
+    }
+    {  // pair (0,5)
+      const double cm = (-z[1] + z[4]);
+      ybar[5] = fma(g0, cm, ybar[5]);
+      ybar[0] = fma(-g5, cm, ybar[0]);
+      const double wk = fma(g0, y[5], -(g5 * y[0]));
+      zbar[1] -= wk;
+      zbar[4] += wk;
+    }
+    {  // pair (0,7)
+      const double cm = (z[3] - z[4]);
+      ybar[7] = fma(g0, cm, ybar[7]);
+      ybar[0] = fma(-g7, cm, ybar[0]);
+      const double wk = fma(g0, y[7], -(g7 * y[0]));
+      zbar[3] += wk;
+      zbar[4] -= wk;
+    }
+    {  // pair (1,2)
+      const double cm = (((-z[0] - z[3]) + z[5]) + z[6]);
+      ybar[2] = fma(g1, cm, ybar[2]);
+      ybar[1] = fma(-g2, cm, ybar[1]);
+      const double wk = fma(g1, y[2], -(g2 * y[1]));
+      zbar[0] -= wk;
+      zbar[3] -= wk;
+      zbar[5] += wk;
+      zbar[6] += wk;
+    }
+    {  // pair (1,3)
+      const double cm = (-z[0] + z[2]);
+      ybar[3] = fma(g1, cm, ybar[3]);
+      ybar[1] = fma(-g3, cm, ybar[1]);
+      const double wk = fma(g1, y[3], -(g3 * y[1]));
+      zbar[0] -= wk;
+      zbar[2] += wk;
+    }
+    {  // pair (1,4)
+      const double cm = (z[0] - z[5]);
+      ybar[4] = fma(g1, cm, ybar[4]);
+      ybar[1] = fma(-g4, cm, ybar[1]);
+      const double wk = fma(g1, y[4], -(g4 * y[1]));
+      zbar[0] += wk;
+      zbar[5] -= wk;
+    }
+    {  // pair (1,5)
+      const double cm = (((z[0] - z[2]) + z[4]) - z[6]);
+      ybar[5] = fma(g1, cm, ybar[5]);
+      ybar[1] = fma(-g5, cm, ybar[1]);
+      const double wk = fma(g1, y[5], -(g5 * y[1]));
+      zbar[0] += wk;
+      zbar[2] -= wk;
+      zbar[4] += wk;
+      zbar[6] -= wk;
+    }
+    {  // pair (1,6)
+      const double cm = (-z[2] + z[5]);
+      ybar[6] = fma(g1, cm, ybar[6]);
+      ybar[1] = fma(-g6, cm, ybar[1]);
+      const double wk = fma(g1, y[6], -(g6 * y[1]));
+      zbar[2] -= wk;
+      zbar[5] += wk;
+    }
+    {  // pair (2,3)
+      const double cm = (((-z[0] - z[1]) + z[6]) + z[7]);
+      ybar[3] = fma(g2, cm, ybar[3]);
+      ybar[2] = fma(-g3, cm, ybar[2]);
+      const double wk = fma(g2, y[3], -(g3 * y[2]));
+      zbar[0] -= wk;
+      zbar[1] -= wk;
+      zbar[6] += wk;
+      zbar[7] += wk;
+    }
+    {  // pair (2,5)
+      const double cm = (z[1] - z[6]);
+      ybar[5] = fma(g2, cm, ybar[5]);
+      ybar[2] = fma(-g5, cm, ybar[2]);
+      const double wk = fma(g2, y[5], -(g5 * y[2]));
+      zbar[1] += wk;
+      zbar[6] -= wk;
+    }
+    {  // pair (2,6)
+      const double cm = (((z[1] - z[3]) + z[5]) - z[7]);
+      ybar[6] = fma(g2, cm, ybar[6]);
+      ybar[2] = fma(-g6, cm, ybar[2]);
+      const double wk = fma(g2, y[6], -(g6 * y[2]));
+      zbar[1] += wk;
+      zbar[3] -= wk;
+      zbar[5] += wk;
+      zbar[7] -= wk;
+    }
+    {  // pair (2,7)
+      const double cm = (-z[3] + z[6]);
+      ybar[7] = fma(g2, cm, ybar[7]);
+      ybar[2] = fma(-g7, cm, ybar[2]);
+      const double wk = fma(g2, y[7], -(g7 * y[2]));
+      zbar[3] -= wk;
+      zbar[6] += wk;
+    }
+    {  // pair (3,4)
+      const double cm = (-z[0] + z[7]);
+      ybar[4] = fma(g3, cm, ybar[4]);
+      ybar[3] = fma(-g4, cm, ybar[3]);
+      const double wk = fma(g3, y[4], -(g4 * y[3]));
+      zbar[0] -= wk;
+      zbar[7] += wk;
+    }
+    {  // pair (3,6)
+      const double cm = (z[2] - z[7]);
+      ybar[6] = fma(g3, cm, ybar[6]);
+      ybar[3] = fma(-g6, cm, ybar[3]);
+      const double wk = fma(g3, y[6], -(g6 * y[3]));
+      zbar[2] += wk;
+      zbar[7] -= wk;
+    }
+    {  // pair (3,7)
+      const double cm = (((-z[0] + z[2]) - z[4]) + z[6]);
+      ybar[7] = fma(g3, cm, ybar[7]);
+      ybar[3] = fma(-g7, cm, ybar[3]);
+      const double wk = fma(g3, y[7], -(g7 * y[3]));
+      zbar[0] -= wk;
+      zbar[2] += wk;
+      zbar[4] -= wk;
+      zbar[6] += wk;
+    }
+    {  // pair (4,5)
+      const double cm = (((-z[0] - z[1]) + z[6]) + z[7]);
+      ybar[5] = fma(g4, cm, ybar[5]);
+      ybar[4] = fma(-g5, cm, ybar[4]);
+      const double wk = fma(g4, y[5], -(g5 * y[4]));
+      zbar[0] -= wk;
+      zbar[1] -= wk;
+      zbar[6] += wk;
+      zbar[7] += wk;
+    }
+    {  // pair (4,6)
+      const double cm = (-z[5] + z[7]);
+      ybar[6] = fma(g4, cm, ybar[6]);
+      ybar[4] = fma(-g6, cm, ybar[4]);
+      const double wk = fma(g4, y[6], -(g6 * y[4]));
+      zbar[5] -= wk;
+      zbar[7] += wk;
+    }
+    {  // pair (4,7)
+      const double cm = (((z[0] + z[3]) - z[5]) - z[6]);
+      ybar[7] = fma(g4, cm, ybar[7]);
+      ybar[4] = fma(-g7, cm, ybar[4]);
+      const double wk = fma(g4, y[7], -(g7 * y[4]));
+      zbar[0] += wk;
+      zbar[3] += wk;
+      zbar[5] -= wk;
+      zbar[6] -= wk;
+    }
+    {  // pair (5,6)
+      const double cm = (((-z[1] - z[2]) + z[4]) + z[7]);
+      ybar[6] = fma(g5, cm, ybar[6]);
+      ybar[5] = fma(-g6, cm, ybar[5]);
+      const double wk = fma(g5, y[6], -(g6 * y[5]));
+      zbar[1] -= wk;
+      zbar[2] -= wk;
+      zbar[4] += wk;
+      zbar[7] += wk;
+    }
+    {  // pair (5,7)
+      const double cm = (z[4] - z[6]);
+      ybar[7] = fma(g5, cm, ybar[7]);
+      ybar[5] = fma(-g7, cm, ybar[5]);
+      const double wk = fma(g5, y[7], -(g7 * y[5]));
+      zbar[4] += wk;
+      zbar[6] -= wk;
+    }
+    {  // pair (6,7)
+      const double cm = (((-z[2] - z[3]) + z[4]) + z[5]);
+      ybar[7] = fma(g6, cm, ybar[7]);
+      ybar[6] = fma(-g7, cm, ybar[6]);
+      const double wk = fma(g6, y[7], -(g7 * y[6]));
+      zbar[2] -= wk;
+      zbar[3] -= wk;
+      zbar[4] += wk;
+      zbar[5] += wk;
+    }
+  }
+  {  // component 1: O = z, I = x
+    const double g0 = Bbar[1] * twelth;
+    const double g1 = Bbar[4] * twelth;
+    const double g2 = Bbar[7] * twelth;
+    const double g3 = Bbar[10] * twelth;
+    const double g4 = Bbar[13] * twelth;
+    const double g5 = Bbar[16] * twelth;
+    const double g6 = Bbar[19] * twelth;
+    const double g7 = Bbar[22] * twelth;
+    {  // pair (0,1)
+      const double cm = (((-x[2] - x[3]) + x[4]) + x[5]);
+      zbar[1] = fma(g0, cm, zbar[1]);
+      zbar[0] = fma(-g1, cm, zbar[0]);
+      const double wk = fma(g0, z[1], -(g1 * z[0]));
+      xbar[2] -= wk;
+      xbar[3] -= wk;
+      xbar[4] += wk;
+      xbar[5] += wk;
+    }
+    {  // pair (0,2)
+      const double cm = (x[1] - x[3]);
+      zbar[2] = fma(g0, cm, zbar[2]);
+      zbar[0] = fma(-g2, cm, zbar[0]);
+      const double wk = fma(g0, z[2], -(g2 * z[0]));
+      xbar[1] += wk;
+      xbar[3] -= wk;
+    }
+    {  // pair (0,3)
+      const double cm = (((x[1] + x[2]) - x[4]) - x[7]);
+      zbar[3] = fma(g0, cm, zbar[3]);
+      zbar[0] = fma(-g3, cm, zbar[0]);
+      const double wk = fma(g0, z[3], -(g3 * z[0]));
+      xbar[1] += wk;
+      xbar[2] += wk;
+      xbar[4] -= wk;
+      xbar[7] -= wk;
+    }
+    {  // pair (0,4)
+      const double cm = (((-x[1] + x[3]) - x[5]) + x[7]);
+      zbar[4] = fma(g0, cm, zbar[4]);
+      zbar[0] = fma(-g4, cm, zbar[0]);
+      const double wk = fma(g0, z[4], -(g4 * z[0]));
+      xbar[1] -= wk;
+      xbar[3] += wk;
+      xbar[5] -= wk;
+      xbar[7] += wk;
+    }
+    {  // pair (0,5)
+      const double cm = (-x[1] + x[4]);
+      zbar[5] = fma(g0, cm, zbar[5]);
+      zbar[0] = fma(-g5, cm, zbar[0]);
+      const double wk = fma(g0, z[5], -(g5 * z[0]));
+      xbar[1] -= wk;
+      xbar[4] += wk;
+    }
+    {  // pair (0,7)
+      const double cm = (x[3] - x[4]);
+      zbar[7] = fma(g0, cm, zbar[7]);
+      zbar[0] = fma(-g7, cm, zbar[0]);
+      const double wk = fma(g0, z[7], -(g7 * z[0]));
+      xbar[3] += wk;
+      xbar[4] -= wk;
+    }
+    {  // pair (1,2)
+      const double cm = (((-x[0] - x[3]) + x[5]) + x[6]);
+      zbar[2] = fma(g1, cm, zbar[2]);
+      zbar[1] = fma(-g2, cm, zbar[1]);
+      const double wk = fma(g1, z[2], -(g2 * z[1]));
+      xbar[0] -= wk;
+      xbar[3] -= wk;
+      xbar[5] += wk;
+      xbar[6] += wk;
+    }
+    {  // pair (1,3)
+      const double cm = (-x[0] + x[2]);
+      zbar[3] = fma(g1, cm, zbar[3]);
+      zbar[1] = fma(-g3, cm, zbar[1]);
+      const double wk = fma(g1, z[3], -(g3 * z[1]));
+      xbar[0] -= wk;
+      xbar[2] += wk;
+    }
+    {  // pair (1,4)
+      const double cm = (x[0] - x[5]);
+      zbar[4] = fma(g1, cm, zbar[4]);
+      zbar[1] = fma(-g4, cm, zbar[1]);
+      const double wk = fma(g1, z[4], -(g4 * z[1]));
+      xbar[0] += wk;
+      xbar[5] -= wk;
+    }
+    {  // pair (1,5)
+      const double cm = (((x[0] - x[2]) + x[4]) - x[6]);
+      zbar[5] = fma(g1, cm, zbar[5]);
+      zbar[1] = fma(-g5, cm, zbar[1]);
+      const double wk = fma(g1, z[5], -(g5 * z[1]));
+      xbar[0] += wk;
+      xbar[2] -= wk;
+      xbar[4] += wk;
+      xbar[6] -= wk;
+    }
+    {  // pair (1,6)
+      const double cm = (-x[2] + x[5]);
+      zbar[6] = fma(g1, cm, zbar[6]);
+      zbar[1] = fma(-g6, cm, zbar[1]);
+      const double wk = fma(g1, z[6], -(g6 * z[1]));
+      xbar[2] -= wk;
+      xbar[5] += wk;
+    }
+    {  // pair (2,3)
+      const double cm = (((-x[0] - x[1]) + x[6]) + x[7]);
+      zbar[3] = fma(g2, cm, zbar[3]);
+      zbar[2] = fma(-g3, cm, zbar[2]);
+      const double wk = fma(g2, z[3], -(g3 * z[2]));
+      xbar[0] -= wk;
+      xbar[1] -= wk;
+      xbar[6] += wk;
+      xbar[7] += wk;
+    }
+    {  // pair (2,5)
+      const double cm = (x[1] - x[6]);
+      zbar[5] = fma(g2, cm, zbar[5]);
+      zbar[2] = fma(-g5, cm, zbar[2]);
+      const double wk = fma(g2, z[5], -(g5 * z[2]));
+      xbar[1] += wk;
+      xbar[6] -= wk;
+    }
+    {  // pair (2,6)
+      const double cm = (((x[1] - x[3]) + x[5]) - x[7]);
+      zbar[6] = fma(g2, cm, zbar[6]);
+      zbar[2] = fma(-g6, cm, zbar[2]);
+      const double wk = fma(g2, z[6], -(g6 * z[2]));
+      xbar[1] += wk;
+      xbar[3] -= wk;
+      xbar[5] += wk;
+      xbar[7] -= wk;
+    }
+    {  // pair (2,7)
+      const double cm = (-x[3] + x[6]);
+      zbar[7] = fma(g2, cm, zbar[7]);
+      zbar[2] = fma(-g7, cm, zbar[2]);
+      const double wk = fma(g2, z[7], -(g7 * z[2]));
+      xbar[3] -= wk;
+      xbar[6] += wk;
+    }
+    {  // pair (3,4)
+      const double cm = (-x[0] + x[7]);
+      zbar[4] = fma(g3, cm, zbar[4]);
+      zbar[3] = fma(-g4, cm, zbar[3]);
+      const double wk = fma(g3, z[4], -(g4 * z[3]));
+      xbar[0] -= wk;
+      xbar[7] += wk;
+    }
+    {  // pair (3,6)
+      const double cm = (x[2] - x[7]);
+      zbar[6] = fma(g3, cm, zbar[6]);
+      zbar[3] = fma(-g6, cm, zbar[3]);
+      const double wk = fma(g3, z[6], -(g6 * z[3]));
+      xbar[2] += wk;
+      xbar[7] -= wk;
+    }
+    {  // pair (3,7)
+      const double cm = (((-x[0] + x[2]) - x[4]) + x[6]);
+      zbar[7] = fma(g3, cm, zbar[7]);
+      zbar[3] = fma(-g7, cm, zbar[3]);
+      const double wk = fma(g3, z[7], -(g7 * z[3]));
+      xbar[0] -= wk;
+      xbar[2] += wk;
+      xbar[4] -= wk;
+      xbar[6] += wk;
+    }
+    {  // pair (4,5)
+      const double cm = (((-x[0] - x[1]) + x[6]) + x[7]);
+      zbar[5] = fma(g4, cm, zbar[5]);
+      zbar[4] = fma(-g5, cm, zbar[4]);
+      const double wk = fma(g4, z[5], -(g5 * z[4]));
+      xbar[0] -= wk;
+      xbar[1] -= wk;
+      xbar[6] += wk;
+      xbar[7] += wk;
+    }
+    {  // pair (4,6)
+      const double cm = (-x[5] + x[7]);
+      zbar[6] = fma(g4, cm, zbar[6]);
+      zbar[4] = fma(-g6, cm, zbar[4]);
+      const double wk = fma(g4, z[6], -(g6 * z[4]));
+      xbar[5] -= wk;
+      xbar[7] += wk;
+    }
+    {  // pair (4,7)
+      const double cm = (((x[0] + x[3]) - x[5]) - x[6]);
+      zbar[7] = fma(g4, cm, zbar[7]);
+      zbar[4] = fma(-g7, cm, zbar[4]);
+      const double wk = fma(g4, z[7], -(g7 * z[4]));
+      xbar[0] += wk;
+      xbar[3] += wk;
+      xbar[5] -= wk;
+      xbar[6] -= wk;
+    }
+    {  // pair (5,6)
+      const double cm = (((-x[1] - x[2]) + x[4]) + x[7]);
+      zbar[6] = fma(g5, cm, zbar[6]);
+      zbar[5] = fma(-g6, cm, zbar[5]);
+      const double wk = fma(g5, z[6], -(g6 * z[5]));
+      xbar[1] -= wk;
+      xbar[2] -= wk;
+      xbar[4] += wk;
+      xbar[7] += wk;
+    }
+    {  // pair (5,7)
+      const double cm = (x[4] - x[6]);
+      zbar[7] = fma(g5, cm, zbar[7]);
+      zbar[5] = fma(-g7, cm, zbar[5]);
+      const double wk = fma(g5, z[7], -(g7 * z[5]));
+      xbar[4] += wk;
+      xbar[6] -= wk;
+    }
+    {  // pair (6,7)
+      const double cm = (((-x[2] - x[3]) + x[4]) + x[5]);
+      zbar[7] = fma(g6, cm, zbar[7]);
+      zbar[6] = fma(-g7, cm, zbar[6]);
+      const double wk = fma(g6, z[7], -(g7 * z[6]));
+      xbar[2] -= wk;
+      xbar[3] -= wk;
+      xbar[4] += wk;
+      xbar[5] += wk;
+    }
+  }
+  {  // component 2: O = x, I = y
+    const double g0 = Bbar[2] * twelth;
+    const double g1 = Bbar[5] * twelth;
+    const double g2 = Bbar[8] * twelth;
+    const double g3 = Bbar[11] * twelth;
+    const double g4 = Bbar[14] * twelth;
+    const double g5 = Bbar[17] * twelth;
+    const double g6 = Bbar[20] * twelth;
+    const double g7 = Bbar[23] * twelth;
+    {  // pair (0,1)
+      const double cm = (((-y[2] - y[3]) + y[4]) + y[5]);
+      xbar[1] = fma(g0, cm, xbar[1]);
+      xbar[0] = fma(-g1, cm, xbar[0]);
+      const double wk = fma(g0, x[1], -(g1 * x[0]));
+      ybar[2] -= wk;
+      ybar[3] -= wk;
+      ybar[4] += wk;
+      ybar[5] += wk;
+    }
+    {  // pair (0,2)
+      const double cm = (y[1] - y[3]);
+      xbar[2] = fma(g0, cm, xbar[2]);
+      xbar[0] = fma(-g2, cm, xbar[0]);
+      const double wk = fma(g0, x[2], -(g2 * x[0]));
+      ybar[1] += wk;
+      ybar[3] -= wk;
+    }
+    {  // pair (0,3)
+      const double cm = (((y[1] + y[2]) - y[4]) - y[7]);
+      xbar[3] = fma(g0, cm, xbar[3]);
+      xbar[0] = fma(-g3, cm, xbar[0]);
+      const double wk = fma(g0, x[3], -(g3 * x[0]));
+      ybar[1] += wk;
+      ybar[2] += wk;
+      ybar[4] -= wk;
+      ybar[7] -= wk;
+    }
+    {  // pair (0,4)
+      const double cm = (((-y[1] + y[3]) - y[5]) + y[7]);
+      xbar[4] = fma(g0, cm, xbar[4]);
+      xbar[0] = fma(-g4, cm, xbar[0]);
+      const double wk = fma(g0, x[4], -(g4 * x[0]));
+      ybar[1] -= wk;
+      ybar[3] += wk;
+      ybar[5] -= wk;
+      ybar[7] += wk;
+    }
+    {  // pair (0,5)
+      const double cm = (-y[1] + y[4]);
+      xbar[5] = fma(g0, cm, xbar[5]);
+      xbar[0] = fma(-g5, cm, xbar[0]);
+      const double wk = fma(g0, x[5], -(g5 * x[0]));
+      ybar[1] -= wk;
+      ybar[4] += wk;
+    }
+    {  // pair (0,7)
+      const double cm = (y[3] - y[4]);
+      xbar[7] = fma(g0, cm, xbar[7]);
+      xbar[0] = fma(-g7, cm, xbar[0]);
+      const double wk = fma(g0, x[7], -(g7 * x[0]));
+      ybar[3] += wk;
+      ybar[4] -= wk;
+    }
+    {  // pair (1,2)
+      const double cm = (((-y[0] - y[3]) + y[5]) + y[6]);
+      xbar[2] = fma(g1, cm, xbar[2]);
+      xbar[1] = fma(-g2, cm, xbar[1]);
+      const double wk = fma(g1, x[2], -(g2 * x[1]));
+      ybar[0] -= wk;
+      ybar[3] -= wk;
+      ybar[5] += wk;
+      ybar[6] += wk;
+    }
+    {  // pair (1,3)
+      const double cm = (-y[0] + y[2]);
+      xbar[3] = fma(g1, cm, xbar[3]);
+      xbar[1] = fma(-g3, cm, xbar[1]);
+      const double wk = fma(g1, x[3], -(g3 * x[1]));
+      ybar[0] -= wk;
+      ybar[2] += wk;
+    }
+    {  // pair (1,4)
+      const double cm = (y[0] - y[5]);
+      xbar[4] = fma(g1, cm, xbar[4]);
+      xbar[1] = fma(-g4, cm, xbar[1]);
+      const double wk = fma(g1, x[4], -(g4 * x[1]));
+      ybar[0] += wk;
+      ybar[5] -= wk;
+    }
+    {  // pair (1,5)
+      const double cm = (((y[0] - y[2]) + y[4]) - y[6]);
+      xbar[5] = fma(g1, cm, xbar[5]);
+      xbar[1] = fma(-g5, cm, xbar[1]);
+      const double wk = fma(g1, x[5], -(g5 * x[1]));
+      ybar[0] += wk;
+      ybar[2] -= wk;
+      ybar[4] += wk;
+      ybar[6] -= wk;
+    }
+    {  // pair (1,6)
+      const double cm = (-y[2] + y[5]);
+      xbar[6] = fma(g1, cm, xbar[6]);
+      xbar[1] = fma(-g6, cm, xbar[1]);
+      const double wk = fma(g1, x[6], -(g6 * x[1]));
+      ybar[2] -= wk;
+      ybar[5] += wk;
+    }
+    {  // pair (2,3)
+      const double cm = (((-y[0] - y[1]) + y[6]) + y[7]);
+      xbar[3] = fma(g2, cm, xbar[3]);
+      xbar[2] = fma(-g3, cm, xbar[2]);
+      const double wk = fma(g2, x[3], -(g3 * x[2]));
+      ybar[0] -= wk;
+      ybar[1] -= wk;
+      ybar[6] += wk;
+      ybar[7] += wk;
+    }
+    {  // pair (2,5)
+      const double cm = (y[1] - y[6]);
+      xbar[5] = fma(g2, cm, xbar[5]);
+      xbar[2] = fma(-g5, cm, xbar[2]);
+      const double wk = fma(g2, x[5], -(g5 * x[2]));
+      ybar[1] += wk;
+      ybar[6] -= wk;
+    }
+    {  // pair (2,6)
+      const double cm = (((y[1] - y[3]) + y[5]) - y[7]);
+      xbar[6] = fma(g2, cm, xbar[6]);
+      xbar[2] = fma(-g6, cm, xbar[2]);
+      const double wk = fma(g2, x[6], -(g6 * x[2]));
+      ybar[1] += wk;
+      ybar[3] -= wk;
+      ybar[5] += wk;
+      ybar[7] -= wk;
+    }
+    {  // pair (2,7)
+      const double cm = (-y[3] + y[6]);
+      xbar[7] = fma(g2, cm, xbar[7]);
+      xbar[2] = fma(-g7, cm, xbar[2]);
+      const double wk = fma(g2, x[7], -(g7 * x[2]));
+      ybar[3] -= wk;
+      ybar[6] += wk;
+    }
+    {  // pair (3,4)
+      const double cm = (-y[0] + y[7]);
+      xbar[4] = fma(g3, cm, xbar[4]);
+      xbar[3] = fma(-g4, cm, xbar[3]);
+      const double wk = fma(g3, x[4], -(g4 * x[3]));
+      ybar[0] -= wk;
+      ybar[7] += wk;
+    }
+    {  // pair (3,6)
+      const double cm = (y[2] - y[7]);
+      xbar[6] = fma(g3, cm, xbar[6]);
+      xbar[3] = fma(-g6, cm, xbar[3]);
+      const double wk = fma(g3, x[6], -(g6 * x[3]));
+      ybar[2] += wk;
+      ybar[7] -= wk;
+    }
+    {  // pair (3,7)
+      const double cm = (((-y[0] + y[2]) - y[4]) + y[6]);
+      xbar[7] = fma(g3, cm, xbar[7]);
+      xbar[3] = fma(-g7, cm, xbar[3]);
+      const double wk = fma(g3, x[7], -(g7 * x[3]));
+      ybar[0] -= wk;
+      ybar[2] += wk;
+      ybar[4] -= wk;
+      ybar[6] += wk;
+    }
+    {  // pair (4,5)
+      const double cm = (((-y[0] - y[1]) + y[6]) + y[7]);
+      xbar[5] = fma(g4, cm, xbar[5]);
+      xbar[4] = fma(-g5, cm, xbar[4]);
+      const double wk = fma(g4, x[5], -(g5 * x[4]));
+      ybar[0] -= wk;
+      ybar[1] -= wk;
+      ybar[6] += wk;
+      ybar[7] += wk;
+    }
+    {  // pair (4,6)
+      const double cm = (-y[5] + y[7]);
+      xbar[6] = fma(g4, cm, xbar[6]);
+      xbar[4] = fma(-g6, cm, xbar[4]);
+      const double wk = fma(g4, x[6], -(g6 * x[4]));
+      ybar[5] -= wk;
+      ybar[7] += wk;
+    }
+    {  // pair (4,7)
+      const double cm = (((y[0] + y[3]) - y[5]) - y[6]);
+      xbar[7] = fma(g4, cm, xbar[7]);
+      xbar[4] = fma(-g7, cm, xbar[4]);
+      const double wk = fma(g4, x[7], -(g7 * x[4]));
+      ybar[0] += wk;
+      ybar[3] += wk;
+      ybar[5] -= wk;
+      ybar[6] -= wk;
+    }
+    {  // pair (5,6)
+      const double cm = (((-y[1] - y[2]) + y[4]) + y[7]);
+      xbar[6] = fma(g5, cm, xbar[6]);
+      xbar[5] = fma(-g6, cm, xbar[5]);
+      const double wk = fma(g5, x[6], -(g6 * x[5]));
+      ybar[1] -= wk;
+      ybar[2] -= wk;
+      ybar[4] += wk;
+      ybar[7] += wk;
+    }
+    {  // pair (5,7)
+      const double cm = (y[4] - y[6]);
+      xbar[7] = fma(g5, cm, xbar[7]);
+      xbar[5] = fma(-g7, cm, xbar[5]);
+      const double wk = fma(g5, x[7], -(g7 * x[5]));
+      ybar[4] += wk;
+      ybar[6] -= wk;
+    }
+    {  // pair (6,7)
+      const double cm = (((-y[2] - y[3]) + y[4]) + y[5]);
+      xbar[7] = fma(g6, cm, xbar[7]);
+      xbar[6] = fma(-g7, cm, xbar[6]);
+      const double wk = fma(g6, x[7], -(g7 * x[6]));
+      ybar[2] -= wk;
+      ybar[3] -= wk;
+      ybar[4] += wk;
+      ybar[5] += wk;
+    }
+  }
+}

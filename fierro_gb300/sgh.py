@@ -105,6 +105,11 @@ def _load():
     lib.fierro_batch_num_instances.restype = i64
     lib.fierro_batch_device_bytes.argtypes = [vp]
     lib.fierro_batch_device_bytes.restype = i64
+    lib.fierro_adj_forward.argtypes = [vp, vp, vp, i64, i64, C.POINTER(i64)]
+    lib.fierro_adj_backward.argtypes = [vp, vp, vp, vp, vp]
+    lib.fierro_adj_verify.argtypes = [vp, C.c_int]
+    lib.fierro_adj_stats.argtypes = [vp, C.POINTER(i64), i64]
+    lib.fierro_adj_release.argtypes = [vp]
     return lib
 
 
@@ -291,6 +296,59 @@ class SGHSolver:
     @property
     def device_bytes(self) -> int:
         return int(_lib.fierro_sgh_device_bytes(self.h))
+
+    def adj_forward(self, sie0=None, gamma=None, cycles: int = 1, ckpt_every: int = 20) -> int:
+        """fierro_adj_forward: replace the current state's sie (and per-element gamma)
+        by the parameters, recompute pressure and sound speed, run `cycles` cycles
+        keeping checkpoints every `ckpt_every`.  Returns the cycles run."""
+        s0 = _f64(sie0, (self.ne,))
+        g0 = _f64(gamma, (self.ne,)) if gamma is None or np.ndim(gamma) else np.full(self.ne, float(gamma))
+        ran = C.c_int64(0)
+        _check(_lib.fierro_adj_forward(self.h, None if s0 is None else s0.ctypes.data,
+                                       None if g0 is None else g0.ctypes.data, cycles, ckpt_every, C.byref(ran)))
+        return ran.value
+
+
+    def adj_backward(self, den=None, pres=None, sie=None, sspd=None, vol=None, coords=None, vel=None):
+        """fierro_adj_backward: adjoints of the final state's fields in, returns
+        (d/d sie0 [Ne], d/d gamma per element [Ne], d/d initial velocity [Nn,3])."""
+        keep = {k: _f64(v) for k, v in dict(den=den, pres=pres, sie=sie, sspd=sspd, vol=vol, coords=coords,
+                                             vel=vel).items()}
+        seed = AdjSeed(*[None if keep[k] is None else keep[k].ctypes.data for k, _ in AdjSeed._fields_])
+        sb, gb, vb = np.empty(self.ne), np.empty(self.ne), np.empty((self.nn, 3))
+        _check(_lib.fierro_adj_backward(self.h, C.byref(seed), sb.ctypes.data, gb.ctypes.data, vb.ctypes.data))
+        return sb, gb, vb
+
+
+    def adj_verify(self, enable: bool = True):
+        _check(_lib.fierro_adj_verify(self.h, 1 if enable else 0))
+
+
+    def adj_stats(self) -> dict:
+        out = (C.c_int64 * len(ADJ_STATS))()
+        _check(_lib.fierro_adj_stats(self.h, out, len(ADJ_STATS)))
+        return dict(zip(ADJ_STATS, list(out)))
+
+
+    def adj_release(self):
+        _check(_lib.fierro_adj_release(self.h))
+
+
+class AdjSeed(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k in ("den", "pres", "sie", "sspd", "vol", "coords", "vel")]
+
+
+ADJ_STATS = ("cycles", "ckpt_every", "segments", "tape_bytes", "ckpt_bytes", "device_bytes", "force_mismatches",
+             "status", "dt_cfl_cycles", "dt_growth_cycles", "dt_other_cycles")
+
+
+def _f64(a, shape=None):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None and a.size != int(np.prod(shape)):
+        raise ValueError("expected %s values, got %d" % (shape, a.size))
+    return a
 
 
 class BatchInstance(C.Structure):

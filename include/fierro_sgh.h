@@ -230,6 +230,64 @@ int fierro_energy_tally_noalloc(const double* elem_mass, const double* elem_sie,
  * throughput, in fused multiply-adds per second (one FMA = 2 FLOP). */
 int fierro_measure_fp64_rate(double* dfma_per_second);
 
+/* ---- discrete adjoint of the cycle loop ------------------------------------
+ * No counterpart in the reference, which has no adjoint; these differentiate the
+ * loop that fierro_sgh_run executes (sgh_solve.cpp:125-634), with the
+ * parameters an element's initial specific internal energy and gamma
+ * (elem_statev[e][0]).  The pair is shaped like a torch.autograd.Function:
+ * forward runs the loop and keeps what backward needs; backward maps adjoints
+ * of the final state to adjoints of the parameters.  Exact arithmetic mode only
+ * (FIERRO_ENOTSUP otherwise).
+ *
+ * fierro_adj_forward: from the handle's current state (a cycle boundary, e.g.
+ * right after set_state), replaces elem_sie (bin 1) by sie0[Ne] and gamma by
+ * gamma[Ne] (either may be NULL: keep the current values), recomputes pressure
+ * and sound speed from them with the ideal-gas EOS, then runs `cycles` cycles
+ * exactly as fierro_sgh_run does, keeping a device-resident checkpoint every
+ * ckpt_every cycles.  The final state is then read with fierro_sgh_get_state.
+ * Device memory: checkpoints (6 Nn + 30 Ne doubles each) plus a replay tape of
+ * ckpt_every cycles ((2 ckpt_every + 1)(9 Nn + 30 Ne) + 48 ckpt_every Ne doubles
+ * for two RK stages); FIERRO_ENOMEM if it does not fit. */
+int fierro_adj_forward(fierro_sgh* h, const double* sie0, const double* gamma, int64_t cycles,
+                       int64_t ckpt_every, int64_t* cycles_run);
+
+/* Adjoints of the final state (d J / d field), host arrays in the caller's
+ * numbering; NULL fields are zero.  Element fields [Ne]; coords and vel
+ * [Nn][3] (bin 1). */
+typedef struct {
+  const double* den;
+  const double* pres;
+  const double* sie;
+  const double* sspd;
+  const double* vol;
+  const double* coords;
+  const double* vel;
+} fierro_adj_seed;
+
+/* fierro_adj_backward: replays each checkpoint segment (bit-identical to the
+ * forward) and runs the reverse pass.  Writes d J / d sie0 [Ne], d J / d gamma
+ * [Ne] (per element; the derivative for one material-wide gamma is their sum)
+ * and d J / d initial node velocity [Nn][3]; any output may be NULL.  Switches
+ * of the forward (limiter, Mach switch, compression, CFL minimiser, dt clamps)
+ * are differentiated on the side the forward took.  The state must be the one
+ * fierro_adj_forward left; backward may be called repeatedly with other seeds. */
+int fierro_adj_backward(fierro_sgh* h, const fierro_adj_seed* seed, double* sie0_bar, double* gamma_bar,
+                        double* vel0_bar);
+
+/* enable != 0: backward also recomputes every corner force of the replay inside
+ * the reverse force kernel and fails (FIERRO_ENUMERIC) unless all match bit for
+ * bit; a self-check of the reverse pass's forward values. */
+int fierro_adj_verify(fierro_sgh* h, int enable);
+
+/* out[0..n), n <= 11: cycles of the last forward, checkpoint interval,
+ * segments, tape bytes, checkpoint bytes, total adjoint device bytes; of the last
+ * backward: force mismatches, status bits, and the number of cycles whose dt came
+ * from the CFL minimum, from the growth cap, and from the other clamps. */
+int fierro_adj_stats(const fierro_sgh* h, int64_t* out, int64_t n);
+
+/* Frees the adjoint's device memory (also done by fierro_sgh_destroy). */
+int fierro_adj_release(fierro_sgh* h);
+
 #ifdef __cplusplus
 }
 #endif

@@ -30,6 +30,10 @@ extern "C" void geom(const double* x, const double* y, const double* z, const do
                      const double* w, double* bmat, double* out) {
   hex_geometry(x, y, z, u, v, w, bmat, 1, 0, out[0], out[1], out[2], out[3]);
 }
+extern "C" void bmat_adj(const double* x, const double* y, const double* z, const double* bbar, double* out) {
+  for (int i = 0; i < 24; ++i) out[i] = 0.0;
+  hex_bmatrix_adjoint(x, y, z, bbar, out, out + 8, out + 16);
+}
 extern "C" double cfl_min(const double* x, const double* y, const double* z) {
   double sx[8], sy[8], sz[8];
   for (int l = 0; l < 8; ++l) { sx[l] = x[l]; sy[l] = y[l]; sz[l] = z[l]; }
@@ -48,6 +52,7 @@ def geomlib(tmp_path_factory):
                     os.path.join(ROOT, "fierro_gb300", "csrc"), str(src), "-o", str(so)], check=True)
     lib = C.CDLL(str(so))
     lib.geom.argtypes = [C.c_void_p] * 8
+    lib.bmat_adj.argtypes = [C.c_void_p] * 5
     lib.cfl_min.argtypes = [C.c_void_p] * 3
     lib.cfl_min.restype = C.c_double
     return lib
@@ -134,3 +139,48 @@ def test_cfl_screening_is_exact(geomlib):
     for h in cases:
         got = _cfl(geomlib, h)
         assert got == exact_min_d2(h), h
+
+
+def test_bmatrix_adjoint(geomlib, oracle_built):
+    """hex_bmatrix_adjoint (the adjoint's corner-normal reverse) equals the
+    gradient of sum(Bbar * B(x)): B is quadratic in the coordinates, so a central
+    difference is exact up to rounding."""
+    from oracle import orc
+    rng = np.random.default_rng(11)
+    base = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], float)
+    for trial in range(20):
+        X = base + rng.uniform(-0.25, 0.25, base.shape)
+        bbar = rng.normal(size=24)
+        cols = [np.ascontiguousarray(X[:, d]) for d in range(3)]
+        out = np.zeros(24)
+        geomlib.bmat_adj(cols[0].ctypes.data, cols[1].ctypes.data, cols[2].ctypes.data, bbar.ctypes.data,
+                         out.ctypes.data)
+        h = 1e-3
+        fd = np.zeros(24)
+        for d in range(3):
+            for p in range(8):
+                Xp, Xm = X.copy(), X.copy()
+                Xp[p, d] += h
+                Xm[p, d] -= h
+                Bp = orc.bmatrix(*[Xp[:, k] for k in range(3)]).ravel()
+                Bm = orc.bmatrix(*[Xm[:, k] for k in range(3)]).ravel()
+                fd[d * 8 + p] = (np.dot(bbar, Bp) - np.dot(bbar, Bm)) / (2 * h)
+        assert np.max(np.abs(out - fd)) <= 1e-10 * max(1.0, np.max(np.abs(fd))), trial
+
+
+def test_volume_gradient_is_bmatrix(oracle_built):
+    """dV/dx_p = B_p for the exact hex volume (the adjoint's volume reverse)."""
+    from oracle import orc
+    rng = np.random.default_rng(12)
+    base = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], float)
+    for trial in range(10):
+        X = base + rng.uniform(-0.25, 0.25, base.shape)
+        B = orc.bmatrix(*[X[:, k] for k in range(3)])
+        h = 1e-5
+        for p in range(8):
+            for d in range(3):
+                Xp, Xm = X.copy(), X.copy()
+                Xp[p, d] += h
+                Xm[p, d] -= h
+                g = (orc.vol_hex(*[Xp[:, k] for k in range(3)]) - orc.vol_hex(*[Xm[:, k] for k in range(3)])) / (2 * h)
+                assert abs(g - B[p, d]) <= 1e-8, (trial, p, d)
