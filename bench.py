@@ -48,6 +48,12 @@ def parse(argv=None):
                     help="run the batched-ensemble benchmark instead (instances/s vs looping the plain solver)")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--batch-cycles", type=int, default=100)
+    ap.add_argument("--adjoint", action="store_true",
+                    help="discrete adjoint: Sedov 64^3, 400 cycles, J = sum M (rho - rho_target)^2")
+    ap.add_argument("--adj-n", type=int, default=64)
+    ap.add_argument("--adj-cycles", type=int, default=400)
+    ap.add_argument("--adj-ckpt", type=int, default=20)
+    ap.add_argument("--adj-dirs", type=int, default=16)
     return ap.parse_args(argv)
 
 
@@ -160,8 +166,9 @@ def alg_bytes(kind: str, nn: int, ne: int, nnz: int) -> float:
 # dram__bytes_read + dram__bytes_write per element of one launch.  k_elem is the
 # mean of its first-stage and last-stage (CFL) launches.
 NCU_PER_ELEM = {
-    "k_force": {"fp64_ops": 528.0, "dram_bytes": (104.547840e6 + 22.322176e6) / 262144},
-    "k_elem": {"fp64_ops": (603.0 + 811.0) / 2, "dram_bytes": (87.241472e6 + 26.444544e6 + 87.148800e6 + 26.663424e6) / 2 / 262144},
+    "k_force": {"fp64_ops": 138412032 / 262144, "dram_bytes": (104.519936e6 + 22.368256e6) / 262144},
+    "k_elem": {"fp64_ops": (158072832 + 171509792) / 2 / 262144,
+               "dram_bytes": (87.254784e6 + 25.970176e6 + 87.096064e6 + 26.185472e6) / 2 / 262144},
 }
 
 
@@ -409,8 +416,98 @@ def batch_bench(args):
     print(json.dumps(line))
 
 
+def adjoint_bench(args):
+    """Discrete adjoint of 400 RK2 cycles of jittered Sedov 64^3: cost of the
+    checkpointed forward and of the backward against the plain forward, and the
+    gradient against central differences of the GPU forward along seeded
+    directions (per-element relative sie perturbations U(-1,1) and a gamma shift
+    U(-1,1)), plus the CPU oracle's forward on a 12^3, 100-cycle deck."""
+    import numpy as np
+    import torch
+    from fierro_gb300 import adjoint, problems, sgh
+    torch.cuda.set_device(0)
+    n, cyc, k = args.adj_n, args.adj_cycles, args.adj_ckpt
+    target = adjoint.sedov_target(n, cyc, jitter=0.1, seed=7)
+    prob = problems.sedov(n, jitter=0.1, seed=7, cycles=cyc)
+    dm = adjoint.DensityMismatch(prob, target, cyc, ckpt_every=k)
+    s = dm.solver
+    J0, sb, gb, vb = dm.gradient()  # warm-up (allocates the tape)
+    s.adj_verify(True)
+    dm.gradient()
+    vstats = s.adj_stats()
+    s.adj_verify(False)
+    t_plain, t_fwd, t_bwd = [], [], []
+    for _ in range(max(args.steps, 1) if args.steps < 5 else 3):
+        s.set_state(dm.state0)
+        s.synchronize()
+        t0 = time.perf_counter()
+        s.run(cyc)
+        t_plain.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        dm.forward()
+        t_fwd.append(time.perf_counter() - t0)
+        seed = 2.0 * dm.mass * (dm.last_den - dm.target)
+        t0 = time.perf_counter()
+        sb2, gb2, _ = s.adj_backward(den=seed)
+        t_bwd.append(time.perf_counter() - t0)
+    tp, tf, tb = min(t_plain), min(t_fwd), min(t_bwd)
+    dirs = []
+    for d_sie, d_g in dm.directions(args.adj_dirs, seed=args.seed):
+        ad = float(np.dot(sb, d_sie) + np.sum(gb) * d_g)
+        fd6 = dm.fd(d_sie, d_g, h=1e-6)
+        est, h, spread, _ = dm.fd_consistent(d_sie, d_g)
+        dirs.append({"ad": ad, "fd_h1e-6": fd6, "rel_h1e-6": abs(fd6 - ad) / abs(fd6), "fd": est, "h": h,
+                     "fd_spread": spread, "rel": abs(est - ad) / abs(est)})
+    fd_check, orc_rel = None, None
+    if dirs:
+        rel = np.array([d["rel"] for d in dirs])
+        spread = np.array([d["fd_spread"] for d in dirs])
+        clean = spread <= 1e-6
+        fd_check = {"directions": len(dirs), "max_rel": float(rel.max()), "median_rel": float(np.median(rel)),
+                    "within_1e-6": int((rel <= 1e-6).sum()),
+                    "fd_self_consistent": int(clean.sum()),
+                    "max_rel_where_fd_self_consistent": float(rel[clean].max()) if clean.any() else None,
+                    "all_within_fd_spread": bool(np.all(rel <= np.maximum(spread, 1e-6))),
+                    "h1e-6_max_rel": float(max(d["rel_h1e-6"] for d in dirs)),
+                    "per_direction": dirs}
+        # the reference algorithm's forward on the CPU (oracle), smaller deck
+        dm12 = adjoint.DensityMismatch(problems.sedov(12, jitter=0.1, seed=7, cycles=100),
+                                       adjoint.sedov_target(12, 100, jitter=0.1, seed=7), 100, ckpt_every=13)
+        J12, sb12, gb12, _ = dm12.gradient()
+        orc_rel = []
+        try:
+            f = dm12.oracle_forward()
+            for d_sie, d_g in dm12.directions(3, seed=args.seed):
+                ad = float(np.dot(sb12, d_sie) + np.sum(gb12) * d_g)
+                fd = dm12.fd(d_sie, d_g, h=1e-6, forward=f)
+                orc_rel.append(abs(fd - ad) / abs(fd))
+        except Exception as exc:  # oracle not built on this machine
+            orc_rel = ["unavailable: %s" % str(exc).splitlines()[0]]
+    line = {"metric": "discrete adjoint cost: backward / plain forward (Sedov %d^3, %d RK2 cycles, FP64)" % (n, cyc),
+            "value": tb / tp, "unit": "x plain forward", "higher_is_better": False, "dtype": "f64",
+            "data": "synthetic", "forward_plus_backward_x": (tf + tb) / tp, "checkpointed_forward_x": tf / tp,
+            "plain_forward_s": tp, "adj_forward_s": tf, "backward_s": tb,
+            "J": J0, "replay_force_mismatches": vstats["force_mismatches"], "status": vstats["status"],
+            "dt_cycles": {"cfl": vstats["dt_cfl_cycles"], "growth": vstats["dt_growth_cycles"],
+                          "other": vstats["dt_other_cycles"]},
+            "adjoint_device_bytes": vstats["device_bytes"], "tape_bytes": vstats["tape_bytes"],
+            "checkpoint_bytes": vstats["ckpt_bytes"],
+            "fd_check": fd_check,
+            "oracle_fd_check_12cubed_100cycles": orc_rel,
+            "config": {"workload": "adjoint sedov%d jitter0.1 seed7" % n, "cycles": cyc, "ckpt_every": k,
+                       "objective": "sum_e M_e (rho_e - rho_target_e)^2, rho_target from origin energy 0.3",
+                       "params": "per-element initial sie and gamma", "fd": "central, steps 1e-5..1e-8; "
+                       "the reported step is the one agreeing best with the next smaller step",
+                       "timing": "host wall clock around fierro_sgh_run / fierro_adj_forward / "
+                       "fierro_adj_backward (each synchronises), best of 3"}}
+    print(json.dumps(line))
+
+
 def main(argv=None):
     args = parse(argv)
+    if args.adjoint:
+        adjoint_bench(args)
+        return
     if args.batch:
         batch_bench(args)
         return

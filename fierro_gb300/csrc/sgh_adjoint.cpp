@@ -35,6 +35,8 @@ struct AdjState {
   size_t slot_doubles = 0, ckpt_doubles = 0;
   double* tape = nullptr;    // (k*S + 1) slots
   double* forces = nullptr;  // k*S blocks of [24][ne]
+  double* ftape = nullptr;   // k*S blocks of [kForceTapeRows][ne]
+  int* fsel = nullptr;       // k*S blocks of [ne]
   double* ckpt = nullptr;    // nseg_cap checkpoints
   Ctrl* ckpt_ctrl = nullptr;
   long long* ckpt_cfl = nullptr;
@@ -136,7 +138,10 @@ int ensure(fierro_sgh* h, int k, int nseg) {
   };
   if ((rc = aalloc(a, &a->tape, nslot * a->slot_doubles))) return fail(rc);
   if ((rc = aalloc(a, &a->forces, (size_t)k * S * 24 * ne))) return fail(rc);
-  a->tape_bytes = sizeof(double) * (nslot * a->slot_doubles + (size_t)k * S * 24 * ne);
+  if ((rc = aalloc(a, &a->ftape, (size_t)k * S * kForceTapeRows * ne))) return fail(rc);
+  if ((rc = aalloc(a, &a->fsel, (size_t)k * S * ne))) return fail(rc);
+  a->tape_bytes = sizeof(double) * (nslot * a->slot_doubles + (size_t)k * S * (24 + kForceTapeRows) * ne) +
+                  sizeof(int) * (size_t)k * S * ne;
   if ((rc = aalloc(a, &a->ckpt, (size_t)nseg * a->ckpt_doubles))) return fail(rc);
   if ((rc = aalloc(a, &a->ckpt_ctrl, (size_t)nseg))) return fail(rc);
   if ((rc = aalloc(a, &a->ckpt_cfl, (size_t)nseg * h->ncfl))) return fail(rc);
@@ -256,7 +261,9 @@ int replay_segment(fierro_sgh* h, AdjState* a, int g, int n) {
       fa.ctrl = a->ctrl;
       fa.fuzz = h->lp.fuzz;
       fa.small = h->lp.small;
-      h->ks->force(fa, st);
+      fa.tape = a->ftape + (size_t)j * kForceTapeRows * ne;
+      fa.tape_sel = a->fsel + (size_t)j * ne;
+      h->ks->force_tape(fa, st);
       NodeArgs na{};
       na.nn = (int)nn;
       na.ne = (int)ne;
@@ -429,7 +436,8 @@ extern "C" int fierro_adj_backward(fierro_sgh* h, const fierro_adj_seed* seed, d
                b.part_e + (size_t)s * b.nbe, 0, st);
         K.node(a->m, b, sn, F, a->rec + i, al.a[s], last ? an_n : none, an_c, last ? 1 : 0,
                b.part_n + (size_t)s * b.nbn, st);
-        K.force(a->m, b, sj, sn, F, h->lp.fuzz, h->lp.small, s > 0 ? b.sbt : a->sb[p ^ 1], s == 0 ? 1 : 0, st);
+        K.force(a->m, b, sj, sn, F, a->ftape + (size_t)j * kForceTapeRows * ne, a->fsel + (size_t)j * ne,
+                h->lp.fuzz, h->lp.small, s > 0 ? b.sbt : a->sb[p ^ 1], s == 0 ? 1 : 0, st);
       }
       K.dt(a->m, b, a->rec + i, h->lp, slot_at(h, a, (long long)i * S), S, al, an_c, a->sb[p ^ 1], st);
       p ^= 1;

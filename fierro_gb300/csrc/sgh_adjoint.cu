@@ -428,16 +428,19 @@ __global__ void __launch_bounds__(kAdjNodeBlock) k_adj_node(const AdjMesh m, con
 
 // ---------------------------------------------------------------------------
 // Corner force in reverse (force_sgh.cpp:35-394, 3D, strength none), with the
-// EOS of its input state.  The forward part repeats the cycle kernel's
-// operations in its order; force_tape (the forces the cycle kernel wrote) is
-// compared bit for bit when b.mismatch is set.
+// EOS of its input state.  The viscosity intermediates come from the replay's
+// force tape (written by the cycle kernel itself, so they are the forward's
+// values); when b.mismatch is set the corner forces are rebuilt from them with
+// the cycle kernel's operations and compared bit for bit with force_tape.
 //   F_l = B_l p + phi mu_l (v* - v_l), mu_l = den (qa c + qb |v_l - v_avg|) |B_l|,
 //   v* = sum mu_l v_l / sum mu_l (if sum mu_l > fuzz), phi = alpha phi0,
 //   phi0 = 1 - max(0, min(1, r_face)), r_face = 0.9 (div_nb + small)/(div + small),
 //   alpha = min(1, 20 vol^(1/3) |div| / (c + fuzz)).
-__global__ void __launch_bounds__(kAdjForceBlock) k_adj_force(const AdjMesh m, const AdjBufs b, const Slot s0,
+__global__ void __launch_bounds__(kAdjForceBlock, 3) k_adj_force(const AdjMesh m, const AdjBufs b, const Slot s0,
                                                                const Slot s1, const double* __restrict__ force_tape,
-                                                               double fuzz, double small, double* __restrict__ sie_out,
+                                                               const double* __restrict__ ft,
+                                                               const int* __restrict__ fsel, double fuzz,
+                                                               double small, double* __restrict__ sie_out,
                                                                int accumulate) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= m.ne) return;
@@ -456,8 +459,6 @@ __global__ void __launch_bounds__(kAdjForceBlock) k_adj_force(const AdjMesh m, c
   const bool compress = div < 0;
   const double qa = compress ? q[0] : q[1];
   const double qb = compress ? q[2] : q[3];
-
-  // forward, as the cycle kernel evaluates it
   double vs0 = 0.0, vs1 = 0.0, vs2 = 0.0;
 #pragma unroll
   for (int l = 0; l < 8; ++l) {
@@ -465,67 +466,20 @@ __global__ void __launch_bounds__(kAdjForceBlock) k_adj_force(const AdjMesh m, c
     vs1 = fma(0.125, vv[l], vs1);
     vs2 = fma(0.125, vw[l], vs2);
   }
+  const double* t = ft + e;
   double mu[8], mv[8];
-  double s0_ = 0.0, s1_ = 0.0, s2_ = 0.0, s3 = 0.0;
-  const double q1c = qa * sspd;
 #pragma unroll
   for (int l = 0; l < 8; ++l) {
-    const double d0 = vu[l] - vs0, d1 = vv[l] - vs1, d2 = vw[l] - vs2;
-    mv[l] = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
-    const double muc = den * (q1c + qb * mv[l]);
-    const double b0 = s0.bmat[(size_t)(l * 3 + 0) * ne + e];
-    const double b1 = s0.bmat[(size_t)(l * 3 + 1) * ne + e];
-    const double b2 = s0.bmat[(size_t)(l * 3 + 2) * ne + e];
-    const double mu_term = muc * sqrt(b0 * b0 + b1 * b1 + b2 * b2);
-    s0_ = s0_ + mu_term * vu[l];
-    s1_ = s1_ + mu_term * vv[l];
-    s2_ = s2_ + mu_term * vw[l];
-    s3 = s3 + mu_term;
-    mu[l] = mu_term;
+    mu[l] = t[(size_t)l * ne];
+    mv[l] = t[(size_t)(8 + l) * ne];
   }
-  double vstar0 = 0.0, vstar1 = 0.0, vstar2 = 0.0;
+  const double vstar0 = t[(size_t)16 * ne], vstar1 = t[(size_t)17 * ne], vstar2 = t[(size_t)18 * ne];
+  const double s3 = t[(size_t)19 * ne], phi0 = t[(size_t)20 * ne], araw = t[(size_t)21 * ne];
+  const double c_length = t[(size_t)22 * ne], r_min = t[(size_t)23 * ne];
+  const int sel = fsel[e];
   const bool use_vstar = s3 > fuzz;
-  if (use_vstar) {
-    vstar0 = s0_ / s3;
-    vstar1 = s1_ / s3;
-    vstar2 = s2_ / s3;
-  }
+  const double q1c = qa * sspd;
   const double D = div + small;
-  const int k0 = m.eie_start[e], k1 = m.eie_start[e + 1];
-  long long kmin = kMaxKey, kmax = (long long)0x8000000000000000ULL;
-  for (int k = k0; k < k1; ++k) {
-    const long long key = okey(s0.div[__ldg(m.eie + k)]);
-    kmin = key < kmin ? key : kmin;
-    kmax = key > kmax ? key : kmax;
-  }
-  double r_min = 1.0;
-  int sel = -1;  // neighbour whose divergence sets phi0 (limiter active)
-  if (k1 > k0) {
-    const long long ksel = D > 0 ? kmin : kmax;
-    const double dsel = okey_decode(ksel);
-    const bool regular = isfinite(D) && D != 0.0 && isfinite(dsel);
-    if (regular) {
-      const double r_face = 0.9 * (dsel + small) / D;
-      r_min = okey(r_face) < okey(1.0) ? r_face : 1.0;
-      if (okey(r_face) < okey(1.0) && r_face > 0.0) {
-        for (int k = k0; k < k1; ++k) {
-          const int nb = __ldg(m.eie + k);
-          if (okey(s0.div[nb]) == ksel) {
-            sel = nb;
-            break;
-          }
-        }
-      }
-    } else {
-      for (int k = k0; k < k1; ++k) {
-        const double r_face = 0.9 * (s0.div[__ldg(m.eie + k)] + small) / D;
-        r_min = fmin(r_face, r_min);
-      }
-    }
-  }
-  const double phi0 = 1.0 - fmax(0.0, r_min);
-  const double c_length = pow_third(vol);
-  const double araw = 20.0 * (c_length * fabs(div)) / (sspd + fuzz);
   const double alpha = fmin(1.0, araw);
   const double phi = alpha * phi0;
   if (b.mismatch) {
@@ -795,10 +749,10 @@ static void launch_node(const AdjMesh& m, const AdjBufs& b, const Slot& s1, cons
                                                                          assign, part);
 }
 static void launch_force(const AdjMesh& m, const AdjBufs& b, const Slot& s0, const Slot& s1,
-                         const double* force_tape, double fuzz, double small, double* sie_out, int accumulate,
-                         cudaStream_t st) {
-  k_adj_force<<<blocks_for(m.ne, kAdjForceBlock), kAdjForceBlock, 0, st>>>(m, b, s0, s1, force_tape, fuzz, small,
-                                                                            sie_out, accumulate);
+                         const double* force_tape, const double* ft, const int* fsel, double fuzz, double small,
+                         double* sie_out, int accumulate, cudaStream_t st) {
+  k_adj_force<<<blocks_for(m.ne, kAdjForceBlock), kAdjForceBlock, 0, st>>>(m, b, s0, s1, force_tape, ft, fsel, fuzz,
+                                                                            small, sie_out, accumulate);
 }
 static void launch_dt(const AdjMesh& m, const AdjBufs& b, const AdjRecord* r, const LoopParams& lp,
                       const Slot& s0, int stages, const AdjAlphas& al, const Node6& an_c, double* sie_c,

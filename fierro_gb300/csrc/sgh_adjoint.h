@@ -4,7 +4,9 @@
 //   Slot j = 0 .. k*S    the state at stage boundary j (slot 0 = checkpoint), one
 //                        contiguous block: node x,y,z,u,v,w,hx,hy,hz [9][nn], then
 //                        element sie,vol,den,pres,sspd,div [6][ne], bmat [24][ne]
-//   force j = 0 .. k*S-1 corner forces of stage j [24][ne]
+//   force j = 0 .. k*S-1 corner forces of stage j [24][ne], and the force kernel's
+//                        viscosity intermediates [kForceTapeRows][ne] + limiter
+//                        neighbour [ne] (the reverse force pass reads them)
 //   AdjRecord per cycle  the dt computation's inputs and result
 // Checkpoint g: node x..w [6][nn], element sie..div + bmat [30][ne], Ctrl and the
 // CFL block minima, i.e. exactly slot 0 of segment g plus the loop scalars.
@@ -106,8 +108,10 @@ struct AdjLaunch {
                cudaStream_t);
   void (*node)(const AdjMesh& m, const AdjBufs& b, const Slot& s1, const double* force, const AdjRecord* r,
                double alpha, const Node6& an_in, const Node6& an_c, int assign, double* part, cudaStream_t);
+  // ft / fsel: the replay's force tape of this stage (kForceTapeRows x ne, ne)
   void (*force)(const AdjMesh& m, const AdjBufs& b, const Slot& s0, const Slot& s1, const double* force_tape,
-                double fuzz, double small, double* sie_out, int accumulate, cudaStream_t);
+                const double* ft, const int* fsel, double fuzz, double small, double* sie_out, int accumulate,
+                cudaStream_t);
   void (*dt)(const AdjMesh& m, const AdjBufs& b, const AdjRecord* r, const LoopParams& lp, const Slot& s0,
              int stages, const AdjAlphas& al, const Node6& an_c, double* sie_c, cudaStream_t);
   // velocity adjoint of the uploaded state into b.fbar[0..2]

@@ -59,7 +59,15 @@ struct ForceArgs {
   const Ctrl* ctrl;   // plain: the solver's control block; batch: one per instance
   const int* inst;    // batch only: instance of each element (negative = padding)
   double fuzz, small;
+  // adjoint replay only (force_tape launcher): the viscosity intermediates of
+  // each element, rows of kForceTapeRows x ne, and the limiter's neighbour
+  double* tape;
+  int* tape_sel;
 };
+
+// Rows of the force kernel's tape: mu[8], |v_l - v_avg|[8], v*[3], sum mu,
+// phi0 (limiter), the Mach-switch argument, vol^(1/3), the limiter's r_min.
+constexpr int kForceTapeRows = 24;
 
 struct NodeArgs {
   int nn, ne;
@@ -121,6 +129,7 @@ struct EnergyArgs {
 // One arithmetic mode's launchers (defined in sgh_kernels.cu, compiled once per mode).
 struct KernelSet {
   void (*force)(const ForceArgs&, cudaStream_t);
+  void (*force_tape)(const ForceArgs&, cudaStream_t);  // the same, also writing a.tape / a.tape_sel
   void (*node)(const NodeArgs&, cudaStream_t);
   void (*elem)(const ElemArgs&, int kind, cudaStream_t);
   void (*dt)(const DtArgs&, cudaStream_t);

@@ -56,7 +56,9 @@ namespace FIERRO_IMPL {
 // (use_shock_dir = 0 at :227, phi_curl unused at :331) and are not computed.
 // Stress is zero for strength-free materials, so tau = -p I and the force's
 // stress term a_k tau(k,d) reduces exactly to B(d) p (two negations).
-template <bool BATCH>
+// TAPE (the adjoint's replay, exact mode) also stores the viscosity
+// intermediates; the stores do not change any value the kernel computes.
+template <bool BATCH, bool TAPE>
 __global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
   if (!BATCH && !a.ctrl->active) return;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -151,7 +153,38 @@ __global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
   double phi = 1.0 - fmax(0.0, r_min);  // pow(phi, 1.0) == phi
   // Mach-number detector (:318-328)
   const double c_length = pow_third(vol);
-  const double alpha = fmin(1.0, 20.0 * (c_length * fabs(div)) / (sspd + a.fuzz));
+  const double araw = 20.0 * (c_length * fabs(div)) / (sspd + a.fuzz);
+  const double alpha = fmin(1.0, araw);
+  if (TAPE) {
+    double* t = a.tape + e;
+#pragma unroll
+    for (int l = 0; l < 8; ++l) {
+      const double d0 = vu[l] - vs0, d1 = vv[l] - vs1, d2 = vw[l] - vs2;
+      t[(size_t)l * ne] = mu[l];
+      t[(size_t)(8 + l) * ne] = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    }
+    t[(size_t)16 * ne] = vstar0;
+    t[(size_t)17 * ne] = vstar1;
+    t[(size_t)18 * ne] = vstar2;
+    t[(size_t)19 * ne] = s3;
+    t[(size_t)20 * ne] = phi;
+    t[(size_t)21 * ne] = araw;
+    t[(size_t)22 * ne] = c_length;
+    t[(size_t)23 * ne] = r_min;
+    // the neighbour whose divergence set phi0 when the limiter is active
+    int sel = -1;
+    const long long ksel = D > 0 ? kmin : kmax;
+    if (k1 > k0 && isfinite(D) && D != 0.0 && isfinite(okey_decode(ksel)) && r_min < 1.0 && r_min > 0.0) {
+      for (int k = k0; k < k1; ++k) {
+        const int nb = __ldg(a.eie + k);
+        if (okey(__ldg(a.div + nb)) == ksel) {
+          sel = nb;
+          break;
+        }
+      }
+    }
+    a.tape_sel[e] = sel;
+  }
   phi = alpha * phi;
   // corner forces (:338-359)
 #pragma unroll
@@ -421,8 +454,11 @@ __global__ void k_energy_final(const EnergyArgs a, int nblocks) {
 static unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 static void launch_force(const ForceArgs& a, cudaStream_t s) {
-  if (a.inst) k_force<true><<<blocks_for(a.ne, kForceBlock), kForceBlock, 0, s>>>(a);
-  else k_force<false><<<blocks_for(a.ne, kForceBlock), kForceBlock, 0, s>>>(a);
+  if (a.inst) k_force<true, false><<<blocks_for(a.ne, kForceBlock), kForceBlock, 0, s>>>(a);
+  else k_force<false, false><<<blocks_for(a.ne, kForceBlock), kForceBlock, 0, s>>>(a);
+}
+static void launch_force_tape(const ForceArgs& a, cudaStream_t s) {
+  k_force<false, true><<<blocks_for(a.ne, kForceBlock), kForceBlock, 0, s>>>(a);
 }
 static void launch_node(const NodeArgs& a, cudaStream_t s) {
   if (a.inst) k_node<true><<<blocks_for(a.nn, kNodeBlock), kNodeBlock, 0, s>>>(a);
@@ -457,14 +493,14 @@ static void launch_energy(const EnergyArgs& a, cudaStream_t s) {
 
 #if FIERRO_FMA
 const KernelSet& kernels_fma() {
-  static const KernelSet k = {fma_impl::launch_force, fma_impl::launch_node, fma_impl::launch_elem,
+  static const KernelSet k = {fma_impl::launch_force, fma_impl::launch_force_tape, fma_impl::launch_node, fma_impl::launch_elem,
                               fma_impl::launch_dt, fma_impl::launch_end, fma_impl::launch_energy,
                               fma_impl::launch_end_batch, "fma"};
   return k;
 }
 #else
 const KernelSet& kernels_exact() {
-  static const KernelSet k = {exact_impl::launch_force, exact_impl::launch_node, exact_impl::launch_elem,
+  static const KernelSet k = {exact_impl::launch_force, exact_impl::launch_force_tape, exact_impl::launch_node, exact_impl::launch_elem,
                               exact_impl::launch_dt, exact_impl::launch_end, exact_impl::launch_energy,
                               exact_impl::launch_end_batch, "exact"};
   return k;
