@@ -279,25 +279,43 @@ def ours(args):
     # same K cycles, download the state (copies inside the timed region)
     e2e = None
     if not args.no_e2e:
-        host = sgh.empty_state(nn, ne, prob.num_state_vars)
+        # the output arrays exist and are resident, as the state arrays a caller
+        # of sgh_solve passes in (and gets back, in place) are
+        host = {k: v.copy() for k, v in st.items()}
         h2d = sum(st[k].nbytes for k in ("node_coords", "node_vel", "node_mass", "elem_den", "elem_pres",
                                          "elem_sspd", "elem_sie", "elem_vol", "elem_mass", "elem_mat_id",
                                          "elem_statev", "elem_div", "elem_stress"))
         d2h = sum(host[k].nbytes for k in host if k != "elem_statev" and k != "elem_mat_id")
-        torch.cuda.synchronize()
-        barrier(dist)
-        te0 = time.perf_counter()
+        # one untimed solve first (the first GPU access to a host page costs a
+        # translation-table walk), then three timed K-cycle solves; the median
+        # is reported (the host and its memory are shared with other jobs)
         solver.set_state(st)
-        solver.run(args.steps)
+        solver.run(1)
         solver.get_state(host)
-        te1 = time.perf_counter()
-        barrier(dist)
-        e_max = reduce_max(dist, te1 - te0)
-        e2e = {"value": ne * args.steps * world / e_max, "unit": UNIT,
+        trials = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            barrier(dist)
+            te0 = time.perf_counter()
+            solver.set_state(st)
+            tu = time.perf_counter()
+            solver.run(args.steps)
+            tr = time.perf_counter()
+            solver.get_state(host)
+            te1 = time.perf_counter()
+            barrier(dist)
+            trials.append((reduce_max(dist, te1 - te0), tu - te0, tr - tu, te1 - tr))
+        trials.sort()
+        med = trials[1]
+        e2e = {"value": ne * args.steps * world / med[0], "unit": UNIT,
                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+               "upload_s": med[1], "run_s": med[2], "download_s": med[3],
+               "trials_s": [[round(x, 4) for x in t] for t in trials],
                "path": "fierro_sgh_set_state + fierro_sgh_run(K) + fierro_sgh_get_state, host buffers in "
-                       "the reference layouts (AoS, caller numbering), one upload and one download per "
-                       "K-cycle solve; bytes per step = per solve / K"}
+                       "the reference layouts (AoS, caller numbering, resident pages), one upload and one "
+                       "download per K-cycle solve, the GPU reading and writing the host arrays over "
+                       "NVLink-C2C; one untimed warm-up solve, median of three timed solves (trials_s: "
+                       "total, upload, run, download); bytes per step = per solve / K"}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -3,8 +3,11 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
+
+#include <unistd.h>
 
 #include <cuda_runtime.h>
 
@@ -288,6 +291,13 @@ static int create_impl(fierro_sgh* h, const fierro_mesh* mesh, const fierro_mate
   h->ncfl = (int)((ne + kElemBlock - 1) / kElemBlock);
   TRY(dalloc(h, &h->d_cfl, (size_t)h->ncfl));
   TRY(dalloc(h, &h->d_ctrl, 1));
+  TRY(dalloc(h, &h->d_node_ext2int, nn));
+  TRY(dalloc(h, &h->d_elem_ext2int, ne));
+  TRY(dalloc(h, &h->d_xfer, 1));
+  {
+    const char* env = std::getenv("FIERRO_STAGED_TRANSFERS");
+    h->direct_host = xfer::direct_host_access() && !(env && env[0] == '1');
+  }
   TRY(dalloc(h, &h->d_energy_part, 2 * 512));
   TRY(dalloc(h, &h->d_energy_out, 2));
   h->stage_elems = std::max(nn, ne);
@@ -302,6 +312,13 @@ static int create_impl(fierro_sgh* h, const fierro_mesh* mesh, const fierro_mate
   TRY(upload_raw(h, h->d_eie_start, t.eie_start.data(), sizeof(int32_t) * (ne + 1)));
   if (!t.eie.empty()) TRY(upload_raw(h, h->d_eie, t.eie.data(), sizeof(int32_t) * t.eie.size()));
   TRY(upload_raw(h, h->d_bc, t.bc_mask.data(), nn));
+  {
+    std::vector<int32_t> m32(std::max(nn, ne));
+    for (size_t j = 0; j < nn; ++j) m32[j] = (int32_t)t.node_ext2int[j];
+    TRY(upload_raw(h, h->d_node_ext2int, m32.data(), sizeof(int32_t) * nn));
+    for (size_t j = 0; j < ne; ++j) m32[j] = (int32_t)t.elem_ext2int[j];
+    TRY(upload_raw(h, h->d_elem_ext2int, m32.data(), sizeof(int32_t) * ne));
+  }
   std::vector<double> q((size_t)num_materials * 4);
   for (int64_t m = 0; m < num_materials; ++m) {
     q[m * 4 + 0] = materials[m].q1;
@@ -336,6 +353,25 @@ extern "C" int fierro_sgh_create(const fierro_mesh* mesh, const fierro_material*
   return FIERRO_OK;
 }
 
+// Loop scalars, bin bookkeeping and the priming element pass of a freshly
+// uploaded state.
+static int finish_set_state(fierro_sgh* h, double time_value, double graphics_time, double dt) {
+  Ctrl c{};
+  c.dt = dt;
+  c.time_value = time_value;
+  c.graphics_time = graphics_time;
+  TRY(upload_raw(h, h->d_ctrl, &c, sizeof(Ctrl)));
+  h->base = 0;
+  h->enq_cycles = 0;
+  h->stage = 0;
+  // prime: corner normals, divergence and CFL partials of the uploaded state
+  h->ks->elem(elem_args(h, 0, 0, 1.0, 0), 2, h->stream);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  h->has_state = true;
+  return FIERRO_OK;
+}
+
 static int set_state_impl(fierro_sgh* h, const fierro_sgh_state* s, double time_value, double graphics_time,
                           double dt) {
   if (!s || !s->node_coords || !s->node_vel || !s->node_mass || !s->elem_den || !s->elem_pres || !s->elem_sspd ||
@@ -344,6 +380,26 @@ static int set_state_impl(fierro_sgh* h, const fierro_sgh_state* s, double time_
   if (s->num_state_vars < 2) return set_error(FIERRO_EINVAL, "set_state: need num_state_vars >= 2");
   const int64_t nn = h->nn, ne = h->ne, nsv = s->num_state_vars;
   const HostTopo& t = h->topo;
+  if (h->direct_host) {
+    // the GPU reads the caller's arrays and validates them in the same pass
+    h->has_state = false;
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    XferStatus xs{};
+    TRY(xfer::upload_state(h, s, &xs));
+    if (xs.flags & (1u << XferStatus::STRESS))
+      return set_error(FIERRO_ENOTSUP, "set_state: non-zero stress (value %lld) needs a strength model (outside "
+                       "this path)", xs.first[XferStatus::STRESS]);
+    if (xs.flags & (1u << XferStatus::MAT_ID))
+      return set_error(FIERRO_EINVAL, "set_state: element %lld material id out of range", xs.first[XferStatus::MAT_ID]);
+    if (xs.flags & (1u << XferStatus::VOLUME))
+      return set_error(FIERRO_ENUMERIC, "set_state: element %lld has a non-positive or non-finite volume",
+                       xs.first[XferStatus::VOLUME]);
+    if (xs.flags & (1u << XferStatus::MASS))
+      return set_error(FIERRO_EINVAL, "set_state: element %lld mass <= 0", xs.first[XferStatus::MASS]);
+    if (xs.flags & (1u << XferStatus::NODE_MASS))
+      return set_error(FIERRO_EINVAL, "set_state: node %lld mass <= 0", xs.first[XferStatus::NODE_MASS]);
+    return finish_set_state(h, time_value, graphics_time, dt);
+  }
   if (s->elem_stress)
     for (int64_t i = 0; i < ne * 18; ++i)
       if (s->elem_stress[i] != 0.0)
@@ -382,26 +438,24 @@ static int set_state_impl(fierro_sgh* h, const fierro_sgh_state* s, double time_
   // the caller's elem_div is what the reference shows before any stage runs
   if (s->elem_div) TRY(upload_gather(h, h->d_div[1], s->elem_div, t.elem_int2ext, 1, 0, &slot));
   else CUDA_TRY(cudaMemsetAsync(h->d_div[1], 0, sizeof(double) * (size_t)ne, h->stream));
-  Ctrl c{};
-  c.dt = dt;
-  c.time_value = time_value;
-  c.graphics_time = graphics_time;
-  TRY(upload_raw(h, h->d_ctrl, &c, sizeof(Ctrl)));
-  h->base = 0;
-  h->enq_cycles = 0;
-  h->stage = 0;
-  // prime: corner normals, divergence and CFL partials of the uploaded state
-  h->ks->elem(elem_args(h, 0, 0, 1.0, 0), 2, h->stream);
-  CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaStreamSynchronize(h->stream));
-  h->has_state = true;
-  return FIERRO_OK;
+  return finish_set_state(h, time_value, graphics_time, dt);
 }
 
 extern "C" int fierro_sgh_set_state(fierro_sgh* h, const fierro_sgh_state* s) {
   clear_error();
   if (!h) return set_error(FIERRO_EINVAL, "handle is NULL");
   return set_state_impl(h, s, 0.0, h->lp.graphics_dt_ival, h->dt_start);
+}
+
+// One store per page, in parallel, so that the pages of an output array exist
+// before the GPU writes it (the array is overwritten completely afterwards).
+static void populate(double* p, size_t bytes) {
+  if (!p || bytes == 0) return;
+  static const size_t page = (size_t)std::max(4096L, sysconf(_SC_PAGESIZE));
+  char* c = reinterpret_cast<char*>(p);
+  const int64_t n = (int64_t)((bytes + page - 1) / page);
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < n; ++k) *(volatile char*)(c + (size_t)k * page) = 0;
 }
 
 extern "C" int fierro_sgh_get_state(fierro_sgh* h, fierro_sgh_state* s) {
@@ -417,6 +471,23 @@ extern "C" int fierro_sgh_get_state(fierro_sgh* h, fierro_sgh_state* s) {
   const int64_t nn = h->nn, ne = h->ne;
   const HostTopo& t = h->topo;
   const int bins[2] = {b0, b1};
+  // the divergence the last executed stage used (reference elem_div)
+  const long long stages_done = cyc * h->rk_num_stages + h->stage;
+  const int qb = stages_done == 0 ? 1 : (int)((stages_done - 1) & 1);
+  if (h->direct_host) {
+    // the kernels write the caller's arrays: make their pages resident first
+    // (a GPU fault per untouched page costs far more than a host store per page)
+    const size_t nb = sizeof(double);
+    populate(s->node_coords, nb * nn * 6);
+    populate(s->node_vel, nb * nn * 6);
+    populate(s->node_mass, nb * nn);
+    populate(s->elem_sie, nb * ne * 2);
+    double* e1[] = {s->elem_den, s->elem_pres, s->elem_sspd, s->elem_vol, s->elem_div, s->elem_mass};
+    for (double* p : e1) populate(p, nb * ne);
+    populate(s->elem_stress, nb * ne * 18);
+    populate(s->corner_force, nb * ne * 24);
+    return xfer::download_state(h, s, bins, qb);
+  }
   for (int rb = 0; rb < 2; ++rb)
     for (int d = 0; d < 3; ++d) {
       if (s->node_coords)
@@ -432,12 +503,7 @@ extern "C" int fierro_sgh_get_state(fierro_sgh* h, fierro_sgh_state* s) {
   if (s->elem_pres) TRY(download_scatter(h, s->elem_pres, h->d_pres, t.elem_int2ext, 1, 0));
   if (s->elem_sspd) TRY(download_scatter(h, s->elem_sspd, h->d_sspd, t.elem_int2ext, 1, 0));
   if (s->elem_vol) TRY(download_scatter(h, s->elem_vol, h->d_vol, t.elem_int2ext, 1, 0));
-  if (s->elem_div) {
-    // the divergence the last executed stage used (reference elem_div)
-    const long long stages_done = cyc * h->rk_num_stages + h->stage;
-    const int qb = stages_done == 0 ? 1 : (int)((stages_done - 1) & 1);
-    TRY(download_scatter(h, s->elem_div, h->d_div[qb], t.elem_int2ext, 1, 0));
-  }
+  if (s->elem_div) TRY(download_scatter(h, s->elem_div, h->d_div[qb], t.elem_int2ext, 1, 0));
   if (s->elem_mass) TRY(download_scatter(h, s->elem_mass, h->d_elem_mass, t.elem_int2ext, 1, 0));
   if (s->elem_stress) std::memset(s->elem_stress, 0, sizeof(double) * (size_t)ne * 18);
   if (s->corner_force) {

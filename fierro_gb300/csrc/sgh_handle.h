@@ -12,6 +12,7 @@
 #include "fierro_sgh.h"
 #include "sgh_device.h"
 #include "sgh_internal.h"
+#include "sgh_xfer.h"
 
 #define CUDA_TRY(expr)                                                                            \
   do {                                                                                            \
@@ -73,6 +74,11 @@ struct fierro_sgh {
   bool has_state = false;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   fierro::AdjState* adj = nullptr;  // discrete-adjoint tape and checkpoints (sgh_adjoint.cpp)
+  // direct transfers (sgh_xfer.cu): caller -> internal maps and the validation word
+  bool direct_host = false;
+  int* d_node_ext2int = nullptr;
+  int* d_elem_ext2int = nullptr;
+  fierro::XferStatus* d_xfer = nullptr;
 };
 
 namespace fierro {

@@ -1,0 +1,39 @@
+// Direct host<->device state transfer (sgh_xfer.cu): the GPU reads and writes the
+// caller's host arrays itself where the device can dereference pageable host
+// memory (GB300: address translation over NVLink-C2C).
+#ifndef FIERRO_SGH_XFER_H
+#define FIERRO_SGH_XFER_H
+
+#include "fierro_sgh.h"
+
+struct fierro_sgh;
+
+namespace fierro {
+
+// Validation result of an upload: bit k of `flags` set when check k failed,
+// first[k] = the smallest caller index (element, node or stress value) that
+// failed it.
+struct XferStatus {
+  enum { STRESS = 0, MAT_ID = 1, VOLUME = 2, MASS = 3, NODE_MASS = 4, COUNT = 5 };
+  unsigned int flags;
+  int pad;
+  long long first[COUNT];
+};
+
+namespace xfer {
+
+// True when kernels may dereference pageable host pointers on the current device.
+bool direct_host_access();
+// Uploads a state (reference layouts) into the handle's bins and reports the
+// validation result; the state on the device is the caller's even when a check
+// failed (the caller then discards it).
+int upload_state(fierro_sgh* h, const fierro_sgh_state* s, XferStatus* status);
+// Writes the handle's state into the non-null fields of `s`: reference bin rb
+// from device bin bins[rb]; elem_div from divergence buffer div_buffer; stress
+// as zeros.
+int download_state(fierro_sgh* h, fierro_sgh_state* s, const int bins[2], int div_buffer);
+
+}  // namespace xfer
+}  // namespace fierro
+
+#endif

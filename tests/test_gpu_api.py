@@ -133,3 +133,32 @@ def test_device_detects_inverted_element_and_recovers(lib_built):
         assert s.run(2) == 2
         out = s.get_state()
         assert np.all(out["elem_vol"] > 0)
+
+
+def test_direct_and_staged_transfers_agree(lib_built, monkeypatch):
+    """The GPU-side transfer (kernels reading and writing the caller's host
+    arrays) and the staged transfer (host permutation through pinned buffers)
+    give the same device state, the same results and the same validation
+    errors."""
+    from fierro_gb300 import sgh
+    prob = _prob()
+    st = sgh.setup(prob)
+    outs = []
+    for staged in ("0", "1"):
+        monkeypatch.setenv("FIERRO_STAGED_TRANSFERS", staged)
+        with sgh.SGHSolver(prob) as s:
+            s.set_state(st)
+            s.run(6)
+            outs.append(s.get_state())
+            bad = {k: v.copy() for k, v in st.items()}
+            bad["elem_vol"][5] = float("nan")
+            with pytest.raises(sgh.FierroError) as ei:
+                s.set_state(bad)
+            assert ei.value.code == sgh.FIERRO_ENUMERIC and "element 5" in str(ei.value)
+            bad = {k: v.copy() for k, v in st.items()}
+            bad["node_mass"][9] = 0.0
+            with pytest.raises(sgh.FierroError) as ei:
+                s.set_state(bad)
+            assert ei.value.code == sgh.FIERRO_EINVAL and "node 9" in str(ei.value)
+    for k in outs[0]:
+        assert np.array_equal(outs[0][k], outs[1][k]), k
