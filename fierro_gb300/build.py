@@ -8,6 +8,7 @@ Translation units:
   csrc/sgh_capi.cpp    the C ABI (g++)
   csrc/sgh_batch.cpp   the batched-ensemble C ABI (g++)
   csrc/sgh_xfer.cu     host<->device state transfer kernels (GPU reads/writes host arrays)
+  csrc/sgh_topo.cu     mesh topology on the GPU (renumbering, CSRs, boundary masks; --fmad=false)
   csrc/sgh_adjoint.cu  discrete-adjoint kernels (--fmad=false, like the exact mode)
   csrc/sgh_adjoint.cpp the adjoint's checkpointing, replay and reverse schedule (g++)
   csrc/sgh_calib.cu    FP64 throughput calibration for the roofline
@@ -64,6 +65,8 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     ]
     calib = os.path.join(CSRC, "sgh_calib.cu")
     units.append((os.path.join(OBJ, "sgh_calib.o"), nvcc_common + ["-c", calib], [calib]))
+    topo = os.path.join(CSRC, "sgh_topo.cu")
+    units.append((os.path.join(OBJ, "sgh_topo.o"), nvcc_common + ["--fmad=false", "-c", topo], [topo]))
     xfer = os.path.join(CSRC, "sgh_xfer.cu")
     units.append((os.path.join(OBJ, "sgh_xfer.o"), nvcc_common + ["-c", xfer], [xfer]))
     adjk = os.path.join(CSRC, "sgh_adjoint.cu")

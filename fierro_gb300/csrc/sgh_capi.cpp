@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include "sgh_handle.h"
+#include "sgh_topo.h"
 
 using namespace fierro;
 
@@ -242,7 +243,15 @@ static int create_impl(fierro_sgh* h, const fierro_mesh* mesh, const fierro_mate
   }
   int dev = 0;
   CUDA_TRY(cudaGetDevice(&dev));
-  TRY(build_topology(mesh, boundaries, num_bcs, true, &h->topo));
+  TRY(check_mesh_header(mesh));
+  TRY(validate_bcs(boundaries, num_bcs));
+  {
+    const char* env = std::getenv("FIERRO_STAGED_TRANSFERS");
+    h->direct_host = xfer::direct_host_access() && !(env && env[0] == '1');
+  }
+  // with direct host access the GPU builds the topology from the caller's arrays
+  // (sgh_topo.cu); otherwise the host builder does
+  if (!h->direct_host) TRY(build_topology(mesh, boundaries, num_bcs, true, &h->topo));
   h->nn = mesh->num_nodes;
   h->ne = mesh->num_elems;
   h->nmat = (int)num_materials;
@@ -264,7 +273,7 @@ static int create_impl(fierro_sgh* h, const fierro_mesh* mesh, const fierro_mate
   TRY(dalloc(h, &h->d_cin_start, nn + 1));
   TRY(dalloc(h, &h->d_cin, ne * 8));
   TRY(dalloc(h, &h->d_eie_start, ne + 1));
-  TRY(dalloc(h, &h->d_eie, t.eie.size()));
+  if (!h->direct_host) TRY(dalloc(h, &h->d_eie, t.eie.size()));
   TRY(dalloc(h, &h->d_mat, ne));
   TRY(dalloc(h, &h->d_bc, nn));
   TRY(dalloc(h, &h->d_qtab, (size_t)num_materials * 4));
@@ -294,10 +303,6 @@ static int create_impl(fierro_sgh* h, const fierro_mesh* mesh, const fierro_mate
   TRY(dalloc(h, &h->d_node_ext2int, nn));
   TRY(dalloc(h, &h->d_elem_ext2int, ne));
   TRY(dalloc(h, &h->d_xfer, 1));
-  {
-    const char* env = std::getenv("FIERRO_STAGED_TRANSFERS");
-    h->direct_host = xfer::direct_host_access() && !(env && env[0] == '1');
-  }
   TRY(dalloc(h, &h->d_energy_part, 2 * 512));
   TRY(dalloc(h, &h->d_energy_out, 2));
   h->stage_elems = std::max(nn, ne);
@@ -306,13 +311,16 @@ static int create_impl(fierro_sgh* h, const fierro_mesh* mesh, const fierro_mate
     CUDA_TRY(cudaEventCreateWithFlags(&h->stage_ev[i], cudaEventDisableTiming));
     CUDA_TRY(cudaEventRecord(h->stage_ev[i], h->stream));
   }
-  TRY(upload_raw(h, h->d_nie, t.nie.data(), sizeof(int32_t) * ne * 8));
-  TRY(upload_raw(h, h->d_cin_start, t.cin_start.data(), sizeof(int32_t) * (nn + 1)));
-  TRY(upload_raw(h, h->d_cin, t.cin.data(), sizeof(int32_t) * ne * 8));
-  TRY(upload_raw(h, h->d_eie_start, t.eie_start.data(), sizeof(int32_t) * (ne + 1)));
-  if (!t.eie.empty()) TRY(upload_raw(h, h->d_eie, t.eie.data(), sizeof(int32_t) * t.eie.size()));
-  TRY(upload_raw(h, h->d_bc, t.bc_mask.data(), nn));
-  {
+  if (h->direct_host) {
+    TRY(topo::build_device(h, mesh, boundaries, num_bcs));
+  } else {
+    TRY(upload_raw(h, h->d_nie, t.nie.data(), sizeof(int32_t) * ne * 8));
+    TRY(upload_raw(h, h->d_cin_start, t.cin_start.data(), sizeof(int32_t) * (nn + 1)));
+    TRY(upload_raw(h, h->d_cin, t.cin.data(), sizeof(int32_t) * ne * 8));
+    TRY(upload_raw(h, h->d_eie_start, t.eie_start.data(), sizeof(int32_t) * (ne + 1)));
+    if (!t.eie.empty()) TRY(upload_raw(h, h->d_eie, t.eie.data(), sizeof(int32_t) * t.eie.size()));
+    TRY(upload_raw(h, h->d_bc, t.bc_mask.data(), nn));
+    h->nnz_eie = (int64_t)t.eie.size();
     std::vector<int32_t> m32(std::max(nn, ne));
     for (size_t j = 0; j < nn; ++j) m32[j] = (int32_t)t.node_ext2int[j];
     TRY(upload_raw(h, h->d_node_ext2int, m32.data(), sizeof(int32_t) * nn));

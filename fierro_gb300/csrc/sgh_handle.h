@@ -79,6 +79,7 @@ struct fierro_sgh {
   int* d_node_ext2int = nullptr;
   int* d_elem_ext2int = nullptr;
   fierro::XferStatus* d_xfer = nullptr;
+  int64_t nnz_eie = 0;  // neighbour-list entries
 };
 
 namespace fierro {

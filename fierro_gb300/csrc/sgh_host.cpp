@@ -184,7 +184,7 @@ int boundary_masks(const fierro_mesh* mesh, const fierro_boundary* bcs, int64_t 
   return FIERRO_OK;
 }
 
-static int validate_mesh(const fierro_mesh* m) {
+int check_mesh_header(const fierro_mesh* m) {
   if (!m) return set_error(FIERRO_EINVAL, "mesh is NULL");
   if (m->num_nodes < 8 || m->num_elems < 1)
     return set_error(FIERRO_EINVAL, "mesh needs at least one hex (num_nodes=%lld num_elems=%lld)",
@@ -192,6 +192,12 @@ static int validate_mesh(const fierro_mesh* m) {
   if (!m->nodes_in_elem || !m->coords) return set_error(FIERRO_EINVAL, "mesh arrays are NULL");
   if (m->num_elems * 8 >= (int64_t)INT32_MAX || m->num_nodes >= (int64_t)INT32_MAX)
     return set_error(FIERRO_EINVAL, "mesh too large for 32-bit device indices");
+  return FIERRO_OK;
+}
+
+static int validate_mesh(const fierro_mesh* m) {
+  int rc = check_mesh_header(m);
+  if (rc) return rc;
   for (int64_t e = 0; e < m->num_elems; ++e) {
     for (int l = 0; l < 8; ++l) {
       uint64_t n = m->nodes_in_elem[e * 8 + l];
@@ -208,7 +214,7 @@ static int validate_mesh(const fierro_mesh* m) {
   return FIERRO_OK;
 }
 
-static int validate_bcs(const fierro_boundary* bcs, int64_t num_bcs) {
+int validate_bcs(const fierro_boundary* bcs, int64_t num_bcs) {
   if (num_bcs < 0 || (num_bcs > 0 && !bcs)) return set_error(FIERRO_EINVAL, "bad boundary list");
   for (int64_t s = 0; s < num_bcs; ++s) {
     if (bcs[s].surface < 0 || bcs[s].surface > 4)

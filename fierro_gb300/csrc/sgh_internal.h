@@ -35,6 +35,11 @@ struct HostTopo {
   int max_corners_per_node = 0;
 };
 
+// Null pointers, sizes and the 32-bit index limit of a mesh (no per-element checks).
+int check_mesh_header(const fierro_mesh* mesh);
+// Surface tags and condition kinds of a boundary deck.
+int validate_bcs(const fierro_boundary* bcs, int64_t num_bcs);
+
 // Validates the mesh and boundary deck and fills `t`.  `renumber` = false keeps
 // the caller's numbering (identity maps).
 int build_topology(const fierro_mesh* mesh, const fierro_boundary* bcs, int64_t num_bcs, bool renumber,

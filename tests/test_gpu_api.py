@@ -162,3 +162,28 @@ def test_direct_and_staged_transfers_agree(lib_built, monkeypatch):
             assert ei.value.code == sgh.FIERRO_EINVAL and "node 9" in str(ei.value)
     for k in outs[0]:
         assert np.array_equal(outs[0][k], outs[1][k]), k
+
+
+def test_device_topology_rejects_corrupt_meshes(lib_built, monkeypatch):
+    """Handle creation validates the mesh on the GPU (direct host access) and on
+    the host (staged builder) alike: out-of-range node ids, repeated nodes in an
+    element and non-finite coordinates are refused with the caller's index."""
+    import copy
+    from fierro_gb300 import sgh
+    for staged in ("0", "1"):
+        monkeypatch.setenv("FIERRO_STAGED_TRANSFERS", staged)
+        prob = _prob()
+        cases = []
+        p = copy.deepcopy(prob)
+        p.mesh.nodes_in_elem[17, 3] = p.mesh.num_nodes + 5
+        cases.append((p, "element 17"))
+        p = copy.deepcopy(prob)
+        p.mesh.nodes_in_elem[23, 6] = p.mesh.nodes_in_elem[23, 1]
+        cases.append((p, "element 23"))
+        p = copy.deepcopy(prob)
+        p.mesh.coords[11, 2] = float("inf")
+        cases.append((p, "coordinate at %d" % (11 * 3 + 2)))
+        for p, where in cases:
+            with pytest.raises(sgh.FierroError) as ei:
+                sgh.SGHSolver(p)
+            assert ei.value.code == sgh.FIERRO_EINVAL and where in str(ei.value), (staged, str(ei.value))
