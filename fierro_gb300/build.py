@@ -9,6 +9,7 @@ Translation units:
   csrc/sgh_batch.cpp   the batched-ensemble C ABI (g++)
   csrc/sgh_xfer.cu     host<->device state transfer kernels (GPU reads/writes host arrays)
   csrc/sgh_topo.cu     mesh topology on the GPU (renumbering, CSRs, boundary masks; --fmad=false)
+  csrc/sgh_setup.cu    the initial state on the GPU for fierro_sgh_setup (--fmad=false)
   csrc/sgh_adjoint.cu  discrete-adjoint kernels (--fmad=false, like the exact mode)
   csrc/sgh_adjoint.cpp the adjoint's checkpointing, replay and reverse schedule (g++)
   csrc/sgh_calib.cu    FP64 throughput calibration for the roofline
@@ -67,6 +68,9 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     units.append((os.path.join(OBJ, "sgh_calib.o"), nvcc_common + ["-c", calib], [calib]))
     topo = os.path.join(CSRC, "sgh_topo.cu")
     units.append((os.path.join(OBJ, "sgh_topo.o"), nvcc_common + ["--fmad=false", "-c", topo], [topo]))
+    setupk = os.path.join(CSRC, "sgh_setup.cu")
+    units.append((os.path.join(OBJ, "sgh_setup.o"),
+                  nvcc_common + ["--fmad=false", "-Xcompiler", "-fopenmp", "-c", setupk], [setupk]))
     xfer = os.path.join(CSRC, "sgh_xfer.cu")
     units.append((os.path.join(OBJ, "sgh_xfer.o"), nvcc_common + ["-c", xfer], [xfer]))
     adjk = os.path.join(CSRC, "sgh_adjoint.cu")

@@ -114,6 +114,40 @@ def main():
         w("  }")
     w("}")
     w("")
+    w("// The exact hex volume alone (geometry.cpp:271-310), the same operations in the")
+    w("// same order as hex_geometry's volume.")
+    w("__device__ __forceinline__ double hex_volume(const double* __restrict__ x, const double* __restrict__ y,")
+    w("    const double* __restrict__ z) {")
+    w("  const double twelth = 1. / 12.;")
+    O, I = comps[0]
+    for k, (p_, t, j) in enumerate(pairs):
+        terms = [v for v in T[p_][t] if v]
+        expr = ("-" if terms[0] < 0 else "") + "%s[%d]" % (I, abs(terms[0]) - 1)
+        for v_ in terms[1:]:
+            expr = "(%s %s %s[%d])" % (expr, "+" if v_ > 0 else "-", I, abs(v_) - 1)
+        w("  const double cm%d = %s;" % (k, expr))
+    used = set()
+    for a in range(8):
+        i = VI[a]
+        for jj in VJ[a]:
+            used.add((i, J[i].index(jj)))
+    for (p_, t) in sorted(used):
+        j = J[p_][t]
+        cm = ("cm%d" % pair_of[(p_, j)]) if p_ < j else ("(-cm%d)" % pair_of[(j, p_)])
+        w("  const double pr%d_%d = %s[%d] * %s;" % (p_, t, O, j, cm))
+    for a in range(8):
+        i = VI[a]
+        slots = [J[i].index(jj) for jj in VJ[a]]
+        expr = "pr%d_%d" % (i, slots[0])
+        for s_ in slots[1:]:
+            expr = "(%s + pr%d_%d)" % (expr, i, s_)
+        w("  const double vi%d = x[%d] * %s;" % (a, i, expr))
+    expr = "vi0"
+    for a in range(1, 8):
+        expr = "(%s + vi%d)" % (expr, a)
+    w("  return %s * twelth;" % expr)
+    w("}")
+    w("")
     w("// Reverse mode of the corner normals: given Bbar[lid*3+dim] (the adjoint of")
     w("// B(lid, dim)), accumulate the coordinate adjoints xbar, ybar, zbar[8].  B is")
     w("// bilinear, B(p,c) = sum_t O[j_t] comb_t(I) / 12, and each unordered pair (p, j)")

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <vector>
@@ -17,6 +18,7 @@
 #include "fierro_sgh.h"
 #include "sgh_hex.h"
 #include "sgh_internal.h"
+#include "sgh_setup.h"
 
 namespace fierro {
 
@@ -334,7 +336,7 @@ extern "C" int fierro_sgh_setup(const fierro_mesh* mesh, const fierro_material* 
                                 const fierro_mat_fill* fills, int64_t num_fills,
                                 const fierro_boundary* boundaries, int64_t num_bcs, fierro_sgh_state* out) {
   clear_error();
-  int rc = validate_mesh(mesh);
+  int rc = check_mesh_header(mesh);
   if (rc) return rc;
   rc = validate_bcs(boundaries, num_bcs);
   if (rc) return rc;
@@ -363,6 +365,13 @@ extern "C" int fierro_sgh_setup(const fierro_mesh* mesh, const fierro_material* 
     if (v == 5 && num_state_vars < 5)
       return set_error(FIERRO_EINVAL, "fill %lld: tg_vortex reads statev(4)", (long long)f);
   }
+  {
+    const char* env = std::getenv("FIERRO_STAGED_TRANSFERS");
+    if (!(env && env[0] == '1') && setup_gpu::usable(fills, num_fills))
+      return setup_gpu::run(mesh, state_vars, num_state_vars, fills, num_fills, boundaries, num_bcs, out);
+  }
+  rc = validate_mesh(mesh);
+  if (rc) return rc;
   const int64_t nn = mesh->num_nodes, ne = mesh->num_elems, nsv = num_state_vars;
   const uint64_t* nie = mesh->nodes_in_elem;
   double* X = out->node_coords;

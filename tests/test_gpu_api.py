@@ -187,3 +187,42 @@ def test_device_topology_rejects_corrupt_meshes(lib_built, monkeypatch):
             with pytest.raises(sgh.FierroError) as ei:
                 sgh.SGHSolver(p)
             assert ei.value.code == sgh.FIERRO_EINVAL and where in str(ei.value), (staged, str(ei.value))
+
+
+def _mixed_deck():
+    """Box / sphere / cylinder fills in sequence (later fills overwrite), three
+    velocity kinds, reflected planes and fixed curved surfaces."""
+    from fierro_gb300 import problems
+    from fierro_gb300.problems import Boundary, Fill, Material, Params, Problem
+    from fierro_gb300.mesh import box_mesh
+    m = box_mesh(11, length=1.0, jitter=0.1, seed=9, permute=True, name="mixed")
+    fills = [Fill("global", 0, den=1.0, sie=1e-10),
+             Fill("box", 1, x1=0.0, x2=0.35, y1=0.0, y2=0.35, z1=0.0, z2=0.35, den=2.0, sie=3.0),
+             Fill("sphere", 0, radius1=0.3, radius2=0.6, velocity="spherical", speed=-0.7, den=1.5, sie=0.2),
+             Fill("cylinder", 1, radius1=0.0, radius2=0.25, velocity="radial", speed=0.4, den=0.8, sie=1.0),
+             Fill("box", 0, x1=0.6, x2=1.0, y1=0.6, y2=1.0, z1=0.0, z2=1.0, velocity="cartesian", u=0.1, v=-0.2,
+                  w=0.3, den=1.1, sie=0.5)]
+    mats = [Material(gamma=1.4), Material(gamma=5.0 / 3.0, q1=1.2, q2ex=0.5)]
+    bcs = [Boundary("x_plane", 0.0, "reflected"), Boundary("y_plane", 0.0, "reflected"),
+           Boundary("sphere", 1.0, "fixed"), Boundary("cylinder", 0.9, "fixed")]
+    return Problem("mixed", m, mats, fills, bcs, Params(cycle_stop=10))
+
+
+def test_gpu_setup_equals_host_setup(lib_built, monkeypatch):
+    """fierro_sgh_setup on the GPU (kernels reading the mesh in place) writes the
+    same initial state, bit for bit, as the host set-up."""
+    from fierro_gb300 import problems, sgh
+    decks = [_prob(), problems.noh(9, jitter=0.1, seed=2, permute=True), _mixed_deck()]
+    for prob in decks:
+        monkeypatch.setenv("FIERRO_STAGED_TRANSFERS", "0")
+        a = sgh.setup(prob)
+        monkeypatch.setenv("FIERRO_STAGED_TRANSFERS", "1")
+        b = sgh.setup(prob)
+        for k in a:
+            assert np.array_equal(a[k], b[k]), (prob.name, k)
+    # and the mixed deck runs through the device topology and transfers
+    monkeypatch.setenv("FIERRO_STAGED_TRANSFERS", "0")
+    prob = _mixed_deck()
+    with sgh.SGHSolver(prob) as s:
+        s.set_state(sgh.setup(prob))
+        assert s.run(10) == 10

@@ -34,6 +34,7 @@ extern "C" void bmat_adj(const double* x, const double* y, const double* z, cons
   for (int i = 0; i < 24; ++i) out[i] = 0.0;
   hex_bmatrix_adjoint(x, y, z, bbar, out, out + 8, out + 16);
 }
+extern "C" double vol_only(const double* x, const double* y, const double* z) { return hex_volume(x, y, z); }
 extern "C" double cfl_min(const double* x, const double* y, const double* z) {
   double sx[8], sy[8], sz[8];
   for (int l = 0; l < 8; ++l) { sx[l] = x[l]; sy[l] = y[l]; sz[l] = z[l]; }
@@ -53,6 +54,8 @@ def geomlib(tmp_path_factory):
     lib = C.CDLL(str(so))
     lib.geom.argtypes = [C.c_void_p] * 8
     lib.bmat_adj.argtypes = [C.c_void_p] * 5
+    lib.vol_only.argtypes = [C.c_void_p] * 3
+    lib.vol_only.restype = C.c_double
     lib.cfl_min.argtypes = [C.c_void_p] * 3
     lib.cfl_min.restype = C.c_double
     return lib
@@ -184,3 +187,16 @@ def test_volume_gradient_is_bmatrix(oracle_built):
                 Xm[p, d] -= h
                 g = (orc.vol_hex(*[Xp[:, k] for k in range(3)]) - orc.vol_hex(*[Xm[:, k] for k in range(3)])) / (2 * h)
                 assert abs(g - B[p, d]) <= 1e-8, (trial, p, d)
+
+
+def test_generated_volume_alone_bitwise(geomlib, oracle_built):
+    """hex_volume (the set-up kernel's volume) equals the oracle's get_vol_hex bit for bit."""
+    from oracle import orc
+    rng = np.random.default_rng(13)
+    base = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], float)
+    for trial in range(300):
+        X = (base + rng.uniform(-0.2, 0.2, base.shape)) * 10 ** rng.uniform(-3, 1) + rng.uniform(-5, 5, 3)
+        cols = [np.ascontiguousarray(X[:, d]) for d in range(3)]
+        a = geomlib.vol_only(*[c.ctypes.data for c in cols])
+        b = orc.vol_hex(*cols)
+        assert a == b, (trial, a, b)
