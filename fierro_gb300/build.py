@@ -12,6 +12,7 @@ Translation units:
   csrc/sgh_setup.cu    the initial state on the GPU for fierro_sgh_setup (--fmad=false)
   csrc/sgh_adjoint.cu  discrete-adjoint kernels (--fmad=false, like the exact mode)
   csrc/sgh_adjoint.cpp the adjoint's checkpointing, replay and reverse schedule (g++)
+  csrc/sgh_output.cpp  graphics dumps: snapshot ring, writer thread, reference file formats (g++)
   csrc/sgh_calib.cu    FP64 throughput calibration for the roofline
   csrc/sgh_noalloc.cu  energy tallies with static scratch (no allocation)
 All compile in parallel; a unit is rebuilt only when it or a header changed.
@@ -72,14 +73,14 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     units.append((os.path.join(OBJ, "sgh_setup.o"),
                   nvcc_common + ["--fmad=false", "-Xcompiler", "-fopenmp", "-c", setupk], [setupk]))
     xfer = os.path.join(CSRC, "sgh_xfer.cu")
-    units.append((os.path.join(OBJ, "sgh_xfer.o"), nvcc_common + ["-c", xfer], [xfer]))
+    units.append((os.path.join(OBJ, "sgh_xfer.o"), nvcc_common + ["--fmad=false", "-c", xfer], [xfer]))
     adjk = os.path.join(CSRC, "sgh_adjoint.cu")
     units.append((os.path.join(OBJ, "sgh_adjoint_k.o"), nvcc_common + ["--fmad=false", "-c", adjk], [adjk]))
     noalloc = os.path.join(CSRC, "sgh_noalloc.cu")
     units.append((os.path.join(OBJ, "sgh_noalloc.o"), nvcc_common + ["-c", noalloc], [noalloc]))
     gxx = ["g++", "-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wall", "-Wno-unknown-pragmas",
            "-I", os.path.join(CUDA_HOME, "include")] + inc
-    for name in ("sgh_host.cpp", "sgh_capi.cpp", "sgh_batch.cpp", "sgh_adjoint.cpp"):
+    for name in ("sgh_host.cpp", "sgh_capi.cpp", "sgh_batch.cpp", "sgh_adjoint.cpp", "sgh_output.cpp"):
         src = os.path.join(CSRC, name)
         units.append((os.path.join(OBJ, name.replace(".cpp", ".o")), gxx + ["-c", src], [src]))
     jobs = []

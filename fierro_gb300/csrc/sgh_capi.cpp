@@ -186,10 +186,16 @@ void enqueue_cycle(fierro_sgh* h, int c) {
   enqueue_dt(h);
   for (int s = 0; s < h->rk_num_stages; ++s) enqueue_stage(h, c, s);
   h->ks->end(h->d_ctrl, h->lp, h->stream);
+  // a write event of this cycle: snapshot of the state it left in bin c ^ 1
+  if (h->out) xfer::launch_snapshot(output_snap_args(h, c ^ 1, 0), h->stream);
 }
 
 int build_graphs(fierro_sgh* h) {
   for (int c = 0; c < 2; ++c) {
+    if (h->graph[c]) {
+      cudaGraphExecDestroy(h->graph[c]);
+      h->graph[c] = nullptr;
+    }
     cudaGraph_t g = nullptr;
     CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     enqueue_cycle(h, c);
@@ -200,6 +206,15 @@ int build_graphs(fierro_sgh* h) {
   }
   return FIERRO_OK;
 }
+
+}  // namespace
+
+int fierro::rebuild_graphs(fierro_sgh* h) {
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return build_graphs(h);
+}
+
+namespace {
 
 int validate_params(const fierro_sgh_params* p) {
   if (!p) return set_error(FIERRO_EINVAL, "params is NULL");
@@ -216,6 +231,7 @@ int validate_params(const fierro_sgh_params* p) {
 extern "C" int fierro_sgh_destroy(fierro_sgh* h) {
   if (!h) return FIERRO_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
+  output_release(h);
   adj_release(h);
   for (int c = 0; c < 2; ++c)
     if (h->graph[c]) cudaGraphExecDestroy(h->graph[c]);
@@ -302,6 +318,8 @@ static int create_impl(fierro_sgh* h, const fierro_mesh* mesh, const fierro_mate
   TRY(dalloc(h, &h->d_ctrl, 1));
   TRY(dalloc(h, &h->d_node_ext2int, nn));
   TRY(dalloc(h, &h->d_elem_ext2int, ne));
+  TRY(dalloc(h, &h->d_node_int2ext, nn));
+  TRY(dalloc(h, &h->d_elem_int2ext, ne));
   TRY(dalloc(h, &h->d_xfer, 1));
   TRY(dalloc(h, &h->d_energy_part, 2 * 512));
   TRY(dalloc(h, &h->d_energy_out, 2));
@@ -326,6 +344,10 @@ static int create_impl(fierro_sgh* h, const fierro_mesh* mesh, const fierro_mate
     TRY(upload_raw(h, h->d_node_ext2int, m32.data(), sizeof(int32_t) * nn));
     for (size_t j = 0; j < ne; ++j) m32[j] = (int32_t)t.elem_ext2int[j];
     TRY(upload_raw(h, h->d_elem_ext2int, m32.data(), sizeof(int32_t) * ne));
+    for (size_t j = 0; j < nn; ++j) m32[j] = (int32_t)t.node_int2ext[j];
+    TRY(upload_raw(h, h->d_node_int2ext, m32.data(), sizeof(int32_t) * nn));
+    for (size_t j = 0; j < ne; ++j) m32[j] = (int32_t)t.elem_int2ext[j];
+    TRY(upload_raw(h, h->d_elem_int2ext, m32.data(), sizeof(int32_t) * ne));
   }
   std::vector<double> q((size_t)num_materials * 4);
   for (int64_t m = 0; m < num_materials; ++m) {
@@ -392,6 +414,7 @@ static int set_state_impl(fierro_sgh* h, const fierro_sgh_state* s, double time_
     // the GPU reads the caller's arrays and validates them in the same pass
     h->has_state = false;
     CUDA_TRY(cudaStreamSynchronize(h->stream));
+    output_reset(h);
     XferStatus xs{};
     TRY(xfer::upload_state(h, s, &xs));
     if (xs.flags & (1u << XferStatus::STRESS))
@@ -422,6 +445,7 @@ static int set_state_impl(fierro_sgh* h, const fierro_sgh_state* s, double time_
   for (int64_t n = 0; n < nn; ++n)
     if (!(s->node_mass[n] > 0.0)) return set_error(FIERRO_EINVAL, "set_state: node %lld mass <= 0", (long long)n);
   CUDA_TRY(cudaStreamSynchronize(h->stream));
+  output_reset(h);
   int slot = 0;
   // reference bin 1 -> device bin 0 (current), bin 0 -> device bin 1
   for (int rb = 0; rb < 2; ++rb) {
@@ -528,7 +552,9 @@ extern "C" int fierro_sgh_enqueue_cycles(fierro_sgh* h, int64_t cycles) {
   if (h->stage != 0) return set_error(FIERRO_EINVAL, "a cycle is partly run; finish it with run_stages");
   for (int64_t i = 0; i < cycles; ++i) {
     const int c = (int)((h->base + h->enq_cycles) & 1);
+    if (h->out) TRY(output_before_cycle(h, h->enq_cycles));
     CUDA_TRY(cudaGraphLaunch(h->graph[c], h->stream));
+    if (h->out) TRY(output_after_cycle(h));
     h->enq_cycles++;
   }
   return FIERRO_OK;
@@ -671,6 +697,41 @@ extern "C" int fierro_sgh_energy(fierro_sgh* h, double* ie, double* ke) {
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   if (ie) *ie = out[0];
   if (ke) *ke = out[1];
+  return FIERRO_OK;
+}
+
+extern "C" int fierro_sgh_device_view(fierro_sgh* h, fierro_device_view* v) {
+  clear_error();
+  if (!h || !v) return set_error(FIERRO_EINVAL, "handle or view is NULL");
+  if (!h->has_state) return set_error(FIERRO_EINVAL, "device_view before set_state");
+  if (h->stage != 0) return set_error(FIERRO_EINVAL, "device_view in the middle of a cycle");
+  long long cyc = 0;
+  TRY(cycles_done(h, &cyc));
+  const int c = bin_now(h, cyc);
+  std::memset(v, 0, sizeof(*v));
+  v->num_nodes = h->nn;
+  v->num_elems = h->ne;
+  v->x = h->d_x[c][0];
+  v->y = h->d_x[c][1];
+  v->z = h->d_x[c][2];
+  v->u = h->d_v[c][0];
+  v->v = h->d_v[c][1];
+  v->w = h->d_v[c][2];
+  v->node_mass = h->d_node_mass;
+  v->den = h->d_den;
+  v->pres = h->d_pres;
+  v->sspd = h->d_sspd;
+  v->sie = h->d_sie[c];
+  v->vol = h->d_vol;
+  v->mass = h->d_elem_mass;
+  const long long stages_done = cyc * h->rk_num_stages;
+  v->div = h->d_div[stages_done == 0 ? 1 : (int)((stages_done - 1) & 1)];
+  v->corner_force = h->d_force;
+  v->node_int2ext = h->d_node_int2ext;
+  v->elem_int2ext = h->d_elem_int2ext;
+  v->node_ext2int = h->d_node_ext2int;
+  v->elem_ext2int = h->d_elem_ext2int;
+  v->stream = h->stream;
   return FIERRO_OK;
 }
 

@@ -33,7 +33,7 @@ struct Ctrl {
   int active;          // the current cycle runs (set by the dt kernel)
   int stopped;         // time_value reached time_final
   unsigned int status; // FIERRO_STATUS_* bits
-  int pad;
+  int wrote;           // the last cycle ended with a write event (graphics dump)
 };
 
 #define FIERRO_STATUS_BAD_VOLUME 1u  // non-positive or non-finite element volume

@@ -30,6 +30,7 @@
 
 namespace fierro {
 struct AdjState;
+struct OutputState;
 }
 
 struct fierro_sgh {
@@ -78,8 +79,11 @@ struct fierro_sgh {
   bool direct_host = false;
   int* d_node_ext2int = nullptr;
   int* d_elem_ext2int = nullptr;
+  int* d_node_int2ext = nullptr;
+  int* d_elem_int2ext = nullptr;
   fierro::XferStatus* d_xfer = nullptr;
   int64_t nnz_eie = 0;  // neighbour-list entries
+  fierro::OutputState* out = nullptr;  // graphics dumps (sgh_output.cpp)
 };
 
 namespace fierro {
@@ -124,6 +128,15 @@ inline int div_parity(const fierro_sgh* h, int c, int s) { return (c * h->rk_num
 
 // Frees the adjoint's device memory (no-op without one).
 void adj_release(fierro_sgh* h);
+
+// Graphics dumps (sgh_output.cpp).
+void output_release(fierro_sgh* h);
+xfer::SnapArgs output_snap_args(fierro_sgh* h, int bin, int force);
+int output_before_cycle(fierro_sgh* h, long long cycles_enqueued);
+int output_after_cycle(fierro_sgh* h);
+void output_reset(fierro_sgh* h);
+// Re-instantiates the per-parity cycle graphs (with or without the snapshot).
+int rebuild_graphs(fierro_sgh* h);
 
 }  // namespace fierro
 

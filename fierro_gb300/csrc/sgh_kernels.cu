@@ -390,6 +390,7 @@ __global__ void __launch_bounds__(256) k_dt_batch(const DtArgs a) {
 
 // End of a cycle (sgh_solve.cpp:590-632).
 __device__ __forceinline__ void end_update(Ctrl* c, const LoopParams& lp) {
+  c->wrote = 0;
   if (!c->active) return;
   c->time_value += c->dt;
   const long long cycle = c->cycle;
@@ -398,6 +399,7 @@ __device__ __forceinline__ void end_update(Ctrl* c, const LoopParams& lp) {
   else if (c->time_value >= lp.time_final) write = true;
   else if (c->time_value >= c->graphics_time) write = true;
   if (write) c->graphics_time = c->time_value + lp.graphics_dt_ival;
+  c->wrote = write ? 1 : 0;
   if (c->time_value >= lp.time_final) c->stopped = 1;
   c->cycle = cycle + 1;
   c->active = 0;

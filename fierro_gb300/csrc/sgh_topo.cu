@@ -346,9 +346,8 @@ int build_device(fierro_sgh* h, const fierro_mesh* mesh, const fierro_boundary* 
   TRY(sc.alloc(&va, (size_t)nmax));
   TRY(sc.alloc(&vb, (size_t)nmax));
   k_centroids<<<nblk(ne), kBlock, 0, st>>>(ne, nie_ext, xyz, cen, box + 6);
-  int *elem_int2ext = nullptr, *node_int2ext = nullptr;
-  TRY(sc.alloc(&elem_int2ext, (size_t)ne));
-  TRY(sc.alloc(&node_int2ext, (size_t)nn));
+  int* elem_int2ext = h->d_elem_int2ext;
+  int* node_int2ext = h->d_node_int2ext;
   {
     uint64_t* k = ka;
     int* v = va;

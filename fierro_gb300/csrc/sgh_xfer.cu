@@ -188,7 +188,80 @@ __global__ void __launch_bounds__(kBlock) k_down_force(const ElemDown a) {
   for (int k = threadIdx.x; k < cnt * 24; k += kBlock) o[k] = buf[k];
 }
 
+// Snapshot of the state for a graphics dump, in the caller's numbering, with
+// the per-element fields write_outputs derives: the element speed from the
+// average of its nodes' velocities (outputs.cpp:133-156) and the element
+// centroid and radii of the state file (outputs.cpp:451-475), in the
+// reference's operation order (this unit compiles without contraction).
+__global__ void __launch_bounds__(kBlock) k_snap(const SnapArgs a) {
+  if (!a.force && !a.ctrl->wrote) return;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t slot = (size_t)(*a.count % (unsigned long long)a.nslots);
+  double* base = a.ring + slot * ((size_t)kSnapNodeRows * a.nn + (size_t)kSnapElemRows * a.ne);
+  if (t < a.nn) {
+    const int j = (int)t, i = a.node_ext2int[j];
+    base[j] = a.x[i];
+    base[(size_t)a.nn + j] = a.y[i];
+    base[2 * (size_t)a.nn + j] = a.z[i];
+    base[3 * (size_t)a.nn + j] = a.u[i];
+    base[4 * (size_t)a.nn + j] = a.v[i];
+    base[5 * (size_t)a.nn + j] = a.w[i];
+  }
+  if (t < a.ne) {
+    const int E = (int)t, e = a.elem_ext2int[E];
+    double* eb = base + (size_t)kSnapNodeRows * a.nn;
+    const size_t ne = (size_t)a.ne;
+    eb[E] = a.den[e];
+    eb[ne + E] = a.pres[e];
+    eb[2 * ne + E] = a.sie[e];
+    eb[3 * ne + E] = a.vol[e];
+    eb[4 * ne + E] = a.mass[e];
+    eb[5 * ne + E] = a.sspd[e];
+    double ev[3] = {0.0, 0.0, 0.0}, ec[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int l = 0; l < 8; ++l) {
+      const int n = a.nie[(size_t)e * 8 + l];
+      ev[0] += a.u[n];
+      ev[1] += a.v[n];
+      ev[2] += a.w[n];
+      ec[0] += a.x[n];
+      ec[1] += a.y[n];
+      ec[2] += a.z[n];
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      ev[d] = ev[d] / 8.0;
+      ec[d] = ec[d] / 8.0;
+    }
+    double speed_sqrd = 0.0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) speed_sqrd += ev[d] * ev[d];
+    eb[6 * ne + E] = sqrt(speed_sqrd);
+    eb[7 * ne + E] = (double)a.mat[e];
+    eb[8 * ne + E] = ec[0];
+    eb[9 * ne + E] = ec[1];
+    eb[10 * ne + E] = ec[2];
+    eb[11 * ne + E] = sqrt(ec[0] * ec[0] + ec[1] * ec[1]);
+    eb[12 * ne + E] = sqrt(ec[0] * ec[0] + ec[1] * ec[1] + ec[2] * ec[2]);
+  }
+}
+
+__global__ void k_snap_publish(const SnapArgs a) {
+  if (!a.force && !a.ctrl->wrote) return;
+  const unsigned long long c = *a.count;
+  a.times[c % (unsigned long long)a.nslots] = a.ctrl->time_value;
+  *a.count = c + 1;
+  __threadfence_system();
+  *(volatile unsigned long long*)a.produced = c + 1;
+}
+
 }  // namespace
+
+void launch_snapshot(const SnapArgs& a, cudaStream_t s) {
+  const long long n = a.nn > a.ne ? a.nn : a.ne;
+  k_snap<<<blocks(n), kBlock, 0, s>>>(a);
+  k_snap_publish<<<1, 1, 0, s>>>(a);
+}
 
 bool direct_host_access() {
   int dev = 0, v = 0;

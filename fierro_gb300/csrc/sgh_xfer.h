@@ -5,6 +5,7 @@
 #define FIERRO_SGH_XFER_H
 
 #include "fierro_sgh.h"
+#include "sgh_device.h"
 
 struct fierro_sgh;
 
@@ -32,6 +33,29 @@ int upload_state(fierro_sgh* h, const fierro_sgh_state* s, XferStatus* status);
 // from device bin bins[rb]; elem_div from divergence buffer div_buffer; stress
 // as zeros.
 int download_state(fierro_sgh* h, fierro_sgh_state* s, const int bins[2], int div_buffer);
+
+// Graphics-dump snapshots (write_outputs, outputs.cpp:10-506): one slot of the
+// device ring holds, in the caller's numbering, node rows x, y, z, u, v, w
+// (kSnapNodeRows x nn) then element rows den, pres, sie, vol, mass, sspd,
+// speed, mat_id, centroid x, y, z, radius_2D, radius_3D (kSnapElemRows x ne).
+constexpr int kSnapNodeRows = 6, kSnapElemRows = 13;
+
+struct SnapArgs {
+  int nn, ne, nslots, force;  // force: snapshot whether or not the cycle wrote
+  const Ctrl* ctrl;
+  const int *node_ext2int, *elem_ext2int, *nie;  // nie: internal [ne][8]
+  const double *x, *y, *z, *u, *v, *w;           // the state bin after the cycle
+  const double *den, *pres, *sie, *vol, *mass, *sspd;
+  const int* mat;
+  double* ring;                  // nslots slots
+  double* times;                 // [nslots] time_value of each slot
+  unsigned long long* count;     // snapshots taken (device)
+  unsigned long long* produced;  // host-mapped mirror of count, written last
+};
+
+// Two launches on `s`: the gather (a no-op unless ctrl->wrote or force) and the
+// single-thread publication of the slot's time and the new count.
+void launch_snapshot(const SnapArgs& a, cudaStream_t s);
 
 }  // namespace xfer
 }  // namespace fierro

@@ -24,6 +24,7 @@ LIB_PATH = os.path.join(HERE, "libfierro_sgh.so")
 
 FIERRO_OK, FIERRO_EINVAL, FIERRO_ENOMEM, FIERRO_ECUDA, FIERRO_ENUMERIC, FIERRO_ETIMEDOUT, FIERRO_ENOTSUP = range(7)
 FP_EXACT, FP_FMA = 0, 1
+OUTPUT_ENSIGHT, OUTPUT_STATE = 1, 2
 _ERRNAMES = {1: "EINVAL", 2: "ENOMEM", 3: "ECUDA", 4: "ENUMERIC", 5: "ETIMEDOUT", 6: "ENOTSUP"}
 
 
@@ -105,6 +106,9 @@ def _load():
     lib.fierro_batch_num_instances.restype = i64
     lib.fierro_batch_device_bytes.argtypes = [vp]
     lib.fierro_batch_device_bytes.restype = i64
+    lib.fierro_sgh_device_view.argtypes = [vp, vp]
+    lib.fierro_sgh_set_output.argtypes = [vp, C.c_char_p, C.c_int, C.c_int]
+    lib.fierro_sgh_flush_output.argtypes = [vp, C.POINTER(i64)]
     lib.fierro_adj_forward.argtypes = [vp, vp, vp, i64, i64, C.POINTER(i64)]
     lib.fierro_adj_backward.argtypes = [vp, vp, vp, vp, vp]
     lib.fierro_adj_verify.argtypes = [vp, C.c_int]
@@ -297,6 +301,41 @@ class SGHSolver:
     def device_bytes(self) -> int:
         return int(_lib.fierro_sgh_device_bytes(self.h))
 
+    def set_output(self, directory: Optional[str], ensight: bool = True, state: bool = True, slots: int = 4):
+        """Graphics dumps of write_outputs (EnSight Gold and the element state
+        text) under `directory`, written by the handle's writer thread while the
+        cycles run; None turns them off."""
+        what = (OUTPUT_ENSIGHT if ensight else 0) | (OUTPUT_STATE if state else 0)
+        _check(_lib.fierro_sgh_set_output(self.h, None if directory is None else directory.encode(),
+                                          what if directory is not None else 0, slots))
+
+    def flush_output(self) -> int:
+        """Waits for the dumps taken so far; returns how many were written since set_state."""
+        n = C.c_int64(0)
+        _check(_lib.fierro_sgh_flush_output(self.h, C.byref(n)))
+        return n.value
+
+    def device_view(self) -> Dict[str, object]:
+        """The device-resident state as torch tensors over the library's memory
+        (no copy), in the device numbering, with the int32 renumbering maps
+        (caller id = node_int2ext[device id]).  Valid until the next call that runs
+        cycles or uploads a state."""
+        import torch
+        from torch.utils.dlpack import from_dlpack
+        v = DeviceView()
+        _check(_lib.fierro_sgh_device_view(self.h, C.byref(v)))
+        dev = torch.cuda.current_device()
+        nn, ne = v.num_nodes, v.num_elems
+        out = {}
+        for k in ("x", "y", "z", "u", "v", "w", "node_mass"):
+            out[k] = from_dlpack(_dlpack_capsule(getattr(v, k), (nn,), 2, 64, dev))
+        for k in ("den", "pres", "sspd", "sie", "vol", "mass", "div"):
+            out[k] = from_dlpack(_dlpack_capsule(getattr(v, k), (ne,), 2, 64, dev))
+        out["corner_force"] = from_dlpack(_dlpack_capsule(v.corner_force, (24, ne), 2, 64, dev))
+        for k, n in (("node_int2ext", nn), ("elem_int2ext", ne), ("node_ext2int", nn), ("elem_ext2int", ne)):
+            out[k] = from_dlpack(_dlpack_capsule(getattr(v, k), (n,), 0, 32, dev))
+        return out
+
     def adj_forward(self, sie0=None, gamma=None, cycles: int = 1, ckpt_every: int = 20) -> int:
         """fierro_adj_forward: replace the current state's sie (and per-element gamma)
         by the parameters, recompute pressure and sound speed, run `cycles` cycles
@@ -332,6 +371,57 @@ class SGHSolver:
 
     def adj_release(self):
         _check(_lib.fierro_adj_release(self.h))
+
+
+class DeviceView(C.Structure):
+    _fields_ = [("num_nodes", C.c_int64), ("num_elems", C.c_int64)] + \
+        [(k, C.c_void_p) for k in ("x", "y", "z", "u", "v", "w", "node_mass", "den", "pres", "sspd", "sie", "vol",
+                                   "mass", "div", "corner_force", "node_int2ext", "elem_int2ext", "node_ext2int",
+                                   "elem_ext2int", "stream")]
+
+
+# ---- DLPack (zero-copy hand-over of device arrays to torch) -------------------
+class _DLDevice(C.Structure):
+    _fields_ = [("device_type", C.c_int32), ("device_id", C.c_int32)]
+
+
+class _DLDataType(C.Structure):
+    _fields_ = [("code", C.c_uint8), ("bits", C.c_uint8), ("lanes", C.c_uint16)]
+
+
+class _DLTensor(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("device", _DLDevice), ("ndim", C.c_int32), ("dtype", _DLDataType),
+                ("shape", C.POINTER(C.c_int64)), ("strides", C.POINTER(C.c_int64)), ("byte_offset", C.c_uint64)]
+
+
+class _DLManagedTensor(C.Structure):
+    pass
+
+
+_DLDeleter = C.CFUNCTYPE(None, C.POINTER(_DLManagedTensor))
+_DLManagedTensor._fields_ = [("dl_tensor", _DLTensor), ("manager_ctx", C.c_void_p), ("deleter", _DLDeleter)]
+_dl_alive = {}  # managed tensors handed out and not yet released by their consumer
+
+
+@_DLDeleter
+def _dl_release(mt):
+    _dl_alive.pop(C.addressof(mt.contents), None)
+
+
+def _dlpack_capsule(ptr: int, shape, code: int, bits: int, device: int):
+    """A 'dltensor' capsule over device memory the library owns (the deleter only
+    drops the descriptor; the memory stays with the handle)."""
+    shp = (C.c_int64 * len(shape))(*shape)
+    mt = _DLManagedTensor()
+    mt.dl_tensor = _DLTensor(C.c_void_p(ptr), _DLDevice(2, device), len(shape), _DLDataType(code, bits, 1),
+                             C.cast(shp, C.POINTER(C.c_int64)), None, 0)
+    mt.manager_ctx = None
+    mt.deleter = _dl_release
+    _dl_alive[C.addressof(mt)] = (mt, shp)
+    new = C.pythonapi.PyCapsule_New
+    new.restype = C.py_object
+    new.argtypes = [C.c_void_p, C.c_char_p, C.c_void_p]
+    return new(C.addressof(mt), b"dltensor", None)
 
 
 class AdjSeed(C.Structure):

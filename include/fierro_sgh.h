@@ -230,6 +230,42 @@ int fierro_energy_tally_noalloc(const double* elem_mass, const double* elem_sie,
  * throughput, in fused multiply-adds per second (one FMA = 2 FLOP). */
 int fierro_measure_fp64_rate(double* dfma_per_second);
 
+/* Graphics dumps (write_outputs, outputs.cpp:10-506), written off the critical
+ * path.  With outputs on, every write event of the cycle loop -- t = 0 of a
+ * freshly uploaded state (sgh_solve.cpp:45) and each cycle that meets the write
+ * condition (graphics_cyc_ival, graphics_time, time_final; sgh_solve.cpp:590-632)
+ * -- snapshots the state into a device ring of `slots` slots; a writer thread
+ * of the handle writes, under `directory`, the reference's files byte for byte:
+ * FIERRO_OUTPUT_ENSIGHT  ensight/Outputs_SGH.case, ensight/data/Outputs_SGH.NNNNN.*
+ * FIERRO_OUTPUT_STATE    state/elem_state_t<time>.txt
+ * Snapshots are taken by fierro_sgh_run / fierro_sgh_enqueue_cycles (which then
+ * keep at most two cycles in flight beyond the free slots), not by the stage-
+ * stepping and event-timed entry points.  directory == NULL or what == 0 turns
+ * outputs off.  A new set_state restarts the numbering at 00000. */
+#define FIERRO_OUTPUT_ENSIGHT 1
+#define FIERRO_OUTPUT_STATE 2
+int fierro_sgh_set_output(fierro_sgh* h, const char* directory, int what, int slots);
+/* Waits until every snapshot taken so far is written; *dumps = dumps written
+ * since the last set_state.  Reports a write error of the writer thread. */
+int fierro_sgh_flush_output(fierro_sgh* h, int64_t* dumps);
+
+/* Device-resident state of a handle for zero-copy use (e.g. torch tensors over
+ * the same memory).  Arrays are in the device numbering (Morton order); the
+ * maps convert: caller id = *_int2ext[device id], device id = *_ext2int[caller
+ * id].  Valid until the next call that runs cycles or uploads a state (the
+ * state bins swap each cycle); work on them belongs on `stream` or after
+ * fierro_sgh_synchronize.  No counterpart in the reference (its device mirror
+ * is private to the DViewCArrayKokkos objects). */
+typedef struct {
+  int64_t num_nodes, num_elems;
+  double *x, *y, *z, *u, *v, *w, *node_mass;                 /* [Nn] */
+  double *den, *pres, *sspd, *sie, *vol, *mass, *div;        /* [Ne] */
+  double* corner_force;                                      /* [24][Ne], row lid*3+dim */
+  const int32_t *node_int2ext, *elem_int2ext, *node_ext2int, *elem_ext2int;
+  void* stream;                                              /* the handle's cudaStream_t */
+} fierro_device_view;
+int fierro_sgh_device_view(fierro_sgh* h, fierro_device_view* view);
+
 /* ---- discrete adjoint of the cycle loop ------------------------------------
  * No counterpart in the reference, which has no adjoint; these differentiate the
  * loop that fierro_sgh_run executes (sgh_solve.cpp:125-634), with the

@@ -5,13 +5,15 @@ Products, all written only under oracle/_ref/ (git-ignored):
 * liborc_sgh.so, liborc_sgh_crpow.so -- the plain-C restatement in oracle/sgh_oracle.c
   (libm pow, and a correctly rounded pow variant), compiled with
   -ffp-contract=off so its doubles follow the reference's uncontracted evaluation.
-* fierro_ref / fierro_ref_geo / fierro_ref_fast -- the reference's own SGH solver
+* fierro_ref / fierro_ref_geo / fierro_ref_fast / fierro_ref_out -- the reference's own SGH solver
   (Explicit-Lagrange-Kokkos/SGH_solver/*.cpp, unmodified) compiled with g++ -fopenmp
   against the project-written MATAR/Kokkos stand-in oracle/compat/matar.h, with
   input.cpp, the mesh reader and the driver replaced by the files in oracle/ref/.
   fierro_ref_geo links the reference's own EnSight reader (read_mesh.cpp);
   fierro_ref reads binary meshes; fierro_ref_fast is fierro_ref with the compiler's
-  default floating-point contraction (used for timing only).
+  default floating-point contraction (used for timing only); fierro_ref_out links
+  the reference's outputs.cpp and writes its EnSight / state files (the checker
+  of the library's graphics dumps).
 
 The reference sources are compiled where they lie when the reference tree is
 present.  They are also staged into oracle/_ref/src/ (git-ignored) so that a
@@ -38,6 +40,7 @@ REF_UNITS = [
 ]
 REF_HEADERS = ["mesh.h", "state.h"]
 REF_GEO_READER = "read_mesh.cpp"
+REF_OUTPUTS = "outputs.cpp"
 
 
 def _run(cmd):
@@ -72,7 +75,7 @@ def build_oracle_lib(verbose=False):
 def _source_dir():
     if os.path.isdir(REF_SGH):
         os.makedirs(STAGE, exist_ok=True)
-        for f in REF_UNITS + REF_HEADERS + [REF_GEO_READER]:
+        for f in REF_UNITS + REF_HEADERS + [REF_GEO_READER, REF_OUTPUTS]:
             dst = os.path.join(STAGE, f)
             srcf = os.path.join(REF_SGH, f)
             if not os.path.exists(dst) or os.path.getmtime(dst) < os.path.getmtime(srcf):
@@ -106,6 +109,14 @@ def build_reference(verbose=False, jobs=None):
             obj = os.path.join(OUT, "obj", "%s.%s.o" % (name, var))
             if not _newer(obj, [path] + headers + [__file__]):
                 jobs_list.append(base + flags + ["-c", path, "-o", obj])
+    # the graphics-dump variant: the reference's own outputs.cpp, harness without its no-op
+    # (outputs.cpp gets <string> through the Kokkos headers in its own build)
+    out_units = [(os.path.join(src_dir, REF_OUTPUTS), REF_OUTPUTS, ["-include", "string"]),
+                 (os.path.join(ref_dir, "ref_harness.cpp"), "ref_harness_out.cpp", ["-DFIERRO_REF_REAL_OUTPUTS"])]
+    for path, name, extra in out_units:
+        obj = os.path.join(OUT, "obj", "%s.exact.o" % name)
+        if os.path.exists(path) and not _newer(obj, [path] + headers + [__file__]):
+            jobs_list.append(base + variants["exact"] + extra + ["-c", path, "-o", obj])
     with ThreadPoolExecutor(max_workers=jobs or os.cpu_count() or 4) as ex:
         list(ex.map(_run, jobs_list))
 
@@ -113,7 +124,10 @@ def build_reference(verbose=False, jobs=None):
         names = REF_UNITS + [reader, "ref_input.cpp", "ref_harness.cpp"]
         return [os.path.join(OUT, "obj", "%s.%s.o" % (n, var)) for n in names]
 
+    out_objs = [o for o in objs("exact", "ref_read_mesh_bin.cpp") if not o.endswith("ref_harness.cpp.exact.o")]
+    out_objs += [os.path.join(OUT, "obj", "%s.exact.o" % n) for n in (REF_OUTPUTS, "ref_harness_out.cpp")]
     out = {
+        "fierro_ref_out": (out_objs, "exact"),
         "fierro_ref": (objs("exact", "ref_read_mesh_bin.cpp"), "exact"),
         "fierro_ref_geo": (objs("exact", REF_GEO_READER), "exact"),
         "fierro_ref_fast": (objs("fast", "ref_read_mesh_bin.cpp"), "fast"),

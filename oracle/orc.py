@@ -222,9 +222,11 @@ def read_state_dump(path: str) -> dict:
 
 
 def run_reference(problem, cycles: int | None = None, kind: str = "fierro_ref", threads: int | None = None,
-                  geo_path: str | None = None, workdir: str | None = None, warmup: int = 0) -> dict:
+                  geo_path: str | None = None, workdir: str | None = None, warmup: int = 0,
+                  cwd: str | None = None) -> dict:
     """Run the reference executable on the deck; returns the final state plus
-    'calc_seconds' (the reference's own cycle-loop timer, sgh_solve.cpp:637-641)."""
+    'calc_seconds' (the reference's own cycle-loop timer, sgh_solve.cpp:637-641).
+    kind='fierro_ref_out' also writes the reference's graphics dumps into `cwd`."""
     from fierro_gb300.mesh import write_mesh_bin
     import copy
     prob = copy.deepcopy(problem)
@@ -251,7 +253,7 @@ def run_reference(problem, cycles: int | None = None, kind: str = "fierro_ref", 
         env.setdefault("OMP_PROC_BIND", "spread")
         env.setdefault("OMP_PLACES", "cores")
         p = subprocess.run([exe, cfg, mesh_path, out], stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
-                           text=True, env=env)
+                           text=True, env=env, cwd=cwd)
         if p.returncode != 0:
             raise RuntimeError("reference run failed:\n" + p.stdout[-4000:])
         st = read_state_dump(out)

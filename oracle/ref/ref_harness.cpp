@@ -2,8 +2,11 @@
 // Explicit-Lagrange-Kokkos/SGH_solver/driver.cpp:70-328 (input, mesh read,
 // connectivity, dual views, get_vol, setup, sgh_solve) followed by a binary dump
 // of the final state.  It also supplies write_outputs (outputs.cpp:10-78) as a
-// no-op, since graphics dumps are outside the measured path.  Linked only into
-// the reference oracle executables built by oracle/build_ref.py.
+// no-op, since graphics dumps are outside the measured path, except in the
+// fierro_ref_out build (-DFIERRO_REF_REAL_OUTPUTS), which links the reference's
+// own outputs.cpp and writes its EnSight and state files into the working
+// directory.  Linked only into the reference oracle executables built by
+// oracle/build_ref.py.
 //
 // usage: fierro_ref <config.txt> <mesh.geo|mesh.bin> <state_out.bin>
 // env FIERRO_REF_WARMUP=W runs W untimed cycles first (see main).
@@ -22,6 +25,7 @@
 
 const char* fierro_ref_config_path = nullptr;
 
+#ifndef FIERRO_REF_REAL_OUTPUTS
 void write_outputs(const mesh_t& mesh, DViewCArrayKokkos<double>& node_coords,
                    DViewCArrayKokkos<double>& node_vel, DViewCArrayKokkos<double>& node_mass,
                    DViewCArrayKokkos<double>& elem_den, DViewCArrayKokkos<double>& elem_pres,
@@ -32,6 +36,7 @@ void write_outputs(const mesh_t& mesh, DViewCArrayKokkos<double>& node_coords,
   graphics_times(graphics_id) = time_value;
   graphics_id = (graphics_id + 1) % graphics_times.size();
 }
+#endif
 
 static void put(FILE* f, const double* p, size_t n) { std::fwrite(p, sizeof(double), n, f); }
 

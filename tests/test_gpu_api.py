@@ -226,3 +226,28 @@ def test_gpu_setup_equals_host_setup(lib_built, monkeypatch):
     with sgh.SGHSolver(prob) as s:
         s.set_state(sgh.setup(prob))
         assert s.run(10) == 10
+
+
+def test_device_view_is_zero_copy_torch(lib_built):
+    """fierro_sgh_device_view through DLPack: torch tensors over the handle's own
+    memory, equal (through the renumbering maps) to get_state."""
+    torch = pytest.importorskip("torch")
+    from fierro_gb300 import sgh
+    prob = _prob()
+    st = sgh.setup(prob)
+    with sgh.SGHSolver(prob) as s:
+        s.set_state(st)
+        s.run(5)
+        host = s.get_state()
+        v = s.device_view()
+        n2e = v["node_int2ext"].long().cpu().numpy()
+        e2e = v["elem_int2ext"].long().cpu().numpy()
+        assert np.array_equal(v["x"].cpu().numpy(), host["node_coords"][1][n2e, 0])
+        assert np.array_equal(v["w"].cpu().numpy(), host["node_vel"][1][n2e, 2])
+        assert np.array_equal(v["sie"].cpu().numpy(), host["elem_sie"][1][e2e])
+        assert np.array_equal(v["den"].cpu().numpy(), host["elem_den"][e2e])
+        cf = v["corner_force"].cpu().numpy()  # [lid*3+dim][e]
+        assert np.array_equal(cf.T.reshape(-1, 8, 3), host["corner_force"].reshape(-1, 8, 3)[e2e])
+        assert np.array_equal(v["node_ext2int"].long().cpu().numpy()[n2e], np.arange(prob.mesh.num_nodes))
+        # zero copy: a second view aliases the same memory
+        assert s.device_view()["den"].data_ptr() == v["den"].data_ptr()
