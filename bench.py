@@ -48,6 +48,8 @@ def parse(argv=None):
                     help="run the batched-ensemble benchmark instead (instances/s vs looping the plain solver)")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--batch-cycles", type=int, default=100)
+    ap.add_argument("--outputs", action="store_true",
+                    help="graphics dumps: cycle time with the writer thread on vs off")
     ap.add_argument("--adjoint", action="store_true",
                     help="discrete adjoint: Sedov 64^3, 400 cycles, J = sum M (rho - rho_target)^2")
     ap.add_argument("--adj-n", type=int, default=64)
@@ -521,8 +523,59 @@ def adjoint_bench(args):
     print(json.dumps(line))
 
 
+def outputs_bench(args):
+    """Graphics dumps (EnSight Gold + element state text, the reference's formats)
+    every 25 cycles of 200 on jittered Sedov 64^3 with a 16-slot snapshot ring:
+    wall time of fierro_sgh_run with the writer thread on against off (the cycle
+    loop's cost of dumping), the time the writer needed after the last cycle
+    (flush), and the writer's text throughput.  The dumps go to a temporary
+    directory."""
+    import shutil
+    import tempfile
+    import torch
+    from fierro_gb300 import problems, sgh
+    torch.cuda.set_device(0)
+    n, cyc = 64, 200
+    p = problems.sedov(n, jitter=0.1, seed=7, cycles=cyc)
+    p.params.graphics_cyc_ival = 25
+    st = sgh.setup(p)
+    res = {}
+    with sgh.SGHSolver(p) as s:
+        s.set_state(st)
+        s.run(5)
+        for mode in ("off", "on", "off"):
+            d = tempfile.mkdtemp(prefix="fierro_out_")
+            s.set_output(d if mode == "on" else None, slots=16)
+            s.set_state(st)
+            s.synchronize()
+            t0 = time.perf_counter()
+            s.run(cyc)
+            s.synchronize()
+            t1 = time.perf_counter()
+            dumps = s.flush_output()
+            t2 = time.perf_counter()
+            size = sum(os.path.getsize(os.path.join(a, f)) for a, _, fs in os.walk(d) for f in fs)
+            res.setdefault(mode, []).append({"run_s": t1 - t0, "flush_s": t2 - t1, "dumps": dumps, "bytes": size})
+            s.set_output(None)
+            shutil.rmtree(d, ignore_errors=True)
+    off = min(r["run_s"] for r in res["off"])
+    on = res["on"][0]
+    line = {"metric": "cycle-loop wall time with graphics dumps on / off (Sedov 64^3, 200 cycles, dump every 25)",
+            "value": on["run_s"] / off, "unit": "x", "higher_is_better": False, "dtype": "f64", "data": "synthetic",
+            "run_off_s": off, "run_on_s": on["run_s"], "writer_tail_s": on["flush_s"], "dumps": on["dumps"],
+            "bytes_written": on["bytes"], "writer_bytes_per_s": on["bytes"] / (on["run_s"] + on["flush_s"]),
+            "slots": 16,
+            "config": {"workload": "sedov64 jitter0.1 seed7", "cycles": cyc, "graphics_cyc_ival": 25,
+                       "formats": "EnSight Gold (case, geo, 9 scalars, 2 vectors) + element state text",
+                       "timing": "host wall clock around fierro_sgh_run (synchronised)"}}
+    print(json.dumps(line))
+
+
 def main(argv=None):
     args = parse(argv)
+    if args.outputs:
+        outputs_bench(args)
+        return
     if args.adjoint:
         adjoint_bench(args)
         return
