@@ -56,6 +56,10 @@ def parse(argv=None):
     ap.add_argument("--adj-cycles", type=int, default=400)
     ap.add_argument("--adj-ckpt", type=int, default=20)
     ap.add_argument("--adj-dirs", type=int, default=16)
+    ap.add_argument("--strength", default=None, choices=["hypo", "hyper"],
+                    help="strength-model run: the workload with the shipped hypo-elastic model as a hypo or "
+                         "hyper model on every element, against the same problem without strength")
+    ap.add_argument("--shear-modulus", type=float, default=1.0)
     return ap.parse_args(argv)
 
 
@@ -185,16 +189,20 @@ def measure_peaks():
 
 
 # ------------------------------------------------------------------ CPU reference
-def run_reference_sample(args, n: int, cycles: int, warmup: int) -> dict:
+def run_reference_sample(args, n: int, cycles: int, warmup: int, strength: str | None = None) -> dict:
     """The reference's own SGH solver (compiled from its sources against the
     MATAR/Kokkos stand-in, OpenMP on every host core) on a bounded sample of the
-    workload: the same jittered, permuted Sedov problem on an n^3 mesh."""
+    workload: the same jittered, permuted Sedov problem on an n^3 mesh (with the
+    test strength model on every material when `strength` is given)."""
     from oracle import build_ref, orc
     if not orc.reference_available("fierro_ref_fast"):
         build_ref.build_reference()
     if not orc.reference_available("fierro_ref_fast"):
         raise RuntimeError("reference executable unavailable (no reference sources on this machine)")
     prob = workload(n, args.seed)
+    if strength:
+        from fierro_gb300 import problems
+        problems.with_strength(prob, strength, args.shear_modulus)
     cores = os.cpu_count() or 1
     st = orc.run_reference(prob, cycles=cycles, kind="fierro_ref_fast", threads=cores, warmup=warmup)
     secs = st["calc_seconds"]
@@ -571,8 +579,102 @@ def outputs_bench(args):
     print(json.dumps(line))
 
 
+def strength_alg_bytes(kind: str, kernel: str, nn: int, ne: int, nnz: int) -> float:
+    """Compulsory bytes of one launch (mean over the two RK stages) of a kernel of
+    a strength run with every element on the model: the plain kernel's bytes plus
+    the stress rows (9 doubles per bin), the cycle-start energy and the shear
+    modulus column the model reads.  Hypo: the force pass reads stress(1) and
+    stress(0) and writes stress(1) on both stages.  Hyper: the force pass reads
+    stress(1) and copies it on the first stage; the element pass reads both bins
+    and writes stress(1)."""
+    base = alg_bytes(kernel, nn, ne, nnz)
+    if kind == "hypo" and kernel == "k_force":
+        return base + ne * (72 + 72 + 72 + 8 + 8)
+    if kind == "hyper" and kernel == "k_force":
+        return base + ne * (72 + 36)
+    if kind == "hyper" and kernel == "k_elem":
+        return base + ne * (72 + 72 + 72 + 8 + 8)
+    return base
+
+
+def strength_bench(args):
+    """The strength-model path at scale: the benchmark workload with every
+    material on the shipped hypo-elastic model (as a hypo or hyper model), timed
+    with per-launch CUDA events like the plain run, against the same problem
+    without strength in the same process, plus the reference CPU solver running
+    the same model on a bounded sample."""
+    import numpy as np
+    import torch
+    from fierro_gb300 import problems, sgh
+    torch.cuda.set_device(0)
+    mode = sgh.FP_EXACT if args.fp_mode == "exact" else sgh.FP_FMA
+    res = {}
+    for kind in ("none", args.strength):
+        prob = workload(args.n, args.seed)
+        if kind != "none":
+            problems.with_strength(prob, kind, args.shear_modulus)
+        st = sgh.setup(prob)
+        nn, ne = prob.mesh.num_nodes, prob.mesh.num_elems
+        with sgh.SGHSolver(prob, fp_mode=mode) as s:
+            s.set_state(st)
+            s.run(args.warmup)
+            clocks = ClockSampler(0)
+            clocks.start()
+            ran, total_ms, kms = s.run_timed(args.steps)
+            ck = clocks.stop()
+            if ran != args.steps:
+                raise RuntimeError("only %d of %d cycles ran" % (ran, args.steps))
+            names = s.launch_names()
+            per = {}
+            for nm, ms in zip(names, kms):
+                per[nm] = per.get(nm, 0.0) + ms
+            out = s.get_state() if kind != "none" else None
+            res[kind] = {"value": ne * args.steps / (total_ms * 1e-3), "ms_per_step": total_ms / args.steps,
+                         "kernels_ms_per_launch": {k: per[k] / (names.count(k) * args.steps) for k in per},
+                         "clocks": ck, "device_bytes": s.device_bytes,
+                         "launches": int(s.launches_per_cycle * args.steps)}
+            if out is not None:
+                res[kind]["max_abs_stress"] = float(np.abs(out["elem_stress"][1]).max())
+                res[kind]["finite"] = bool(np.isfinite(out["node_coords"]).all())
+        nnz = int(solver_neighbor_count(prob))
+    r, plain = res[args.strength], res["none"]
+    per = r["kernels_ms_per_launch"]
+    dom = max(("k_force", "k_node", "k_elem"), key=lambda k: per[k])
+    ab = strength_alg_bytes(args.strength, dom, nn, ne, nnz)
+    hbm_peak, peak_kind = measure_peaks()
+    achieved = ab / (per[dom] * 1e-3) / 1e9
+    cpu = None
+    if not args.no_cpu_baseline:
+        try:
+            cpu = run_reference_sample(args, args.cpu_n, args.cpu_cycles, 1, strength=args.strength)
+        except Exception as exc:
+            cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "reference",
+                   "sample": "unavailable: " + str(exc).splitlines()[0]}
+    line = {"metric": "SGH element-cycles/s with the %s strength model, %d^3 perturbed Sedov, FP64 RK2"
+                      % (args.strength, args.n),
+            "value": r["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": dict(config_of(args), fp_mode=args.fp_mode, strength=args.strength,
+                           shear_modulus=args.shear_modulus, model="linear hypo-elastic (sgh_user_mat.cuh)"),
+            "gpu_launches": r["launches"],
+            "plain_value": plain["value"], "strength_over_plain_time": plain["value"] / r["value"],
+            "kernels_ms_per_launch": {"strength": per, "plain": plain["kernels_ms_per_launch"]},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": None, "peak_kind": peak_kind,
+                         "alg_bytes_per_launch": ab, "avg_launch_ms": per[dom]},
+            "max_abs_stress": r["max_abs_stress"], "finite": r["finite"],
+            "cpu_baseline": None if cpu is None else {k: cpu[k] for k in ("value", "unit", "cores", "kind",
+                                                                         "sample")},
+            "clocks": r["clocks"], "device_bytes": r["device_bytes"]}
+    print(json.dumps(line))
+
+
 def main(argv=None):
     args = parse(argv)
+    if args.strength:
+        strength_bench(args)
+        return
     if args.outputs:
         outputs_bench(args)
         return

@@ -13,6 +13,7 @@
 
 #include "sgh_handle.h"
 #include "sgh_topo.h"
+#include "sgh_user_mat.cuh"
 
 using namespace fierro;
 
@@ -148,6 +149,35 @@ ElemArgs elem_args(fierro_sgh* h, int cur_bin, int c, double alpha, int div_out)
   return a;
 }
 
+ForceArgs stage_force_args(fierro_sgh* h, int c, int s) {
+  const int rb = (s == 0) ? c : (c ^ 1);
+  ForceArgs a = force_args(h, rb, div_parity(h, c, s));
+  if (h->strength) {
+    // stress(1) is the cycle-start bin until the first stage writes bin c^1
+    a.stress_cur = h->d_stress[rb];
+    a.stress0 = h->d_stress[c];
+    a.stress_out = h->d_stress[c ^ 1];
+    a.stype = h->d_stype;
+    a.statev = h->d_statev;
+    a.sie0 = h->d_sie[c];
+    a.rk_alpha = stage_alpha(h, s);
+    a.copy_stress = s == 0;
+  }
+  return a;
+}
+
+ElemArgs stage_elem_args(fierro_sgh* h, int c, int s) {
+  ElemArgs a = elem_args(h, c ^ 1, c, stage_alpha(h, s), div_parity(h, c, s) ^ 1);
+  if (h->has_hyper) {
+    a.mat = h->d_mat;
+    a.stype = h->d_stype;
+    a.stress0 = h->d_stress[c];
+    a.stress1 = h->d_stress[c ^ 1];
+    a.statev = h->d_statev;
+  }
+  return a;
+}
+
 int cycles_done(fierro_sgh* h, long long* cyc) {
   Ctrl c;
   CUDA_TRY(cudaMemcpyAsync(&c, h->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
@@ -165,12 +195,9 @@ namespace {
 
 // Stage s of a cycle whose start state is in bin c.
 void enqueue_stage(fierro_sgh* h, int c, int s) {
-  const double alpha = stage_alpha(h, s);
-  const int rb = (s == 0) ? c : (c ^ 1);
-  const int q = div_parity(h, c, s);
-  h->ks->force(force_args(h, rb, q), h->stream);
-  h->ks->node(node_args(h, c, alpha), h->stream);
-  h->ks->elem(elem_args(h, c ^ 1, c, alpha, q ^ 1), (s == h->rk_num_stages - 1) ? 1 : 0, h->stream);
+  h->ks->force(stage_force_args(h, c, s), h->stream);
+  h->ks->node(node_args(h, c, stage_alpha(h, s)), h->stream);
+  h->ks->elem(stage_elem_args(h, c, s), (s == h->rk_num_stages - 1) ? 1 : 0, h->stream);
 }
 
 void enqueue_dt(fierro_sgh* h) {
@@ -236,6 +263,7 @@ extern "C" int fierro_sgh_destroy(fierro_sgh* h) {
   for (int c = 0; c < 2; ++c)
     if (h->graph[c]) cudaGraphExecDestroy(h->graph[c]);
   for (void* p : h->allocations) cudaFree(p);
+  if (h->d_statev) cudaFree(h->d_statev);
   for (int i = 0; i < 2; ++i) {
     if (h->h_stage[i]) cudaFreeHost(h->h_stage[i]);
     if (h->stage_ev[i]) cudaEventDestroy(h->stage_ev[i]);
@@ -254,8 +282,11 @@ static int create_impl(fierro_sgh* h, const fierro_mesh* mesh, const fierro_mate
   if (num_materials < 1 || !materials) return set_error(FIERRO_EINVAL, "need at least one material");
   for (int64_t m = 0; m < num_materials; ++m) {
     if (materials[m].eos_model != 0) return set_error(FIERRO_ENOTSUP, "material %lld: only the ideal-gas EOS", (long long)m);
-    if (materials[m].strength_type != 0)
-      return set_error(FIERRO_ENOTSUP, "material %lld: strength models are outside this path", (long long)m);
+    if (materials[m].strength_type < 0 || materials[m].strength_type > 2)
+      return set_error(FIERRO_EINVAL, "material %lld: strength_type %d unknown (0 none, 1 hypo, 2 hyper)",
+                       (long long)m, materials[m].strength_type);
+    if (materials[m].strength_type != 0) h->strength = true;
+    if (materials[m].strength_type == 2) h->has_hyper = true;
   }
   int dev = 0;
   CUDA_TRY(cudaGetDevice(&dev));
@@ -313,6 +344,14 @@ static int create_impl(fierro_sgh* h, const fierro_mesh* mesh, const fierro_mate
   TRY(dalloc(h, &h->d_sie[1], ne));
   TRY(dalloc(h, &h->d_bmat, ne * 24));
   TRY(dalloc(h, &h->d_force, ne * 24));
+  if (h->strength) {
+    TRY(dalloc(h, &h->d_stress[0], ne * 9));
+    TRY(dalloc(h, &h->d_stress[1], ne * 9));
+    TRY(dalloc(h, &h->d_stype, (size_t)num_materials));
+    std::vector<int> st((size_t)num_materials);
+    for (int64_t m = 0; m < num_materials; ++m) st[m] = materials[m].strength_type;
+    TRY(upload_raw(h, h->d_stype, st.data(), sizeof(int) * st.size()));
+  }
   h->ncfl = (int)((ne + kElemBlock - 1) / kElemBlock);
   TRY(dalloc(h, &h->d_cfl, (size_t)h->ncfl));
   TRY(dalloc(h, &h->d_ctrl, 1));
@@ -402,14 +441,42 @@ static int finish_set_state(fierro_sgh* h, double time_value, double graphics_ti
   return FIERRO_OK;
 }
 
+// The device copy of the element state variables of a strength handle, sized
+// for nsv columns; the cycle graphs hold its address, so a new allocation
+// re-captures them.
+static int size_statev(fierro_sgh* h, int64_t nsv) {
+  if (!h->strength || (h->d_statev && h->nsv == nsv)) return FIERRO_OK;
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (h->d_statev) {
+    cudaFree(h->d_statev);
+    h->dev_bytes -= sizeof(double) * (size_t)(h->nsv * h->ne);
+    h->d_statev = nullptr;
+  }
+  const size_t bytes = sizeof(double) * (size_t)(nsv * h->ne);
+  cudaError_t err = cudaMalloc(&h->d_statev, bytes);
+  if (err != cudaSuccess) {
+    h->d_statev = nullptr;
+    h->nsv = 0;
+    return set_error(FIERRO_ENOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(err));
+  }
+  h->dev_bytes += bytes;
+  h->nsv = nsv;
+  return build_graphs(h);
+}
+
 static int set_state_impl(fierro_sgh* h, const fierro_sgh_state* s, double time_value, double graphics_time,
                           double dt) {
   if (!s || !s->node_coords || !s->node_vel || !s->node_mass || !s->elem_den || !s->elem_pres || !s->elem_sspd ||
       !s->elem_sie || !s->elem_vol || !s->elem_mass || !s->elem_mat_id || !s->elem_statev)
     return set_error(FIERRO_EINVAL, "set_state: required state arrays missing");
   if (s->num_state_vars < 2) return set_error(FIERRO_EINVAL, "set_state: need num_state_vars >= 2");
+  if (h->strength && s->num_state_vars < kUserStrengthStateVars)
+    return set_error(FIERRO_EINVAL, "set_state: the strength model reads %d state variables, the state has %lld",
+                     kUserStrengthStateVars, (long long)s->num_state_vars);
   const int64_t nn = h->nn, ne = h->ne, nsv = s->num_state_vars;
   const HostTopo& t = h->topo;
+  h->has_state = false;
+  TRY(size_statev(h, nsv));
   if (h->direct_host) {
     // the GPU reads the caller's arrays and validates them in the same pass
     h->has_state = false;
@@ -418,8 +485,8 @@ static int set_state_impl(fierro_sgh* h, const fierro_sgh_state* s, double time_
     XferStatus xs{};
     TRY(xfer::upload_state(h, s, &xs));
     if (xs.flags & (1u << XferStatus::STRESS))
-      return set_error(FIERRO_ENOTSUP, "set_state: non-zero stress (value %lld) needs a strength model (outside "
-                       "this path)", xs.first[XferStatus::STRESS]);
+      return set_error(FIERRO_ENOTSUP, "set_state: non-zero stress (value %lld) needs a handle with a strength "
+                       "material", xs.first[XferStatus::STRESS]);
     if (xs.flags & (1u << XferStatus::MAT_ID))
       return set_error(FIERRO_EINVAL, "set_state: element %lld material id out of range", xs.first[XferStatus::MAT_ID]);
     if (xs.flags & (1u << XferStatus::VOLUME))
@@ -431,10 +498,10 @@ static int set_state_impl(fierro_sgh* h, const fierro_sgh_state* s, double time_
       return set_error(FIERRO_EINVAL, "set_state: node %lld mass <= 0", xs.first[XferStatus::NODE_MASS]);
     return finish_set_state(h, time_value, graphics_time, dt);
   }
-  if (s->elem_stress)
+  if (s->elem_stress && !h->strength)
     for (int64_t i = 0; i < ne * 18; ++i)
       if (s->elem_stress[i] != 0.0)
-        return set_error(FIERRO_ENOTSUP, "set_state: non-zero stress needs a strength model (outside this path)");
+        return set_error(FIERRO_ENOTSUP, "set_state: non-zero stress needs a handle with a strength material");
   for (int64_t e = 0; e < ne; ++e) {
     if (s->elem_mat_id[e] >= (uint64_t)h->nmat)
       return set_error(FIERRO_EINVAL, "set_state: element %lld material id out of range", (long long)e);
@@ -464,6 +531,20 @@ static int set_state_impl(fierro_sgh* h, const fierro_sgh_state* s, double time_
   TRY(upload_gather(h, h->d_elem_mass, s->elem_mass, t.elem_int2ext, 1, 0, &slot));
   TRY(upload_gather(h, h->d_gamma, s->elem_statev, t.elem_int2ext, (size_t)nsv, 0, &slot));
   TRY(upload_gather(h, h->d_csmin, s->elem_statev, t.elem_int2ext, (size_t)nsv, 1, &slot));
+  if (h->strength) {
+    for (int64_t k = 0; k < nsv; ++k)
+      TRY(upload_gather(h, h->d_statev + (size_t)(k * ne), s->elem_statev, t.elem_int2ext, (size_t)nsv, (size_t)k,
+                        &slot));
+    // reference bin rb -> device bin rb ^ 1, component i*3+j -> row i*3+j
+    for (int rb = 0; rb < 2; ++rb)
+      for (int k = 0; k < 9; ++k) {
+        double* dst = h->d_stress[rb ^ 1] + (size_t)(k * ne);
+        if (s->elem_stress)
+          TRY(upload_gather(h, dst, s->elem_stress + (size_t)(rb * ne * 9), t.elem_int2ext, 9, (size_t)k, &slot));
+        else
+          CUDA_TRY(cudaMemsetAsync(dst, 0, sizeof(double) * (size_t)ne, h->stream));
+      }
+  }
   std::vector<int32_t> mat((size_t)ne);
   for (int64_t e = 0; e < ne; ++e) mat[e] = (int32_t)s->elem_mat_id[t.elem_int2ext[e]];
   TRY(upload_raw(h, h->d_mat, mat.data(), sizeof(int32_t) * (size_t)ne));
@@ -494,6 +575,9 @@ extern "C" int fierro_sgh_get_state(fierro_sgh* h, fierro_sgh_state* s) {
   clear_error();
   if (!h || !s) return set_error(FIERRO_EINVAL, "handle or state is NULL");
   if (!h->has_state) return set_error(FIERRO_EINVAL, "get_state before set_state");
+  if (h->strength && s->elem_statev && s->num_state_vars != h->nsv)
+    return set_error(FIERRO_EINVAL, "get_state: num_state_vars %lld, the handle holds %lld",
+                     (long long)s->num_state_vars, (long long)h->nsv);
   long long cyc = 0;
   TRY(cycles_done(h, &cyc));
   const int c = bin_now(h, cyc);  // cycle-start bin of the current (or next) cycle
@@ -518,6 +602,7 @@ extern "C" int fierro_sgh_get_state(fierro_sgh* h, fierro_sgh_state* s) {
     for (double* p : e1) populate(p, nb * ne);
     populate(s->elem_stress, nb * ne * 18);
     populate(s->corner_force, nb * ne * 24);
+    if (h->strength) populate(s->elem_statev, nb * ne * (size_t)h->nsv);
     return xfer::download_state(h, s, bins, qb);
   }
   for (int rb = 0; rb < 2; ++rb)
@@ -537,7 +622,18 @@ extern "C" int fierro_sgh_get_state(fierro_sgh* h, fierro_sgh_state* s) {
   if (s->elem_vol) TRY(download_scatter(h, s->elem_vol, h->d_vol, t.elem_int2ext, 1, 0));
   if (s->elem_div) TRY(download_scatter(h, s->elem_div, h->d_div[qb], t.elem_int2ext, 1, 0));
   if (s->elem_mass) TRY(download_scatter(h, s->elem_mass, h->d_elem_mass, t.elem_int2ext, 1, 0));
-  if (s->elem_stress) std::memset(s->elem_stress, 0, sizeof(double) * (size_t)ne * 18);
+  if (s->elem_stress && h->strength) {
+    for (int rb = 0; rb < 2; ++rb)
+      for (int k = 0; k < 9; ++k)
+        TRY(download_scatter(h, s->elem_stress + (size_t)(rb * ne * 9), h->d_stress[bins[rb]] + (size_t)(k * ne),
+                             t.elem_int2ext, 9, (size_t)k));
+  } else if (s->elem_stress) {
+    std::memset(s->elem_stress, 0, sizeof(double) * (size_t)ne * 18);
+  }
+  if (s->elem_statev && h->strength)
+    for (int64_t k = 0; k < h->nsv; ++k)
+      TRY(download_scatter(h, s->elem_statev, h->d_statev + (size_t)(k * ne), t.elem_int2ext, (size_t)h->nsv,
+                           (size_t)k));
   if (s->corner_force) {
     // device [lid*3+dim][e] -> reference [(E*8+lid)*3+dim]
     for (int r = 0; r < 24; ++r)
@@ -628,14 +724,11 @@ extern "C" int fierro_sgh_run_timed(fierro_sgh* h, int64_t cycles, float* kernel
     enqueue_dt(h);
     CUDA_TRY(cudaEventRecord(ev[k++], h->stream));
     for (int s = 0; s < h->rk_num_stages; ++s) {
-      const double alpha = stage_alpha(h, s);
-      const int rb = (s == 0) ? c : (c ^ 1);
-      const int q = div_parity(h, c, s);
-      h->ks->force(force_args(h, rb, q), h->stream);
+      h->ks->force(stage_force_args(h, c, s), h->stream);
       CUDA_TRY(cudaEventRecord(ev[k++], h->stream));
-      h->ks->node(node_args(h, c, alpha), h->stream);
+      h->ks->node(node_args(h, c, stage_alpha(h, s)), h->stream);
       CUDA_TRY(cudaEventRecord(ev[k++], h->stream));
-      h->ks->elem(elem_args(h, c ^ 1, c, alpha, q ^ 1), (s == h->rk_num_stages - 1) ? 1 : 0, h->stream);
+      h->ks->elem(stage_elem_args(h, c, s), (s == h->rk_num_stages - 1) ? 1 : 0, h->stream);
       CUDA_TRY(cudaEventRecord(ev[k++], h->stream));
     }
     h->ks->end(h->d_ctrl, h->lp, h->stream);

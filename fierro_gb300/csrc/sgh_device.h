@@ -10,6 +10,8 @@
 //            geometry (row lid*3+dim), written by the element kernel and read by
 //            the next stage's force kernel
 //   force    [24][ne]  corner forces, row lid*3+dim
+//   stress   two bins of [9][ne] (row i*3+j) and statev [nsv][ne], only on a
+//            handle with a strength material
 //   div      two buffers: the force pass of a stage reads one, the element pass
 //            writes the next stage's into the other (so the reference-visible
 //            elem_div, the one the last stage used, survives)
@@ -63,6 +65,17 @@ struct ForceArgs {
   // each element, rows of kForceTapeRows x ne, and the limiter's neighbour
   double* tape;
   int* tape_sel;
+  // strength materials (set when the handle has one; stress rows [9][ne],
+  // row i*3+j): the reference's stress(1) as this stage's force reads it, the
+  // cycle-start stress(0), and where the stage's stress(1) goes
+  const double* stress_cur;
+  const double* stress0;
+  double* stress_out;
+  const int* stype;    // [nmat] strength_type: 0 none, 1 hypo, 2 hyper
+  double* statev;      // [nsv][ne] element state variables
+  const double* sie0;  // cycle-start energy (the reference passes elem_sie bin 0)
+  double rk_alpha;
+  int copy_stress;     // stage 0: elements without a hypo model carry stress_cur over
 };
 
 // Rows of the force kernel's tape: mu[8], |v_l - v_avg|[8], v*[3], sum mu,
@@ -105,6 +118,12 @@ struct ElemArgs {
   const int* inst;            // batch only: instance of each element (negative = padding)
   const double* dt_cfl_tab;   // batch only: CFL number per instance
   double rk_alpha, dt_cfl, fuzz;
+  // hyper strength materials (set when the handle has one): stress rows [9][ne]
+  const int* mat;
+  const int* stype;
+  const double* stress0;  // cycle-start stress(0)
+  double* stress1;        // stress(1), updated in place
+  double* statev;         // [nsv][ne]
 };
 
 struct DtArgs {

@@ -84,6 +84,14 @@ struct fierro_sgh {
   fierro::XferStatus* d_xfer = nullptr;
   int64_t nnz_eie = 0;  // neighbour-list entries
   fierro::OutputState* out = nullptr;  // graphics dumps (sgh_output.cpp)
+  // strength materials (sgh_user_mat.cuh): two stress bins [9][ne] and the
+  // element state variables [nsv][ne] (sized by set_state, owned separately)
+  bool strength = false;   // some material has strength_type 1 or 2
+  bool has_hyper = false;  // some material has strength_type 2
+  int* d_stype = nullptr;
+  double* d_stress[2] = {};
+  double* d_statev = nullptr;
+  int64_t nsv = 0;
 };
 
 namespace fierro {
@@ -114,6 +122,10 @@ int cycles_done(fierro_sgh* h, long long* cyc);
 ForceArgs force_args(fierro_sgh* h, int rb, int q);
 NodeArgs node_args(fierro_sgh* h, int c, double alpha);
 ElemArgs elem_args(fierro_sgh* h, int cur_bin, int c, double alpha, int div_out);
+// The force and element records of RK stage s of a cycle whose start state is in
+// bin c, with the stress bins of a strength handle.
+ForceArgs stage_force_args(fierro_sgh* h, int c, int s);
+ElemArgs stage_elem_args(fierro_sgh* h, int c, int s);
 
 // Bins at a cycle boundary after `done` executed cycles: state bin and start bin.
 inline int bin_now(const fierro_sgh* h, long long cycles_done) { return (int)((h->base + cycles_done) & 1); }

@@ -351,8 +351,9 @@ extern "C" int fierro_sgh_setup(const fierro_mesh* mesh, const fierro_material* 
                      (long long)out->num_state_vars, (long long)num_state_vars);
   for (int64_t m = 0; m < num_materials; ++m) {
     if (materials[m].eos_model != 0) return set_error(FIERRO_ENOTSUP, "material %lld: only the ideal-gas EOS", (long long)m);
-    if (materials[m].strength_type != 0)
-      return set_error(FIERRO_ENOTSUP, "material %lld: strength models are outside this path", (long long)m);
+    if (materials[m].strength_type < 0 || materials[m].strength_type > 2)
+      return set_error(FIERRO_EINVAL, "material %lld: strength_type %d unknown (0 none, 1 hypo, 2 hyper)",
+                       (long long)m, materials[m].strength_type);
   }
   for (int64_t f = 0; f < num_fills; ++f) {
     if (fills[f].mat_id < 0 || fills[f].mat_id >= num_materials)

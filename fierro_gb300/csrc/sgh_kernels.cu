@@ -49,16 +49,41 @@ namespace FIERRO_IMPL {
 #include "sgh_common.cuh"
 #include "sgh_hex_geometry.cuh"
 #include "sgh_cfl.cuh"
+#include "sgh_user_mat.cuh"
+
+// Velocity gradient (momentum.cpp:59-144): L(i,j) = (sum_l v_i(l) B(l,j)) / vol,
+// B the outward corner normals in rows [lid*3+dim][ne], summed over l in order.
+__device__ __forceinline__ void velocity_gradient(const double (&u)[8], const double (&v)[8], const double (&w)[8],
+                                                  const double* bmat, int ne, int e, double vol, double (&L)[9]) {
+  const double inverse_vol = 1.0 / vol;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    double b = bmat[(size_t)j * ne + e];
+    double su = u[0] * b, sv = v[0] * b, sw = w[0] * b;
+#pragma unroll
+    for (int l = 1; l < 8; ++l) {
+      b = bmat[(size_t)(l * 3 + j) * ne + e];
+      su = su + u[l] * b;
+      sv = sv + v[l] * b;
+      sw = sw + w[l] * b;
+    }
+    L[j] = su * inverse_vol;
+    L[3 + j] = sv * inverse_vol;
+    L[6 + j] = sw * inverse_vol;
+  }
+}
 
 // ---------------------------------------------------------------------------
-// Corner forces (force_sgh.cpp:35-394, 3D, strength none).  The reference's
-// shock-direction, velocity-gradient and curl terms only feed unused values
-// (use_shock_dir = 0 at :227, phi_curl unused at :331) and are not computed.
-// Stress is zero for strength-free materials, so tau = -p I and the force's
-// stress term a_k tau(k,d) reduces exactly to B(d) p (two negations).
+// Corner forces (force_sgh.cpp:35-394, 3D).  The reference's shock-direction
+// and curl terms only feed unused values (use_shock_dir = 0 at :227, phi_curl
+// unused at :331) and are not computed.  Without strength materials stress is
+// zero, so tau = -p I and the force's stress term a_k tau(k,d) reduces exactly
+// to B(d) p (two negations).  STRENGTH (a handle with a strength material)
+// forms tau = stress(1) - p I and the force as the reference writes it, then
+// runs the hypo model (:366-391) with the velocity gradient of this state.
 // TAPE (the adjoint's replay, exact mode) also stores the viscosity
 // intermediates; the stores do not change any value the kernel computes.
-template <bool BATCH, bool TAPE>
+template <bool BATCH, bool TAPE, bool STRENGTH>
 __global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
   if (!BATCH && !a.ctrl->active) return;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -186,16 +211,57 @@ __global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
     a.tape_sel[e] = sel;
   }
   phi = alpha * phi;
-  // corner forces (:338-359)
+  if (!STRENGTH) {
+    // corner forces (:338-359)
 #pragma unroll
-  for (int l = 0; l < 8; ++l) {
-    const double pm = phi * mu[l];
-    const double b0 = a.bmat[(size_t)(l * 3 + 0) * ne + e];
-    const double b1 = a.bmat[(size_t)(l * 3 + 1) * ne + e];
-    const double b2 = a.bmat[(size_t)(l * 3 + 2) * ne + e];
-    a.force[(size_t)(l * 3 + 0) * ne + e] = b0 * pres + pm * (vstar0 - vu[l]);
-    a.force[(size_t)(l * 3 + 1) * ne + e] = b1 * pres + pm * (vstar1 - vv[l]);
-    a.force[(size_t)(l * 3 + 2) * ne + e] = b2 * pres + pm * (vstar2 - vw[l]);
+    for (int l = 0; l < 8; ++l) {
+      const double pm = phi * mu[l];
+      const double b0 = a.bmat[(size_t)(l * 3 + 0) * ne + e];
+      const double b1 = a.bmat[(size_t)(l * 3 + 1) * ne + e];
+      const double b2 = a.bmat[(size_t)(l * 3 + 2) * ne + e];
+      a.force[(size_t)(l * 3 + 0) * ne + e] = b0 * pres + pm * (vstar0 - vu[l]);
+      a.force[(size_t)(l * 3 + 1) * ne + e] = b1 * pres + pm * (vstar1 - vv[l]);
+      a.force[(size_t)(l * 3 + 2) * ne + e] = b2 * pres + pm * (vstar2 - vw[l]);
+    }
+  } else {
+    // Cauchy stress tau = stress(1) - p I (:128-140), then the corner forces with
+    // the inward normals -B (:98-102, :338-359)
+    double sc[9], tau[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      sc[k] = a.stress_cur[(size_t)k * ne + e];
+      tau[k] = sc[k];
+    }
+    tau[0] -= pres;
+    tau[4] -= pres;
+    tau[8] -= pres;
+    const double vs[3] = {vstar0, vstar1, vstar2};
+#pragma unroll
+    for (int l = 0; l < 8; ++l) {
+      const double pm = phi * mu[l];
+      const double a0 = -a.bmat[(size_t)(l * 3 + 0) * ne + e];
+      const double a1 = -a.bmat[(size_t)(l * 3 + 1) * ne + e];
+      const double a2 = -a.bmat[(size_t)(l * 3 + 2) * ne + e];
+      const double vl[3] = {vu[l], vv[l], vw[l]};
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        a.force[(size_t)(l * 3 + d) * ne + e] =
+            a0 * tau[d] + a1 * tau[3 + d] + a2 * tau[6 + d] + pm * (vs[d] - vl[d]);
+    }
+    // stress update of hypo materials (:362-391); the others carry stress(1) over
+    // from the cycle-start bin on the first stage (rk_init's copy)
+    if (a.stype[mat] == 1) {
+      double L[9], s0[9];
+      velocity_gradient(vu, vv, vw, a.bmat, ne, e, vol, L);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) s0[k] = a.stress0[(size_t)k * ne + e];
+      user_strength_model(sc, s0, L, a.statev + e, ne, mat, den, a.sie0[e], vol, a.ctrl->dt, a.rk_alpha);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) a.stress_out[(size_t)k * ne + e] = sc[k];
+    } else if (a.copy_stress) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) a.stress_out[(size_t)k * ne + e] = sc[k];
+    }
   }
 }
 
@@ -251,10 +317,13 @@ __global__ void __launch_bounds__(kNodeBlock) k_node(const NodeArgs a) {
 // ---------------------------------------------------------------------------
 // Element update.  KIND 0: stage; 1: last stage (adds the CFL partials);
 // 2: prime (corner normals, divergence and CFL of an uploaded state).
+// STRENGTH (a handle with a hyper material) runs the hyper model between the
+// density and the EOS (properties.cpp:46-95) with the velocity gradient of the
+// updated state.
 // In a batch every block lies inside one instance (instances' element ranges are
 // padded to whole blocks, padding marked by a negative instance id), so the
 // activity test and the CFL partial are per block.
-template <int KIND, bool BATCH>
+template <int KIND, bool BATCH, bool STRENGTH>
 __global__ void __launch_bounds__(kElemBlock) k_elem(const ElemArgs a) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   const int ib = BATCH ? a.inst[blockIdx.x * kElemBlock] : 0;
@@ -308,6 +377,21 @@ __global__ void __launch_bounds__(kElemBlock) k_elem(const ElemArgs a) {
       a.vol[e] = vol;
       // update_state (properties.cpp:39, eos.cpp:85-98)
       const double den = a.mass[e] / vol;
+      if (STRENGTH) {
+        const int mat = a.mat[e];
+        if (a.stype[mat] == 2) {
+          double L[9], s0[9], s1[9];
+          velocity_gradient(u, v, w, a.bmat, ne, e, vol, L);
+#pragma unroll
+          for (int k = 0; k < 9; ++k) {
+            s0[k] = a.stress0[(size_t)k * ne + e];
+            s1[k] = a.stress1[(size_t)k * ne + e];
+          }
+          user_strength_model(s1, s0, L, a.statev + e, ne, mat, den, a.sie0[e], vol, ctrl->dt, a.rk_alpha);
+#pragma unroll
+          for (int k = 0; k < 9; ++k) a.stress1[(size_t)k * ne + e] = s1[k];
+        }
+      }
       const double gamma = a.gamma[e], csmin = a.csmin[e];
       const double pres = (gamma - 1.0) * sie1 * den;
       sspd = sqrt(gamma * (gamma - 1.0) * sie1);
@@ -456,26 +540,29 @@ __global__ void k_energy_final(const EnergyArgs a, int nblocks) {
 static unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 static void launch_force(const ForceArgs& a, cudaStream_t s) {
-  if (a.inst) k_force<true, false><<<blocks_for(a.ne, kForceBlock), kForceBlock, 0, s>>>(a);
-  else k_force<false, false><<<blocks_for(a.ne, kForceBlock), kForceBlock, 0, s>>>(a);
+  const unsigned g = blocks_for(a.ne, kForceBlock);
+  if (a.inst) k_force<true, false, false><<<g, kForceBlock, 0, s>>>(a);
+  else if (a.stress_out) k_force<false, false, true><<<g, kForceBlock, 0, s>>>(a);
+  else k_force<false, false, false><<<g, kForceBlock, 0, s>>>(a);
 }
 static void launch_force_tape(const ForceArgs& a, cudaStream_t s) {
-  k_force<false, true><<<blocks_for(a.ne, kForceBlock), kForceBlock, 0, s>>>(a);
+  k_force<false, true, false><<<blocks_for(a.ne, kForceBlock), kForceBlock, 0, s>>>(a);
 }
 static void launch_node(const NodeArgs& a, cudaStream_t s) {
   if (a.inst) k_node<true><<<blocks_for(a.nn, kNodeBlock), kNodeBlock, 0, s>>>(a);
   else k_node<false><<<blocks_for(a.nn, kNodeBlock), kNodeBlock, 0, s>>>(a);
 }
-template <bool B>
+template <bool B, bool S>
 static void launch_elem_t(const ElemArgs& a, int kind, cudaStream_t s) {
   const unsigned g = blocks_for(a.ne, kElemBlock);
-  if (kind == 0) k_elem<0, B><<<g, kElemBlock, 0, s>>>(a);
-  else if (kind == 1) k_elem<1, B><<<g, kElemBlock, 0, s>>>(a);
-  else k_elem<2, B><<<g, kElemBlock, 0, s>>>(a);
+  if (kind == 0) k_elem<0, B, S><<<g, kElemBlock, 0, s>>>(a);
+  else if (kind == 1) k_elem<1, B, S><<<g, kElemBlock, 0, s>>>(a);
+  else k_elem<2, B, false><<<g, kElemBlock, 0, s>>>(a);
 }
 static void launch_elem(const ElemArgs& a, int kind, cudaStream_t s) {
-  if (a.inst) launch_elem_t<true>(a, kind, s);
-  else launch_elem_t<false>(a, kind, s);
+  if (a.inst) launch_elem_t<true, false>(a, kind, s);
+  else if (a.stress1) launch_elem_t<false, true>(a, kind, s);
+  else launch_elem_t<false, false>(a, kind, s);
 }
 static void launch_dt(const DtArgs& a, cudaStream_t s) {
   if (a.part_start) k_dt_batch<<<a.ninst, 256, 0, s>>>(a);

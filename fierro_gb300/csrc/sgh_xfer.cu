@@ -8,8 +8,8 @@
 // into a staging buffer.  Threads walk the caller's numbering, so every host
 // access is a coalesced stream; the permutation becomes a scatter (upload) or
 // gather (download) in HBM.  Validation of the uploaded state (material ids,
-// volumes, masses, zero stress) happens in the same pass and reports the first
-// offending caller index.
+// volumes, masses, and zero stress on a handle without strength materials)
+// happens in the same pass and reports the first offending caller index.
 #include <climits>
 #include <cstdint>
 
@@ -76,6 +76,10 @@ struct ElemUp {
   double *d_den, *d_pres, *d_sspd, *d_vol, *d_mass, *d_gamma, *d_csmin, *d_div;
   int* d_mat;
   XferStatus* st;
+  // strength handles: stress [2][ne][9] -> device bins [9][ne], statev -> [nsv][ne]
+  const double* stress;
+  double* d_stress[2];
+  double* d_statev;
 };
 
 __global__ void __launch_bounds__(kBlock) k_up_elems(const ElemUp a) {
@@ -98,6 +102,21 @@ __global__ void __launch_bounds__(kBlock) k_up_elems(const ElemUp a) {
   if (mid >= (uint64_t)a.nmat) flag(a.st, XferStatus::MAT_ID, E);
   if (!(vol > 0.0) || !isfinite(vol)) flag(a.st, XferStatus::VOLUME, E);
   if (!(mass > 0.0)) flag(a.st, XferStatus::MASS, E);
+  if (a.d_statev)
+    for (int k = 0; k < a.nsv; ++k) a.d_statev[(size_t)k * a.ne + e] = a.statev[(size_t)E * a.nsv + k];
+  if (a.stress) {
+    // a missing stress array is a zero stress
+#pragma unroll
+    for (int rb = 0; rb < 2; ++rb)
+#pragma unroll
+      for (int k = 0; k < 9; ++k)
+        a.d_stress[rb ^ 1][(size_t)k * a.ne + e] = a.stress[((size_t)rb * a.ne + E) * 9 + k];
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_zero(double* p, long long n) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+    p[k] = 0.0;
 }
 
 __global__ void __launch_bounds__(kBlock) k_check_zero(const double* p, long long n, XferStatus* st) {
@@ -139,19 +158,24 @@ __global__ void __launch_bounds__(kBlock) k_down_nodes(const NodeDown a) {
 }
 
 struct ElemDown {
-  int ne;
+  int ne, nsv;
   const int* ext2int;
-  double *sie, *den, *pres, *sspd, *vol, *div, *mass, *stress, *corner_force;  // may be null
+  double *sie, *den, *pres, *sspd, *vol, *div, *mass, *stress, *corner_force, *statev;  // may be null
   const double* d_sie[2];  // reference bin rb
   const double *d_den, *d_pres, *d_sspd, *d_vol, *d_div, *d_mass, *d_force;
+  const double* d_stress[2];  // reference bin rb, [9][ne]; null: the stress is zero
+  const double* d_statev;     // [nsv][ne]
 };
 
 __global__ void __launch_bounds__(kBlock) k_down_elems(const ElemDown a) {
+  __shared__ double buf[kBlock * 9];
   const int E0 = blockIdx.x * kBlock;
   const int E = E0 + threadIdx.x;
   const int cnt = min(kBlock, a.ne - E0);
+  const int e = E < a.ne ? a.ext2int[E] : 0;
   if (E < a.ne) {
-    const int e = a.ext2int[E];
+    if (a.statev)
+      for (int k = 0; k < a.nsv; ++k) a.statev[(size_t)E * a.nsv + k] = a.d_statev[(size_t)k * a.ne + e];
     if (a.sie) {
       a.sie[E] = a.d_sie[0][e];
       a.sie[(size_t)a.ne + E] = a.d_sie[1][e];
@@ -167,7 +191,16 @@ __global__ void __launch_bounds__(kBlock) k_down_elems(const ElemDown a) {
 #pragma unroll
     for (int rb = 0; rb < 2; ++rb) {
       double* o = a.stress + ((size_t)rb * a.ne + E0) * 9;
-      for (int k = threadIdx.x; k < cnt * 9; k += kBlock) o[k] = 0.0;
+      if (a.d_stress[rb]) {
+        __syncthreads();
+        if (E < a.ne)
+#pragma unroll
+          for (int k = 0; k < 9; ++k) buf[threadIdx.x * 9 + k] = a.d_stress[rb][(size_t)k * a.ne + e];
+        __syncthreads();
+        for (int k = threadIdx.x; k < cnt * 9; k += kBlock) o[k] = buf[k];
+      } else {
+        for (int k = threadIdx.x; k < cnt * 9; k += kBlock) o[k] = 0.0;
+      }
     }
   }
 }
@@ -317,8 +350,20 @@ int upload_state(fierro_sgh* h, const fierro_sgh_state* s, XferStatus* host_stat
   eu.d_div = h->d_div[1];  // the caller's elem_div is what the reference shows before any stage runs
   eu.d_mat = h->d_mat;
   eu.st = h->d_xfer;
+  if (h->strength) {
+    eu.stress = s->elem_stress;
+    eu.d_stress[0] = h->d_stress[0];
+    eu.d_stress[1] = h->d_stress[1];
+    eu.d_statev = h->d_statev;
+    if (!s->elem_stress) {
+      int dev = 0, sms = 0;
+      CUDA_TRY(cudaGetDevice(&dev));
+      CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+      for (int b = 0; b < 2; ++b) k_zero<<<sms * 4, kBlock, 0, stream>>>(h->d_stress[b], (long long)ne * 9);
+    }
+  }
   k_up_elems<<<blocks(ne), kBlock, 0, stream>>>(eu);
-  if (s->elem_stress) {
+  if (s->elem_stress && !h->strength) {
     int dev = 0, sms = 0;
     CUDA_TRY(cudaGetDevice(&dev));
     CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -369,6 +414,13 @@ int download_state(fierro_sgh* h, fierro_sgh_state* s, const int bins[2], int di
   ed.d_div = h->d_div[div_buffer];
   ed.d_mass = h->d_elem_mass;
   ed.d_force = h->d_force;
+  if (h->strength) {
+    ed.d_stress[0] = h->d_stress[bins[0]];
+    ed.d_stress[1] = h->d_stress[bins[1]];
+    ed.statev = s->elem_statev;
+    ed.nsv = (int)h->nsv;
+    ed.d_statev = h->d_statev;
+  }
   k_down_elems<<<blocks(ne), kBlock, 0, stream>>>(ed);
   if (s->corner_force) k_down_force<<<(unsigned)((ne + kForceChunk - 1) / kForceChunk), kBlock, 0, stream>>>(ed);
   CUDA_TRY(cudaGetLastError());

@@ -21,12 +21,17 @@ VELOCITY = {"cartesian": 0, "radial": 1, "spherical": 2, "radial_linear": 3,
 # bdy::bdy_tag and bdy::bdy_hydro_conds (mesh.h:897-918)
 SURFACE = {"x_plane": 0, "y_plane": 1, "z_plane": 2, "cylinder": 3, "sphere": 4}
 HYDRO_BC = {"fixed": 0, "reflected": 1}
+# model::strength_tag (state.h:103-113)
+STRENGTH = {"none": 0, "hypo": 1, "hyper": 2}
 
 
 @dataclass
 class Material:
     """material_t (state.h:130-178) with its model state variables:
-    statev(0) = gamma, statev(1) = minimum sound speed, statev(2) = c_v."""
+    statev(0) = gamma, statev(1) = minimum sound speed, statev(2) = c_v,
+    statev(3) = the shear modulus read by the shipped strength model.
+    ``strength`` is the strength_type: "none", "hypo" (stress updated in the
+    force pass) or "hyper" (updated in the state pass)."""
     q1: float = 1.0
     q1ex: float = 1.0
     q2: float = 1.3333
@@ -34,9 +39,15 @@ class Material:
     gamma: float = 5.0 / 3.0
     csmin: float = 1.0e-14
     cv: float = 1.0
+    strength: str = "none"
+    shear_modulus: float = 0.0
+
+    @property
+    def strength_type(self) -> int:
+        return STRENGTH[self.strength]
 
     def state_vars(self, n: int) -> List[float]:
-        sv = [self.gamma, self.csmin, self.cv] + [0.0] * max(0, n - 3)
+        sv = [self.gamma, self.csmin, self.cv, self.shear_modulus] + [0.0] * max(0, n - 4)
         return sv[:n]
 
 
@@ -120,6 +131,9 @@ class Problem:
             out.append("fill " + " ".join(repr(float(v)) for v in vals))
         for b in self.boundaries:
             out.append("bc %d %r %d" % (SURFACE[b.surface], float(b.value), HYDRO_BC[b.hydro_bc]))
+        for i, m in enumerate(self.materials):
+            if m.strength_type:
+                out.append("strength %d %d" % (i, m.strength_type))
         return "\n".join(out) + "\n"
 
 
@@ -166,3 +180,35 @@ def noh(n: int = 32, length: float = 1.0, gamma: float = 5.0 / 3.0, speed: float
     params = Params(time_final=0.6, dt_cfl=cfl, cycle_stop=cycles)
     mat = Material(q1=1.0, q1ex=1.0, q2=1.3333, q2ex=0.0, gamma=gamma, csmin=1.0e-14, cv=1.0)
     return Problem("noh", mesh, [mat], fills, _planes_at_zero(), params)
+
+
+def with_strength(problem: Problem, kind: str = "hypo", shear_modulus: float = 1.0) -> Problem:
+    """The deck with every material given a strength model: ``kind`` is "hypo" or
+    "hyper" (strength_type 1 or 2) and the shipped linear hypo-elastic model
+    reads its shear modulus from statev(3)."""
+    for m in problem.materials:
+        m.strength = kind
+        m.shear_modulus = shear_modulus
+    problem.name = "%s_%s" % (problem.name, kind)
+    return problem
+
+
+def sedov_mixed_strength(n: int = 10, shear_modulus: float = 5.0, cycles: int = 50, jitter: float = 0.1,
+                         seed: int = 5, permute: bool = True, length: float = 1.2) -> Problem:
+    """Sedov with three materials: the gas without strength everywhere, a hypo
+    material in the slab z < length/2 (it also holds the blast element) and a
+    hyper material in the block x > length/2, z > length/2."""
+    p = sedov(n, length=length, cycles=cycles, jitter=jitter, seed=seed, permute=permute)
+    base = p.materials[0]
+    mk = lambda kind: Material(q1=base.q1, q1ex=base.q1ex, q2=base.q2, q2ex=base.q2ex, gamma=base.gamma,
+                               csmin=base.csmin, cv=base.cv, strength=kind, shear_modulus=shear_modulus)
+    p.materials = [base, mk("hypo"), mk("hyper")]
+    half = 0.5 * length
+    glob, blast = p.fills
+    p.fills = [glob,
+               Fill("box", 1, x1=0.0, x2=length, y1=0.0, y2=length, z1=0.0, z2=half, den=1.0, sie=1.0e-10),
+               Fill("box", 2, x1=half, x2=length, y1=0.0, y2=length, z1=half, z2=length, den=1.0, sie=1.0e-10),
+               Fill(blast.volume, 1, x1=blast.x1, x2=blast.x2, y1=blast.y1, y2=blast.y2, z1=blast.z1, z2=blast.z2,
+                    den=blast.den, sie=blast.sie, velocity=blast.velocity)]
+    p.name = "sedov_mixed_strength"
+    return p

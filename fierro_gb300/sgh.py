@@ -143,7 +143,7 @@ def c_mesh(mesh) -> tuple:
 
 def c_materials(problem: Problem):
     mats = problem.materials
-    return (Material * len(mats))(*[Material(0, 0, q.q1, q.q1ex, q.q2, q.q2ex) for q in mats])
+    return (Material * len(mats))(*[Material(0, q.strength_type, q.q1, q.q1ex, q.q2, q.q2ex) for q in mats])
 
 
 def c_boundaries(problem: Problem):

@@ -46,8 +46,15 @@ extern "C" {
 #define FIERRO_FP_FMA 1     /* same schedule with fused multiply-adds and
                                reciprocal reuse (differs in the last bits) */
 
-/* material_t (state.h:130-178).  eos_model 0 = ideal_gas (eos.cpp:12);
- * strength_type must be 0 (model::none). */
+/* material_t (state.h:130-178).  eos_model 0 = ideal_gas (eos.cpp:12).
+ * strength_type (model::strength_tag, state.h:103-113): 0 none, 1 hypo (the
+ * stress model runs in the force pass, force_sgh.cpp:362-391), 2 hyper (in the
+ * state update, properties.cpp:46-95).  The model is the library's compiled-in
+ * user_strength_model (fierro_gb300/csrc/sgh_user_mat.cuh), the counterpart of
+ * the reference's user_mat.cpp function pointer; the shipped one is linear
+ * hypo-elasticity with shear modulus statev(3).  A handle with a strength
+ * material carries the full stress tensor (both bins) and all state variables
+ * on the device and needs num_state_vars >= 4. */
 typedef struct {
   int eos_model;
   int strength_type;
@@ -100,14 +107,18 @@ typedef struct {
   double* node_mass;     /* (in) [Nn] */
   double* elem_den;      /* (in) [Ne] */
   double* elem_pres;     /* (in) [Ne] */
-  double* elem_stress;   /* [2][Ne][3][3]; must be zero (no strength model) */
+  double* elem_stress;   /* [2][Ne][3][3]; NULL reads as zero.  Without a strength
+                            material it must be zero; with one it is carried and
+                            returned by get_state */
   double* elem_sspd;     /* (in) [Ne] */
   double* elem_sie;      /* (in) [2][Ne] */
   double* elem_vol;      /* (in) [Ne] */
   double* elem_div;      /* [Ne] (recomputed by the first stage) */
   double* elem_mass;     /* (in) [Ne] */
   uint64_t* elem_mat_id; /* (in) [Ne] */
-  double* elem_statev;   /* (in) [Ne][num_state_vars] */
+  double* elem_statev;   /* (in) [Ne][num_state_vars]; get_state returns it on a
+                            handle with a strength material (the model may
+                            update columns >= 2) */
   double* corner_force;  /* [8Ne][3] (output of the last stage) */
   int64_t num_state_vars;
 } fierro_sgh_state;
@@ -272,8 +283,8 @@ int fierro_sgh_device_view(fierro_sgh* h, fierro_device_view* view);
  * parameters an element's initial specific internal energy and gamma
  * (elem_statev[e][0]).  The pair is shaped like a torch.autograd.Function:
  * forward runs the loop and keeps what backward needs; backward maps adjoints
- * of the final state to adjoints of the parameters.  Exact arithmetic mode only
- * (FIERRO_ENOTSUP otherwise).
+ * of the final state to adjoints of the parameters.  Exact arithmetic mode and
+ * handles without strength materials only (FIERRO_ENOTSUP otherwise).
  *
  * fierro_adj_forward: from the handle's current state (a cycle boundary, e.g.
  * right after set_state), replaces elem_sie (bin 1) by sie0[Ne] and gamma by

@@ -8,7 +8,9 @@ Products, all written only under oracle/_ref/ (git-ignored):
 * fierro_ref / fierro_ref_geo / fierro_ref_fast / fierro_ref_out -- the reference's own SGH solver
   (Explicit-Lagrange-Kokkos/SGH_solver/*.cpp, unmodified) compiled with g++ -fopenmp
   against the project-written MATAR/Kokkos stand-in oracle/compat/matar.h, with
-  input.cpp, the mesh reader and the driver replaced by the files in oracle/ref/.
+  input.cpp, the mesh reader and the driver replaced by the files in oracle/ref/,
+  and a test strength model (oracle/ref/ref_user_mat.cpp) that decks can assign to a
+  material through the reference's strength_model pointer.
   fierro_ref_geo links the reference's own EnSight reader (read_mesh.cpp);
   fierro_ref reads binary meshes; fierro_ref_fast is fierro_ref with the compiler's
   default floating-point contraction (used for timing only); fierro_ref_out links
@@ -100,7 +102,7 @@ def build_reference(verbose=False, jobs=None):
     variants = {"exact": ["-ffp-contract=off"], "fast": []}
     units = [(os.path.join(src_dir, u), u) for u in REF_UNITS + [REF_GEO_READER]]
     units += [(os.path.join(ref_dir, u), u) for u in
-              ["ref_input.cpp", "ref_harness.cpp", "ref_read_mesh_bin.cpp"]]
+              ["ref_input.cpp", "ref_harness.cpp", "ref_read_mesh_bin.cpp", "ref_user_mat.cpp"]]
     headers = [os.path.join(src_dir, h) for h in REF_HEADERS] + [os.path.join(compat, "matar.h")]
 
     jobs_list = []
@@ -121,7 +123,7 @@ def build_reference(verbose=False, jobs=None):
         list(ex.map(_run, jobs_list))
 
     def objs(var, reader):
-        names = REF_UNITS + [reader, "ref_input.cpp", "ref_harness.cpp"]
+        names = REF_UNITS + [reader, "ref_input.cpp", "ref_harness.cpp", "ref_user_mat.cpp"]
         return [os.path.join(OUT, "obj", "%s.%s.o" % (n, var)) for n in names]
 
     out_objs = [o for o in objs("exact", "ref_read_mesh_bin.cpp") if not o.endswith("ref_harness.cpp.exact.o")]

@@ -104,7 +104,7 @@ class Oracle:
         if not self.h:
             raise ValueError("oracle rejected the mesh")
         mats = (OrcMaterial * len(problem.materials))(
-            *[OrcMaterial(0, 0, q.q1, q.q1ex, q.q2, q.q2ex) for q in problem.materials])
+            *[OrcMaterial(0, q.strength_type, q.q1, q.q1ex, q.q2, q.q2ex) for q in problem.materials])
         sv = np.ascontiguousarray(problem.state_vars())
         if L.orc_set_materials(self.h, len(problem.materials), mats, problem.num_state_vars, sv.ctypes.data):
             raise ValueError("oracle rejected the materials")
@@ -161,12 +161,15 @@ class Oracle:
 
     def state(self) -> dict:
         """The compared fields: bin-1 node coords/vel, elem den/pres/sie/sspd/vol,
-        plus both bins, node mass and corner forces."""
+        stress, plus both bins, node mass, corner forces and state variables."""
         nn, ne = self.nn, self.ne
         x = self.get(ORC_NODE_COORDS).reshape(2, nn, 3)
         v = self.get(ORC_NODE_VEL).reshape(2, nn, 3)
         sie = self.get(ORC_ELEM_SIE).reshape(2, ne)
+        stress = self.get(ORC_ELEM_STRESS).reshape(2, ne, 3, 3)
         return {
+            "stress": stress[1].copy(), "stress0": stress[0].copy(),
+            "statev": self.get(ORC_ELEM_STATEV).reshape(ne, -1),
             "coords": x[1].copy(), "vel": v[1].copy(), "coords0": x[0].copy(), "vel0": v[0].copy(),
             "den": self.get(ORC_ELEM_DEN), "pres": self.get(ORC_ELEM_PRES), "sie": sie[1].copy(),
             "sie0": sie[0].copy(), "sspd": self.get(ORC_ELEM_SSPD), "vol": self.get(ORC_ELEM_VOL),
@@ -216,9 +219,16 @@ def read_state_dump(path: str) -> dict:
     sie = take(2 * ne).reshape(2, ne)
     vol, div, mass = take(ne), take(ne), take(ne)
     cf = take(8 * ne * 3).reshape(8 * ne, 3)
-    return {"coords": x[1], "vel": v[1], "coords0": x[0], "vel0": v[0], "den": den, "pres": pres,
-            "sie": sie[1], "sie0": sie[0], "sspd": sspd, "vol": vol, "div": div, "mass": mass,
-            "node_mass": nm, "corner_force": cf, "time": t}
+    out = {"coords": x[1], "vel": v[1], "coords0": x[0], "vel0": v[0], "den": den, "pres": pres,
+           "sie": sie[1], "sie0": sie[0], "sspd": sspd, "vol": vol, "div": div, "mass": mass,
+           "node_mass": nm, "corner_force": cf, "time": t}
+    if a.size >= pos + 2 * ne * 9 + 1:
+        stress = take(2 * ne * 9).reshape(2, ne, 3, 3)
+        (nsv,) = struct.unpack("<Q", buf[24 + 8 * pos:32 + 8 * pos])
+        pos += 1
+        out["stress"], out["stress0"] = stress[1], stress[0]
+        out["statev"] = take(ne * nsv).reshape(ne, nsv)
+    return out
 
 
 def run_reference(problem, cycles: int | None = None, kind: str = "fierro_ref", threads: int | None = None,

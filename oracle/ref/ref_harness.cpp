@@ -13,7 +13,8 @@
 // The dump (little endian): "FSGHSTAT", u64 num_nodes, u64 num_elems,
 // f64 time_value, then f64 arrays node_coords[2][Nn][3], node_vel[2][Nn][3],
 // node_mass[Nn], elem_den[Ne], elem_pres[Ne], elem_sspd[Ne], elem_sie[2][Ne],
-// elem_vol[Ne], elem_div[Ne], elem_mass[Ne], corner_force[8Ne][3].
+// elem_vol[Ne], elem_div[Ne], elem_mass[Ne], corner_force[8Ne][3],
+// elem_stress[2][Ne][3][3], u64 num_state_vars, elem_statev[Ne][num_state_vars].
 #include <chrono>
 #include <cstdint>
 #include <cstdio>
@@ -144,6 +145,10 @@ int main(int argc, char* argv[]) {
     put(f, &elem.div(0), num_elems);
     put(f, &elem.mass(0), num_elems);
     put(f, &corner.force(0, 0), num_corners * 3);
+    put(f, &elem.stress(0, 0, 0, 0), rk_num_bins * num_elems * 9);
+    const uint64_t nsv = num_state_vars;
+    std::fwrite(&nsv, sizeof(uint64_t), 1, f);
+    put(f, &elem.statev(0, 0), num_elems * num_state_vars);
     std::fclose(f);
   }
   Kokkos::finalize();

@@ -8,11 +8,14 @@
 //   material q1 q1ex q2 q2ex sv0 .. sv{num_state_vars-1}
 //   fill volume mat_id x1 x2 y1 y2 z1 z2 r1 r2 velocity u v w speed sie den
 //   bc surface value hydro_bc
+//   strength mat_id type             type 1 = hypo, 2 = hyper: the material runs
+//                                    fierro_test_strength_model (ref_user_mat.cpp)
 // Numbers are parsed with strtod, so a %.17g (or hex-float) value round-trips.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "matar.h"
@@ -20,6 +23,16 @@
 #include "state.h"
 
 extern const char* fierro_ref_config_path;
+
+void fierro_test_strength_model(const DViewCArrayKokkos<double>& elem_pres,
+                                const DViewCArrayKokkos<double>& elem_stress, const size_t elem_gid,
+                                const size_t mat_id, const DViewCArrayKokkos<double>& elem_state_vars,
+                                const DViewCArrayKokkos<double>& elem_sspd, const double den, const double sie,
+                                const ViewCArrayKokkos<double>& vel_grad,
+                                const ViewCArrayKokkos<size_t>& elem_node_gids,
+                                const DViewCArrayKokkos<double>& node_coords,
+                                const DViewCArrayKokkos<double>& node_vel, const double vol, const double dt,
+                                const double rk_alpha);
 
 namespace {
 
@@ -60,6 +73,7 @@ void input(CArrayKokkos<material_t>& material, CArrayKokkos<mat_fill_t>& mat_fil
   std::vector<MatRec> mats;
   std::vector<FillRec> fills;
   std::vector<BcRec> bcs;
+  std::vector<std::pair<size_t, int>> strengths;
   char buf[4096];
   while (std::fgets(buf, sizeof(buf), f)) {
     std::string line(buf);
@@ -87,6 +101,8 @@ void input(CArrayKokkos<material_t>& material, CArrayKokkos<mat_fill_t>& mat_fil
       fills.push_back(r);
     } else if (k == "bc") {
       bcs.push_back(BcRec{(int)num(t[1]), num(t[2]), (int)num(t[3])});
+    } else if (k == "strength") {
+      strengths.emplace_back((size_t)num(t[1]), (int)num(t[2]));
     }
   }
   std::fclose(f);
@@ -110,6 +126,14 @@ void input(CArrayKokkos<material_t>& material, CArrayKokkos<mat_fill_t>& mat_fil
     material(m).q2ex = mats[m].q2ex;
     material(m).num_state_vars = max_num_state_vars;
     for (size_t v = 0; v < max_num_state_vars && v < mats[m].sv.size(); ++v) state_vars(m, v) = mats[m].sv[v];
+  }
+  for (const auto& st : strengths) {
+    if (st.first >= num_materials || st.second < 1 || st.second > 2) {
+      std::fprintf(stderr, "bad strength line: material %zu type %d\n", st.first, st.second);
+      std::exit(2);
+    }
+    material(st.first).strength_type = (model::strength_tag)st.second;
+    material(st.first).strength_model = fierro_test_strength_model;
   }
   for (size_t i = 0; i < num_fills; ++i) {
     const double* v = fills[i].v;

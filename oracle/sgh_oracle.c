@@ -263,8 +263,10 @@ void orc_destroy(orc_sim* s) {
 int orc_set_materials(orc_sim* s, int num_materials, const orc_material* m, int num_state_vars,
                       const double* state_vars) {
   if (num_materials <= 0 || num_state_vars < 2) return 1;
-  for (int i = 0; i < num_materials; ++i)
-    if (m[i].eos_model != 0 || m[i].strength_type != 0) return 1;
+  for (int i = 0; i < num_materials; ++i) {
+    if (m[i].eos_model != 0 || m[i].strength_type < 0 || m[i].strength_type > 2) return 1;
+    if (m[i].strength_type != 0 && num_state_vars < 4) return 1;
+  }
   free(s->mat); free(s->state_vars); free(s->statev);
   s->nmat = num_materials;
   s->nsv = num_state_vars;
@@ -573,18 +575,53 @@ static void get_divergence(orc_sim* s) {
   }
 }
 
-/* force_sgh.cpp:12-399 get_force_sgh (3D, strength none).  The shock direction,
- * velocity gradient and curl terms of the reference feed only unused variables
- * (use_shock_dir = 0 at :227, phi_curl unused at :331) and are omitted. */
-static void get_force_sgh(orc_sim* s, const orc_params* p) {
+/* momentum.cpp:59-144 get_velgrad: L(i,j) = (sum_l v_i(l) B(l,j)) / vol with B the
+ * outward corner normals, summed over l in order, times the reciprocal volume. */
+static void get_velgrad(double L[3][3], const double u[8], const double v[8], const double w[8],
+                        double B[8][3], double vol) {
+  const double inverse_vol = 1.0 / vol;
+  const double* vc[3] = {u, v, w};
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double acc = vc[i][0] * B[0][j];
+      for (int l = 1; l < 8; ++l) acc = acc + vc[i][l] * B[l][j];
+      L[i][j] = acc * inverse_vol;
+    }
+}
+
+/* The test strength model the reference oracle build assigns through
+ * material_t::strength_model (oracle/ref/ref_user_mat.cpp): linear
+ * hypo-elasticity of the deviatoric stress, G = statev(3),
+ * stress(1) = stress(0) + rk_alpha dt 2 G (D - tr(D)/3 I), D = (L + L^T)/2. */
+static void strength_model(orc_sim* s, int64_t e, double L[3][3], double dt, double rk_alpha) {
+  const size_t ne = (size_t)s->ne;
+  const double G = s->statev[(size_t)e * (size_t)s->nsv + 3];
+  double D[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) D[i][j] = 0.5 * (L[i][j] + L[j][i]);
+  const double tr = D[0][0] + D[1][1] + D[2][2];
+  for (int i = 0; i < 3; ++i) D[i][i] -= tr / 3.0;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      s->stress[ne * 9 + (size_t)e * 9 + (size_t)(i * 3 + j)] =
+          s->stress[(size_t)e * 9 + (size_t)(i * 3 + j)] + rk_alpha * dt * 2.0 * G * D[i][j];
+}
+
+/* force_sgh.cpp:12-399 get_force_sgh (3D).  The shock direction and curl terms
+ * of the reference feed only unused variables (use_shock_dir = 0 at :227,
+ * phi_curl unused at :331) and are omitted; the velocity gradient is formed for
+ * hypo materials only, whose strength model (:366-391) reads it. */
+static void get_force_sgh(orc_sim* s, const orc_params* p, double rk_alpha) {
   const double fuzz = p->fuzz, small = p->small;
   const size_t ne = (size_t)s->ne;
 #pragma omp parallel for schedule(static)
   for (int64_t e = 0; e < s->ne; ++e) {
     double x[8], y[8], z[8], an[8][3], tau[3][3], muc[8], sum[4], vel_star[3];
     double vol = s->vol[e];
+    double Bout[8][3];
     gather_x1(s, e, x, y, z);
     orc_bmatrix(x, y, z, an);
+    memcpy(Bout, an, sizeof(Bout));
     for (int l = 0; l < 8; ++l)
       for (int d = 0; d < 3; ++d) an[l][d] = (-1.0) * an[l][d];
     double div = s->div[e];
@@ -640,6 +677,17 @@ static void get_force_sgh(orc_sim* s, const orc_params* p) {
             phi * muc[l] * (vel_star[d] - V1(s, n, d));
       }
     }
+    if (M->strength_type == 1) {
+      double u[8], v[8], w[8], L[3][3];
+      for (int l = 0; l < 8; ++l) {
+        int64_t n = s->nie[e * 8 + l];
+        u[l] = V1(s, n, 0);
+        v[l] = V1(s, n, 1);
+        w[l] = V1(s, n, 2);
+      }
+      get_velgrad(L, u, v, w, Bout, vol);
+      strength_model(s, e, L, s->dt, rk_alpha);
+    }
   }
 }
 
@@ -682,12 +730,26 @@ static void update_position(orc_sim* s, double rk_alpha, double dt) {
     }
 }
 
-/* properties.cpp:9-114 update_state (strength none) */
-static void update_state(orc_sim* s) {
+/* properties.cpp:9-114 update_state: density, the hyper strength model with the
+ * velocity gradient of the updated state (:46-95), then the EOS. */
+static void update_state(orc_sim* s, double rk_alpha) {
   const size_t ne = (size_t)s->ne;
 #pragma omp parallel for schedule(static)
   for (int64_t e = 0; e < s->ne; ++e) {
     s->den[e] = s->mass[e] / s->vol[e];
+    if (s->mat[s->mat_id[e]].strength_type == 2) {
+      double x[8], y[8], z[8], B[8][3], u[8], v[8], w[8], L[3][3];
+      gather_x1(s, e, x, y, z);
+      orc_bmatrix(x, y, z, B);
+      for (int l = 0; l < 8; ++l) {
+        int64_t n = s->nie[e * 8 + l];
+        u[l] = V1(s, n, 0);
+        v[l] = V1(s, n, 1);
+        w[l] = V1(s, n, 2);
+      }
+      get_velgrad(L, u, v, w, B, s->vol[e]);
+      strength_model(s, e, L, s->dt, rk_alpha);
+    }
     ideal_gas(s, e, s->den[e], s->sie[ne + (size_t)e]);
   }
 }
@@ -696,13 +758,13 @@ static void update_state(orc_sim* s) {
 static void rk_stage(orc_sim* s, const orc_params* p, int stage) {
   double rk_alpha = 1.0 / ((double)p->rk_num_stages - (double)stage);
   get_divergence(s);
-  get_force_sgh(s, p);
+  get_force_sgh(s, p, rk_alpha);
   update_velocity(s, rk_alpha, s->dt);
   boundary_velocity(s);
   update_energy(s, rk_alpha, s->dt);
   update_position(s, rk_alpha, s->dt);
   get_vol(s);
-  update_state(s);
+  update_state(s, rk_alpha);
 }
 
 /* sgh_solve.cpp:590-632: time advance, graphics-time bookkeeping, stop test. */

@@ -28,10 +28,12 @@
 extern "C" {
 #endif
 
-/* material_t (state.h:130-178); only the ideal-gas EOS and strength "none". */
+/* material_t (state.h:130-178); the ideal-gas EOS only.  strength_type 1 (hypo)
+ * and 2 (hyper) run the test strength model of oracle/ref/ref_user_mat.cpp
+ * (shear modulus statev(3); needs num_state_vars >= 4). */
 typedef struct {
   int eos_model;      /* 0 = ideal_gas (eos.cpp:12) */
-  int strength_type;  /* 0 = model::none (state.h:107-112) */
+  int strength_type;  /* model::strength_tag (state.h:107-112): 0 none, 1 hypo, 2 hyper */
   double q1, q1ex, q2, q2ex;
 } orc_material;
 

@@ -8,6 +8,11 @@ and Noh decks of fierro_gb300.problems, and its states after one cycle and after
 the full run are stored as float64 .npz files.  Also stored: checksums of the
 shipped meshes, so the box generator can be checked without the reference tree.
 
+Strength-model cases (strength_*.npz) run the reference with the test strength
+model of oracle/ref/ref_user_mat.cpp assigned through material_t::strength_model,
+on meshes from the box generator, and also store the stress bins and the
+element state variables.
+
 Run from the repository root (needs the reference tree):
     python tests/golden/make_golden.py
 """
@@ -28,6 +33,19 @@ FIELDS = ("coords", "vel", "den", "pres", "sie", "sspd", "vol")
 
 def digest(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+STRENGTH_FIELDS = ("stress", "stress0", "statev", "corner_force", "div")
+
+
+def strength_cases():
+    """The strength-model decks (also used by the tests, which import this)."""
+    from fierro_gb300 import problems
+    return {
+        "sedov8_hypo": problems.with_strength(problems.sedov(8, cycles=40), "hypo", 10.0),
+        "noh8_hyper": problems.with_strength(problems.noh(8, cycles=60), "hyper", 0.05),
+        "sedov10_mixed": problems.sedov_mixed_strength(10, shear_modulus=5.0, cycles=50),
+    }
 
 
 def main():
@@ -55,6 +73,16 @@ def main():
             np.savez_compressed(fn, **out)
             meta[name]["c%d" % c] = {"file": os.path.basename(fn), "time": float(st["time"])}
             print(fn, os.path.getsize(fn))
+    meta["strength"] = {}
+    for name, prob in strength_cases().items():
+        st = orc.run_reference(prob, threads=1)
+        out = {k: st[k] for k in FIELDS + STRENGTH_FIELDS}
+        out["time"] = np.array(st["time"])
+        fn = os.path.join(HERE, "strength_%s.npz" % name)
+        np.savez_compressed(fn, **out)
+        meta["strength"][name] = {"file": os.path.basename(fn), "time": float(st["time"]),
+                                  "cycles": prob.params.cycle_stop, "deck": prob.config_text()}
+        print(fn, os.path.getsize(fn))
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(meta, f, indent=1, sort_keys=True)
 

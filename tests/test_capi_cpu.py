@@ -96,11 +96,36 @@ def test_setup_rejects_unsupported_models(lib_built):
     from fierro_gb300 import sgh
     prob = _deck()
 
-    def hypo(mats):
-        mats[0].strength_type = 1
+    def eos(mats):
+        mats[0].eos_model = 1
 
-    rc, msg = _setup_rc(prob, mutate_mat=hypo)
-    assert rc == sgh.FIERRO_ENOTSUP and "strength" in msg
+    def unknown_strength(mats):
+        mats[0].strength_type = 3
+
+    rc, msg = _setup_rc(prob, mutate_mat=eos)
+    assert rc == sgh.FIERRO_ENOTSUP and "EOS" in msg
+    rc, msg = _setup_rc(prob, mutate_mat=unknown_strength)
+    assert rc == sgh.FIERRO_EINVAL and "strength_type" in msg
+
+
+@pytest.mark.parametrize("kind", ["hypo", "hyper"])
+def test_setup_with_strength_material(lib_built, oracle_built, kind):
+    """setup (setup.cpp:10-424) with a strength material: stress zero, the state
+    variables (shear modulus in statev(3)) copied from the material, the rest as
+    without strength; equal to the C restatement's setup."""
+    from fierro_gb300 import sgh
+    from oracle import orc
+    prob = _deck()
+    prob.materials[0].strength = kind
+    prob.materials[0].shear_modulus = 2.5
+    st = sgh.setup(prob)
+    assert np.all(st["elem_stress"] == 0.0)
+    assert np.all(st["elem_statev"][:, 3] == 2.5)
+    o = orc.Oracle(prob)
+    r = o.state()
+    np.testing.assert_array_equal(st["elem_statev"], r["statev"])
+    np.testing.assert_array_equal(st["elem_sie"][1], r["sie"])
+    np.testing.assert_array_equal(st["elem_pres"], r["pres"])
 
 
 def test_reflected_bc_needs_plane(lib_built):

@@ -97,3 +97,53 @@ def test_geometry_identities(oracle_built):
         t = rng.uniform(-3, 3, 3)
         x2, y2, z2 = (h + t).T
         assert abs(orc.vol_hex(x2, y2, z2) - V) <= 1e-12 * V
+
+
+def _strength_cases():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    return mg.strength_cases()
+
+
+@pytest.mark.parametrize("case", ["sedov8_hypo", "noh8_hyper", "sedov10_mixed"])
+def test_oracle_strength_equals_reference_golden(oracle_built, case):
+    """Strength models: the C restatement with the test hypo-elastic model, called
+    as a hypo model (force pass) or a hyper model (state update), equals the
+    reference running the same model through material_t::strength_model, bit for
+    bit, including both stress bins and the state variables."""
+    from oracle import orc
+    prob = _strength_cases()[case]
+    meta = json.load(open(os.path.join(GOLDEN, "golden.json")))["strength"][case]
+    assert prob.config_text() == meta["deck"]
+    ref = load_golden("strength_" + case)
+    assert np.abs(ref["stress"]).max() > 1e-3  # the stress is not negligible
+    o = orc.Oracle(prob)
+    o.run_cycles(prob.params.cycle_stop)
+    st = o.state()
+    assert st["time"] == float(ref["time"])
+    assert_bitwise(st, ref, FIELDS + ("corner_force", "div", "stress", "stress0", "statev"), label=case)
+
+
+def test_oracle_strength_equals_reference_live(oracle_built):
+    """The same against the reference executable run here, on a hyper Sedov with
+    a jittered, permuted mesh, when the reference build is available."""
+    from fierro_gb300 import problems
+    from oracle import orc
+    if not orc.reference_available("fierro_ref"):
+        pytest.skip("reference executable not built on this machine")
+    prob = problems.with_strength(problems.sedov(9, jitter=0.1, seed=4, permute=True, cycles=30), "hyper", 8.0)
+    ref = orc.run_reference(prob, threads=2)
+    o = orc.Oracle(prob)
+    o.run_cycles(30)
+    assert_bitwise(o.state(), ref, FIELDS + ("corner_force", "stress", "stress0"), label="sedov9 hyper")
+
+
+def test_oracle_strength_needs_shear_modulus_column(oracle_built):
+    from fierro_gb300 import problems
+    from oracle import orc
+    prob = problems.with_strength(problems.sedov(4, cycles=2), "hypo", 1.0)
+    prob.num_state_vars = 3
+    with pytest.raises(ValueError):
+        orc.Oracle(prob)
