@@ -579,6 +579,17 @@ def outputs_bench(args):
     print(json.dumps(line))
 
 
+# The same per-element counters for the strength instantiations, from the capture
+# summarised in profiles/strength_kernels_sedov64_ncu_full.md (64^3, exact mode,
+# mean of the two RK-stage launches): hypo k_force<0,0,1>, hyper k_elem<*,0,1>.
+NCU_PER_ELEM_STRENGTH = {
+    ("hypo", "k_force"): {"fp64_ops": (233308160 + 214695936) / 2 / 262144,
+                          "dram_bytes": (125.731072e6 + 36.583424e6 + 145.0176e6 + 37.52832e6) / 2 / 262144},
+    ("hyper", "k_elem"): {"fp64_ops": (207093760 + 220530720) / 2 / 262144,
+                          "dram_bytes": (109.706496e6 + 43.420928e6 + 109.884416e6 + 43.996672e6) / 2 / 262144},
+}
+
+
 def strength_alg_bytes(kind: str, kernel: str, nn: int, ne: int, nnz: int) -> float:
     """Compulsory bytes of one launch (mean over the two RK stages) of a kernel of
     a strength run with every element on the model: the plain kernel's bytes plus
@@ -643,6 +654,8 @@ def strength_bench(args):
     ab = strength_alg_bytes(args.strength, dom, nn, ne, nnz)
     hbm_peak, peak_kind = measure_peaks()
     achieved = ab / (per[dom] * 1e-3) / 1e9
+    nc = NCU_PER_ELEM_STRENGTH.get((args.strength, dom)) if args.fp_mode == "exact" else None
+    fp64_rate = sgh.measure_fp64_rate()
     cpu = None
     if not args.no_cpu_baseline:
         try:
@@ -661,8 +674,15 @@ def strength_bench(args):
             "plain_value": plain["value"], "strength_over_plain_time": plain["value"] / r["value"],
             "kernels_ms_per_launch": {"strength": per, "plain": plain["kernels_ms_per_launch"]},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": None, "peak_kind": peak_kind,
-                         "alg_bytes_per_launch": ab, "avg_launch_ms": per[dom]},
+                         "frac": achieved / hbm_peak, "traffic": nc["dram_bytes"] * ne if nc else None,
+                         "peak_kind": peak_kind, "alg_bytes_per_launch": ab, "avg_launch_ms": per[dom],
+                         "binding_pipe": "fp64",
+                         "fp64": None if nc is None else {
+                             "achieved": nc["fp64_ops"] * ne / (per[dom] * 1e-3) / 1e9, "peak": fp64_rate / 1e9,
+                             "unit": "G FP64 thread-instructions/s",
+                             "frac": nc["fp64_ops"] * ne / (per[dom] * 1e-3) / fp64_rate,
+                             "peak_kind": "measured DFMA rate on this GPU (fierro_measure_fp64_rate)",
+                             "ops_per_elem": nc["fp64_ops"]}},
             "max_abs_stress": r["max_abs_stress"], "finite": r["finite"],
             "cpu_baseline": None if cpu is None else {k: cpu[k] for k in ("value", "unit", "cores", "kind",
                                                                          "sample")},
