@@ -1,12 +1,15 @@
-"""Hex meshes for the SGH solver: structured box generation (optionally jittered
-and randomly renumbered from a seed), an EnSight Gold ``.geo`` reader, and the
-binary mesh format read by the reference oracle harness.
+"""Hex and quad meshes for the SGH solver: structured box generation (optionally
+jittered and randomly renumbered from a seed), an EnSight Gold ``.geo`` reader,
+and the binary mesh format read by the reference oracle harness.
 
 Meshes follow the reference's conventions (Explicit-Lagrange-Kokkos/SGH_solver):
 ``coords`` is ``[num_nodes][3]`` float64 and ``nodes_in_elem`` is ``[num_elems][8]``
 0-based with the hex node ordering of mesh.h:15-45 (nodes 0-3 counter-clockwise on
 the k face, 4-7 above them).  Box meshes number nodes with i fastest, then j, then
-k, exactly like the shipped ``mesh_12x12x12.geo`` / ``mesh_Box_32.geo``.
+k, exactly like the shipped ``mesh_12x12x12.geo`` / ``mesh_Box_32.geo``.  2D-RZ
+meshes have ``coords`` ``[num_nodes][2]`` (x = axial, y = radial) and quads
+``[num_elems][4]`` counter-clockwise (0 at (i, j), 1 at (i+1, j), 2 at
+(i+1, j+1), 3 at (i, j+1); sgh_solve.cpp:513-519).
 """
 from __future__ import annotations
 
@@ -50,6 +53,11 @@ class HexMesh:
     @property
     def num_elems(self) -> int:
         return int(self.nodes_in_elem.shape[0])
+
+    @property
+    def dims(self) -> int:
+        """3 for hex meshes, 2 for 2D-RZ quad meshes."""
+        return int(self.coords.shape[1])
 
 
 def box_mesh(nx: int, ny: int | None = None, nz: int | None = None, length=(1.0, 1.0, 1.0),
@@ -113,6 +121,57 @@ def box_mesh(nx: int, ny: int | None = None, nz: int | None = None, length=(1.0,
     return HexMesh(np.ascontiguousarray(coords), np.ascontiguousarray(nie), name=name)
 
 
+def quad_mesh(nx: int, ny: int | None = None, length=(1.0, 1.0), jitter: float = 0.0, seed: int = 0,
+              permute: bool = False, origin=(0.0, 0.0), name: str = "") -> HexMesh:
+    """Uniform nx*ny quad mesh of [x0, x0+Lx] x [y0, y0+Ly] for the 2D-RZ path
+    (x axial, y radial).  jitter and permute as in box_mesh: interior nodes move
+    by U(-jitter*h, +jitter*h) per axis, boundary nodes keep their coordinate on
+    the edge-normal axis."""
+    ny = nx if ny is None else ny
+    if np.isscalar(length):
+        length = (float(length),) * 2
+    Lx, Ly = (float(v) for v in length)
+    hx, hy = Lx / nx, Ly / ny
+    xs = origin[0] + np.arange(nx + 1, dtype=np.float64) * hx
+    ys = origin[1] + np.arange(ny + 1, dtype=np.float64) * hy
+    Y, X = np.meshgrid(ys, xs, indexing="ij")
+    coords = np.stack([X.ravel(), Y.ravel()], axis=1)
+    nn = coords.shape[0]
+    if jitter:
+        J, I = np.meshgrid(np.arange(ny + 1), np.arange(nx + 1), indexing="ij")
+        I, J = I.ravel(), J.ravel()
+        interior = (I > 0) & (I < nx) & (J > 0) & (J < ny)
+        for ax, h in enumerate((hx, hy)):
+            r = uniform01(seed, 1 + ax, nn)
+            coords[:, ax] = np.where(interior, coords[:, ax] + (2.0 * r - 1.0) * jitter * h, coords[:, ax])
+    ej, ei = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+    ei, ej = ei.ravel(), ej.ravel()
+
+    def nid(a, b):
+        return a + (nx + 1) * b
+
+    nie = np.stack([nid(ei, ej), nid(ei + 1, ej), nid(ei + 1, ej + 1), nid(ei, ej + 1)], axis=1).astype(np.int64)
+    if permute:
+        ne = nie.shape[0]
+        eperm = np.argsort(splitmix64(np.arange(ne, dtype=np.uint64) + np.uint64(seed * 7919 + 11)), kind="stable")
+        nperm = np.argsort(splitmix64(np.arange(nn, dtype=np.uint64) + np.uint64(seed * 104729 + 13)), kind="stable")
+        inv = np.empty(nn, dtype=np.int64)
+        inv[nperm] = np.arange(nn, dtype=np.int64)
+        coords = coords[nperm]
+        nie = inv[nie[eperm]]
+    return HexMesh(np.ascontiguousarray(coords), np.ascontiguousarray(nie), name=name)
+
+
+def quad_rz_volumes(coords: np.ndarray, nodes_in_elem: np.ndarray) -> np.ndarray:
+    """Volume per radian of quads revolved about the x axis (Pappus: area times
+    centroid radius), for problem set-up values only."""
+    x = coords[nodes_in_elem][:, :, 0]
+    y = coords[nodes_in_elem][:, :, 1]
+    a = 0.5 * (x * np.roll(y, -1, axis=1) - np.roll(x, -1, axis=1) * y).sum(axis=1)
+    cy = ((y + np.roll(y, -1, axis=1)) * (x * np.roll(y, -1, axis=1) - np.roll(x, -1, axis=1) * y)).sum(axis=1)
+    return cy / 6.0
+
+
 def read_geo(path: str) -> HexMesh:
     """EnSight Gold .geo reader for single-part hexa8 meshes, with the reference's
     conventions (read_mesh.cpp:12-147: 8 header lines, node count, x[], y[], z[],
@@ -136,11 +195,12 @@ def read_geo(path: str) -> HexMesh:
 
 def write_mesh_bin(path: str, mesh: HexMesh) -> None:
     """Binary mesh read by the reference oracle's mesh reader:
-    'FSGHMESH', u64 Nn, u64 Ne, f64 x[Nn], y[Nn], z[Nn], u64 nodes_in_elem[Ne][8]."""
+    'FSGHMESH', u64 Nn, u64 Ne, f64 x[Nn], y[Nn] (and z[Nn] for hexes),
+    u64 nodes_in_elem[Ne][8 or 4]."""
     with open(path, "wb") as f:
         f.write(b"FSGHMESH")
         f.write(struct.pack("<QQ", mesh.num_nodes, mesh.num_elems))
-        for d in range(3):
+        for d in range(mesh.dims):
             f.write(np.ascontiguousarray(mesh.coords[:, d], dtype="<f8").tobytes())
         f.write(np.ascontiguousarray(mesh.nodes_in_elem, dtype="<u8").tobytes())
 

@@ -11,7 +11,7 @@ from typing import List
 
 import numpy as np
 
-from .mesh import HexMesh, box_mesh, hex_volumes
+from .mesh import HexMesh, box_mesh, hex_volumes, quad_mesh
 
 # region::vol_tag (mesh.h:824-830)
 REGION = {"global": 0, "box": 1, "cylinder": 2, "sphere": 3}
@@ -122,6 +122,8 @@ class Problem:
             "graphics_cyc_ival %d" % p.graphics_cyc_ival, "cycle_stop %d" % p.cycle_stop,
             "rk_num_stages %d" % p.rk_num_stages, "num_state_vars %d" % self.num_state_vars,
         ]
+        if self.mesh.dims == 2:
+            out.append("num_dims 2")
         for m in self.materials:
             sv = " ".join(repr(float(v)) for v in m.state_vars(self.num_state_vars))
             out.append("material %r %r %r %r %s" % (m.q1, m.q1ex, m.q2, m.q2ex, sv))
@@ -212,3 +214,42 @@ def sedov_mixed_strength(n: int = 10, shear_modulus: float = 5.0, cycles: int = 
                     den=blast.den, sie=blast.sie, velocity=blast.velocity)]
     p.name = "sedov_mixed_strength"
     return p
+
+
+def sedov_rz(n: int = 32, length: float = 1.2, energy: float = 0.49339, gamma: float = 5.0 / 3.0,
+             cycles: int = 200, jitter: float = 0.0, seed: int = 0, permute: bool = False,
+             mesh: HexMesh | None = None, cfl: float = 0.4) -> Problem:
+    """2D-RZ Sedov blast, the deck of the reference's RZ test
+    (tests-for-Explicit-Lagrange-Kokkos/input_for_SedovRZ_test.cpp): n x n quads on
+    [0, length]^2 (x axial, y radial), gamma 5/3, rho 1, sie 1e-10, a sphere of
+    radius length/n at the origin holding sie = 0.5 energy / (rho pi r^3), four
+    reflecting planes."""
+    if mesh is None:
+        mesh = quad_mesh(n, length=length, jitter=jitter, seed=seed, permute=permute, name="sedov_rz%d" % n)
+    r2 = length / n
+    vol = 3.141592653589793 * (r2 ** 3 - 0.0 ** 3)
+    fills = [
+        Fill("global", 0, den=1.0, sie=1.0e-10, velocity="cartesian"),
+        Fill("sphere", 0, radius1=0.0, radius2=r2, den=1.0, sie=0.5 * energy / (1.0 * vol), velocity="cartesian"),
+    ]
+    params = Params(time_final=1.0, dt_cfl=cfl, cycle_stop=cycles, graphics_dt_ival=1.0e8)
+    mat = Material(q1=1.0, q1ex=1.0, q2=1.3333, q2ex=0.0, gamma=gamma, csmin=1.0e-14, cv=1.0)
+    bcs = [Boundary("x_plane", 0.0, "reflected"), Boundary("y_plane", 0.0, "reflected"),
+           Boundary("x_plane", length, "reflected"), Boundary("y_plane", length, "reflected")]
+    return Problem("sedov_rz", mesh, [mat], fills, bcs, params, info={"h": length / n})
+
+
+def noh_rz(n: int = 32, length: float = 1.0, gamma: float = 5.0 / 3.0, speed: float = -1.0,
+           cycles: int = 300, jitter: float = 0.0, seed: int = 0, permute: bool = False,
+           mesh: HexMesh | None = None, cfl: float = 0.4) -> Problem:
+    """2D-RZ Noh implosion, the deck of the reference's RZ test
+    (tests-for-Explicit-Lagrange-Kokkos/input_for_NohRZ_test.cpp): n x n quads on
+    [0, length]^2, gamma 5/3, rho 1, sie 1e-9, velocity speed * (x, y)/|(x, y)|,
+    reflecting planes x = 0 and y = 0 (the axis)."""
+    if mesh is None:
+        mesh = quad_mesh(n, length=length, jitter=jitter, seed=seed, permute=permute, name="noh_rz%d" % n)
+    fills = [Fill("global", 0, den=1.0, sie=1.0e-9, velocity="radial", speed=speed)]
+    params = Params(time_final=0.6, dt_cfl=cfl, cycle_stop=cycles)
+    mat = Material(q1=1.0, q1ex=1.0, q2=1.3333, q2ex=0.0, gamma=gamma, csmin=1.0e-14, cv=1.0)
+    bcs = [Boundary("x_plane", 0.0, "reflected"), Boundary("y_plane", 0.0, "reflected")]
+    return Problem("noh_rz", mesh, [mat], fills, bcs, params)

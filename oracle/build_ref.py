@@ -3,7 +3,8 @@
 Products, all written only under oracle/_ref/ (git-ignored):
 
 * liborc_sgh.so, liborc_sgh_crpow.so -- the plain-C restatement in oracle/sgh_oracle.c
-  (libm pow, and a correctly rounded pow variant), compiled with
+  and its 2D-RZ counterpart oracle/sgh_oracle_rz.c (libm pow, and a correctly
+  rounded pow variant of the 3D Mach detector), compiled with
   -ffp-contract=off so its doubles follow the reference's uncontracted evaluation.
 * fierro_ref / fierro_ref_geo / fierro_ref_fast / fierro_ref_out -- the reference's own SGH solver
   (Explicit-Lagrange-Kokkos/SGH_solver/*.cpp, unmodified) compiled with g++ -fopenmp
@@ -64,13 +65,14 @@ def build_oracle_lib(verbose=False):
     reference) and oracle/_ref/liborc_sgh_crpow.so (correctly rounded pow)."""
     os.makedirs(OUT, exist_ok=True)
     src = os.path.join(HERE, "sgh_oracle.c")
+    src_rz = os.path.join(HERE, "sgh_oracle_rz.c")
     hdr = os.path.join(HERE, "sgh_oracle.h")
     libs = {"liborc_sgh.so": [], "liborc_sgh_crpow.so": ["-DORC_CR_POW"]}
     for name, extra in libs.items():
         lib = os.path.join(OUT, name)
-        if not _newer(lib, [src, hdr, __file__]):
+        if not _newer(lib, [src, src_rz, hdr, __file__]):
             _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off"] + extra +
-                 ["-o", lib, src, "-lm"])
+                 ["-o", lib, src, src_rz, "-lm"])
     return os.path.join(OUT, "liborc_sgh.so")
 
 

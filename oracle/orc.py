@@ -80,6 +80,17 @@ def lib(variant: str = "libm"):
         _lib.orc_bmatrix.argtypes = [C.c_void_p] * 4
         _lib.orc_vol_hex.restype = C.c_double
         _lib.orc_vol_hex.argtypes = [C.c_void_p] * 3
+        # the 2D-RZ restatement (oracle/sgh_oracle_rz.c): the same calls with orc_rz_
+        for name in ("create", "destroy", "set_materials", "set_boundaries", "setup", "init_time",
+                     "run_cycles", "run_stages", "energy", "time", "get", "set"):
+            f3, f2 = getattr(_lib, "orc_" + name), getattr(_lib, "orc_rz_" + name)
+            f2.restype, f2.argtypes = f3.restype, f3.argtypes
+        _lib.orc_rz_bmatrix.argtypes = [C.c_void_p] * 3
+        _lib.orc_rz_vol_quad.restype = C.c_double
+        _lib.orc_rz_vol_quad.argtypes = [C.c_void_p] * 2
+        _lib.orc_rz_area_quad.restype = C.c_double
+        _lib.orc_rz_area_quad.argtypes = [C.c_void_p] * 2
+        _lib.orc_rz_corner_areas.argtypes = [C.c_void_p] * 3
         _libs[variant] = _lib
     return _libs[variant]
 
@@ -90,28 +101,30 @@ def make_params(p) -> OrcParams:
 
 
 class Oracle:
-    """One problem instance in the C restatement."""
+    """One problem instance in the C restatement (3D hex, or 2D-RZ quad meshes
+    through the orc_rz_ calls)."""
 
     def __init__(self, problem, setup=True, variant: str = "libm"):
         from fierro_gb300.problems import REGION, VELOCITY, SURFACE, HYDRO_BC
         self.variant = variant
-        L = lib(variant)
         m = problem.mesh
+        self.dims = m.dims
+        self._p = "orc_rz_" if self.dims == 2 else "orc_"
         self.nn, self.ne = m.num_nodes, m.num_elems
         self._nie = np.ascontiguousarray(m.nodes_in_elem, dtype=np.int64)
         self._xyz = np.ascontiguousarray(m.coords, dtype=np.float64)
-        self.h = L.orc_create(self.nn, self.ne, self._nie.ctypes.data, self._xyz.ctypes.data)
+        self.h = self._f("create")(self.nn, self.ne, self._nie.ctypes.data, self._xyz.ctypes.data)
         if not self.h:
             raise ValueError("oracle rejected the mesh")
         mats = (OrcMaterial * len(problem.materials))(
             *[OrcMaterial(0, q.strength_type, q.q1, q.q1ex, q.q2, q.q2ex) for q in problem.materials])
         sv = np.ascontiguousarray(problem.state_vars())
-        if L.orc_set_materials(self.h, len(problem.materials), mats, problem.num_state_vars, sv.ctypes.data):
+        if self._f("set_materials")(self.h, len(problem.materials), mats, problem.num_state_vars, sv.ctypes.data):
             raise ValueError("oracle rejected the materials")
         nb = len(problem.boundaries)
         bcs = (OrcBoundary * max(nb, 1))(*[OrcBoundary(SURFACE[b.surface], b.value, HYDRO_BC[b.hydro_bc])
                                            for b in problem.boundaries])
-        if L.orc_set_boundaries(self.h, nb, bcs):
+        if self._f("set_boundaries")(self.h, nb, bcs):
             raise ValueError("oracle rejected the boundaries")
         self.params = make_params(problem.params)
         if setup:
@@ -119,52 +132,54 @@ class Oracle:
             fills = (OrcFill * max(len(fl), 1))(*[OrcFill(
                 REGION[f.volume], f.mat_id, f.x1, f.x2, f.y1, f.y2, f.z1, f.z2, f.radius1, f.radius2,
                 VELOCITY[f.velocity], f.u, f.v, f.w, f.speed, f.sie, f.den) for f in fl])
-            if L.orc_setup(self.h, len(fl), fills):
+            if self._f("setup")(self.h, len(fl), fills):
                 raise ValueError("oracle setup failed")
-        L.orc_init_time(self.h, C.byref(self.params))
+        self._f("init_time")(self.h, C.byref(self.params))
 
     def _L(self):
         return lib(self.variant)
 
+    def _f(self, name):
+        return getattr(self._L(), self._p + name)
+
     def __del__(self):
         if getattr(self, "h", None):
-            self._L().orc_destroy(self.h)
+            self._f("destroy")(self.h)
             self.h = None
 
     def run_cycles(self, n: int) -> int:
-        return int(self._L().orc_run_cycles(self.h, C.byref(self.params), n))
+        return int(self._f("run_cycles")(self.h, C.byref(self.params), n))
 
     def run_stages(self, n: int) -> int:
-        return int(self._L().orc_run_stages(self.h, C.byref(self.params), n))
+        return int(self._f("run_stages")(self.h, C.byref(self.params), n))
 
     def get(self, which: int) -> np.ndarray:
-        L = self._L()
-        n = L.orc_get(self.h, which, None) if which != ORC_BDY_NODE_MASK else self.nn
+        n = self._f("get")(self.h, which, None) if which != ORC_BDY_NODE_MASK else self.nn
         dt = np.int32 if which == ORC_BDY_NODE_MASK else (np.int64 if which == ORC_ELEM_MAT_ID else np.float64)
         out = np.empty(n, dtype=dt)
-        L.orc_get(self.h, which, out.ctypes.data)
+        self._f("get")(self.h, which, out.ctypes.data)
         return out
 
     def set(self, which: int, arr: np.ndarray) -> None:
         a = np.ascontiguousarray(arr)
-        self._L().orc_set(self.h, which, a.ctypes.data)
+        self._f("set")(self.h, which, a.ctypes.data)
 
     def energy(self):
         ie, ke = C.c_double(), C.c_double()
-        self._L().orc_energy(self.h, C.byref(ie), C.byref(ke))
+        self._f("energy")(self.h, C.byref(ie), C.byref(ke))
         return ie.value, ke.value
 
     def time(self):
         t, dt, gt, cyc = C.c_double(), C.c_double(), C.c_double(), C.c_int64()
-        self._L().orc_time(self.h, C.byref(t), C.byref(dt), C.byref(gt), C.byref(cyc))
+        self._f("time")(self.h, C.byref(t), C.byref(dt), C.byref(gt), C.byref(cyc))
         return t.value, dt.value, gt.value, cyc.value
 
     def state(self) -> dict:
         """The compared fields: bin-1 node coords/vel, elem den/pres/sie/sspd/vol,
         stress, plus both bins, node mass, corner forces and state variables."""
-        nn, ne = self.nn, self.ne
-        x = self.get(ORC_NODE_COORDS).reshape(2, nn, 3)
-        v = self.get(ORC_NODE_VEL).reshape(2, nn, 3)
+        nn, ne, D = self.nn, self.ne, self.dims
+        x = self.get(ORC_NODE_COORDS).reshape(2, nn, D)
+        v = self.get(ORC_NODE_VEL).reshape(2, nn, D)
         sie = self.get(ORC_ELEM_SIE).reshape(2, ne)
         stress = self.get(ORC_ELEM_STRESS).reshape(2, ne, 3, 3)
         return {
@@ -175,7 +190,7 @@ class Oracle:
             "sie0": sie[0].copy(), "sspd": self.get(ORC_ELEM_SSPD), "vol": self.get(ORC_ELEM_VOL),
             "div": self.get(ORC_ELEM_DIV), "mass": self.get(ORC_ELEM_MASS),
             "node_mass": self.get(ORC_NODE_MASS),
-            "corner_force": self.get(ORC_CORNER_FORCE).reshape(ne * 8, 3),
+            "corner_force": self.get(ORC_CORNER_FORCE).reshape(ne * 2 ** D, D),
             "time": self.time()[0],
         }
 
@@ -197,11 +212,12 @@ def reference_available(kind: str = "fierro_ref") -> bool:
     return os.path.exists(os.path.join(REF_DIR, kind))
 
 
-def read_state_dump(path: str) -> dict:
+def read_state_dump(path: str, dims: int = 3) -> dict:
     with open(path, "rb") as f:
         buf = f.read()
     assert buf[:8] == b"FSGHSTAT"
     nn, ne = struct.unpack("<QQ", buf[8:24])
+    D, npe = dims, 2 ** dims
     a = np.frombuffer(buf, dtype="<f8", offset=24)
     pos = 0
 
@@ -212,13 +228,13 @@ def read_state_dump(path: str) -> dict:
         return out.copy()
 
     t = take(1)[0]
-    x = take(2 * nn * 3).reshape(2, nn, 3)
-    v = take(2 * nn * 3).reshape(2, nn, 3)
+    x = take(2 * nn * D).reshape(2, nn, D)
+    v = take(2 * nn * D).reshape(2, nn, D)
     nm = take(nn)
     den, pres, sspd = take(ne), take(ne), take(ne)
     sie = take(2 * ne).reshape(2, ne)
     vol, div, mass = take(ne), take(ne), take(ne)
-    cf = take(8 * ne * 3).reshape(8 * ne, 3)
+    cf = take(npe * ne * D).reshape(npe * ne, D)
     out = {"coords": x[1], "vel": v[1], "coords0": x[0], "vel0": v[0], "den": den, "pres": pres,
            "sie": sie[1], "sie0": sie[0], "sspd": sspd, "vol": vol, "div": div, "mass": mass,
            "node_mass": nm, "corner_force": cf, "time": t}
@@ -266,7 +282,7 @@ def run_reference(problem, cycles: int | None = None, kind: str = "fierro_ref", 
                            text=True, env=env, cwd=cwd)
         if p.returncode != 0:
             raise RuntimeError("reference run failed:\n" + p.stdout[-4000:])
-        st = read_state_dump(out)
+        st = read_state_dump(out, prob.mesh.dims)
     ms = re.findall(r"Calculation time in seconds:\s*([0-9.eE+-]+)", p.stdout)
     st["calc_seconds"] = float(ms[-1]) if ms else float("nan")
     m = re.search(r"Setup time in seconds:\s*([0-9.eE+-]+)", p.stdout)

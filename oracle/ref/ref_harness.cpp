@@ -11,9 +11,9 @@
 // usage: fierro_ref <config.txt> <mesh.geo|mesh.bin> <state_out.bin>
 // env FIERRO_REF_WARMUP=W runs W untimed cycles first (see main).
 // The dump (little endian): "FSGHSTAT", u64 num_nodes, u64 num_elems,
-// f64 time_value, then f64 arrays node_coords[2][Nn][3], node_vel[2][Nn][3],
+// f64 time_value, then f64 arrays node_coords[2][Nn][D], node_vel[2][Nn][D],
 // node_mass[Nn], elem_den[Ne], elem_pres[Ne], elem_sspd[Ne], elem_sie[2][Ne],
-// elem_vol[Ne], elem_div[Ne], elem_mass[Ne], corner_force[8Ne][3],
+// elem_vol[Ne], elem_div[Ne], elem_mass[Ne], corner_force[2^D Ne][D] (D = num_dims),
 // elem_stress[2][Ne][3][3], u64 num_state_vars, elem_statev[Ne][num_state_vars].
 #include <chrono>
 #include <cstdint>
@@ -134,8 +134,8 @@ int main(int argc, char* argv[]) {
     std::fwrite("FSGHSTAT", 1, 8, f);
     std::fwrite(hdr, sizeof(uint64_t), 2, f);
     put(f, &time_value, 1);
-    put(f, &node.coords(0, 0, 0), rk_num_bins * num_nodes * 3);
-    put(f, &node.vel(0, 0, 0), rk_num_bins * num_nodes * 3);
+    put(f, &node.coords(0, 0, 0), rk_num_bins * num_nodes * num_dims);
+    put(f, &node.vel(0, 0, 0), rk_num_bins * num_nodes * num_dims);
     put(f, &node.mass(0), num_nodes);
     put(f, &elem.den(0), num_elems);
     put(f, &elem.pres(0), num_elems);
@@ -144,7 +144,7 @@ int main(int argc, char* argv[]) {
     put(f, &elem.vol(0), num_elems);
     put(f, &elem.div(0), num_elems);
     put(f, &elem.mass(0), num_elems);
-    put(f, &corner.force(0, 0), num_corners * 3);
+    put(f, &corner.force(0, 0), num_corners * num_dims);
     put(f, &elem.stress(0, 0, 0, 0), rk_num_bins * num_elems * 9);
     const uint64_t nsv = num_state_vars;
     std::fwrite(&nsv, sizeof(uint64_t), 1, f);

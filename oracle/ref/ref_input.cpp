@@ -4,7 +4,8 @@
 // the reference oracle build (oracle/build_ref.py), never into the library.
 //
 // The problem is read from the text file named by fierro_ref_config_path:
-//   <key> <value>                    scalar controls (dt_start, time_final, ...)
+//   <key> <value>                    scalar controls (dt_start, time_final, ...,
+//                                    num_dims 2 for the 2D-RZ path)
 //   material q1 q1ex q2 q2ex sv0 .. sv{num_state_vars-1}
 //   fill volume mat_id x1 x2 y1 y2 z1 z2 r1 r2 velocity u v w speed sie den
 //   bc surface value hydro_bc
@@ -91,6 +92,7 @@ void input(CArrayKokkos<material_t>& material, CArrayKokkos<mat_fill_t>& mat_fil
     else if (k == "cycle_stop") cycle_stop = (size_t)std::strtoull(t[1].c_str(), nullptr, 10);
     else if (k == "rk_num_stages") rk_num_stages = (size_t)std::strtoull(t[1].c_str(), nullptr, 10);
     else if (k == "num_state_vars") max_num_state_vars = (size_t)std::strtoull(t[1].c_str(), nullptr, 10);
+    else if (k == "num_dims") num_dims = (size_t)std::strtoull(t[1].c_str(), nullptr, 10);
     else if (k == "material") {
       MatRec m{num(t[1]), num(t[2]), num(t[3]), num(t[4]), {}};
       for (size_t i = 5; i < t.size(); ++i) m.sv.push_back(num(t[i]));

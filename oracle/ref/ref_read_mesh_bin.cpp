@@ -4,8 +4,8 @@
 // oracle build; the EnSight build links the reference's own read_mesh.cpp.
 //
 // File layout (little endian): "FSGHMESH", u64 num_nodes, u64 num_elems,
-// f64 x[num_nodes], f64 y[num_nodes], f64 z[num_nodes],
-// u64 nodes_in_elem[num_elems][8] (0-based).
+// f64 x[num_nodes], f64 y[num_nodes], f64 z[num_nodes] (no z for num_dims 2),
+// u64 nodes_in_elem[num_elems][2^num_dims] (0-based).
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -31,17 +31,18 @@ void read_mesh_ensight(char* MESH, mesh_t& mesh, node_t& node, elem_t& elem, cor
   mesh.initialize_nodes(nn);
   node.initialize(rk_num_bins, nn, num_dims);
   double* tmp = (double*)std::malloc(sizeof(double) * nn);
-  for (size_t d = 0; d < 3; ++d) {
+  for (size_t d = 0; d < num_dims; ++d) {
     if (std::fread(tmp, sizeof(double), nn, in) != nn) std::exit(2);
     for (size_t n = 0; n < nn; ++n) node.coords(0, n, d) = tmp[n];
   }
   std::free(tmp);
   mesh.initialize_elems(ne, num_dims);
   elem.initialize(rk_num_bins, nn, 3);  // sized by num_nodes, as read_mesh.cpp:106 does
-  uint64_t* conn = (uint64_t*)std::malloc(sizeof(uint64_t) * ne * 8);
-  if (std::fread(conn, sizeof(uint64_t), ne * 8, in) != ne * 8) std::exit(2);
+  const size_t npe = num_dims == 2 ? 4 : 8;
+  uint64_t* conn = (uint64_t*)std::malloc(sizeof(uint64_t) * ne * npe);
+  if (std::fread(conn, sizeof(uint64_t), ne * npe, in) != ne * npe) std::exit(2);
   for (size_t e = 0; e < ne; ++e)
-    for (size_t l = 0; l < 8; ++l) mesh.nodes_in_elem.host(e, l) = conn[e * 8 + l];
+    for (size_t l = 0; l < npe; ++l) mesh.nodes_in_elem.host(e, l) = conn[e * npe + l];
   std::free(conn);
   mesh.nodes_in_elem.update_device();
   size_t num_corners = ne * mesh.num_nodes_in_elem;

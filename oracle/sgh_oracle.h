@@ -105,6 +105,32 @@ int64_t orc_set(orc_sim* s, int which, const void* in);
 void orc_bmatrix(const double x[8], const double y[8], const double z[8], double B[8][3]);
 double orc_vol_hex(const double x[8], const double y[8], const double z[8]);
 
+/* ---- 2D-RZ (num_dims == 2), oracle/sgh_oracle_rz.c --------------------------
+ * The same calls for quad meshes: coordinates [num_nodes][2] (x axial, y
+ * radial), nodes_in_elem [num_elems][4], and in orc_rz_get / orc_rz_set
+ * node_coords / node_vel [2][Nn][2] and corner_force [4Ne][2].  Materials
+ * accept strength_type 0 and 1 (hyper is refused); boundaries accept x and y
+ * planes and cylinders (fixed); fills refuse the spherical velocity. */
+typedef struct orc_rz orc_rz;
+orc_rz* orc_rz_create(int64_t num_nodes, int64_t num_elems, const int64_t* nodes_in_elem,
+                      const double* coords);
+void orc_rz_destroy(orc_rz* s);
+int orc_rz_set_materials(orc_rz* s, int num_materials, const orc_material* m, int num_state_vars,
+                         const double* state_vars);
+int orc_rz_set_boundaries(orc_rz* s, int num_bcs, const orc_boundary* b);
+int orc_rz_setup(orc_rz* s, int num_fills, const orc_fill* fills);
+void orc_rz_init_time(orc_rz* s, const orc_params* p);
+int64_t orc_rz_run_cycles(orc_rz* s, const orc_params* p, int64_t ncycles);
+int64_t orc_rz_run_stages(orc_rz* s, const orc_params* p, int64_t nstages);
+void orc_rz_energy(const orc_rz* s, double* ie, double* ke);
+void orc_rz_time(const orc_rz* s, double* time_value, double* dt, double* graphics_time, int64_t* cycle);
+int64_t orc_rz_get(const orc_rz* s, int which, void* out);
+int64_t orc_rz_set(orc_rz* s, int which, const void* in);
+void orc_rz_bmatrix(const double x[4], const double y[4], double B[4][2]);
+double orc_rz_vol_quad(const double x[4], const double y[4]);
+double orc_rz_area_quad(const double x[4], const double y[4]);
+void orc_rz_corner_areas(const double x[4], const double y[4], double ca[4]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -8,6 +8,10 @@ and Noh decks of fierro_gb300.problems, and its states after one cycle and after
 the full run are stored as float64 .npz files.  Also stored: checksums of the
 shipped meshes, so the box generator can be checked without the reference tree.
 
+2D-RZ cases (rz_*.npz) run the reference with num_dims = 2 on quad meshes from
+the generator, the decks of the reference's own RZ tests
+(tests-for-Explicit-Lagrange-Kokkos/input_for_{Sedov,Noh}RZ_test.cpp).
+
 Strength-model cases (strength_*.npz) run the reference with the test strength
 model of oracle/ref/ref_user_mat.cpp assigned through material_t::strength_model,
 on meshes from the box generator, and also store the stress bins and the
@@ -48,6 +52,18 @@ def strength_cases():
     }
 
 
+def rz_cases():
+    """The 2D-RZ decks (num_dims 2; also used by the tests, which import this)."""
+    from fierro_gb300 import problems
+    return {
+        "sedov_rz16": problems.sedov_rz(16, cycles=200),
+        "noh_rz16": problems.noh_rz(16, cycles=200),
+        "noh_rz12_jp": problems.noh_rz(12, jitter=0.1, seed=5, permute=True, cycles=80),
+        "sedov_rz12_jp_hypo": problems.with_strength(
+            problems.sedov_rz(12, jitter=0.1, seed=2, permute=True, cycles=60), "hypo", 10.0),
+    }
+
+
 def main():
     from fierro_gb300 import mesh, problems
     from oracle import build_ref, orc
@@ -82,6 +98,16 @@ def main():
         np.savez_compressed(fn, **out)
         meta["strength"][name] = {"file": os.path.basename(fn), "time": float(st["time"]),
                                   "cycles": prob.params.cycle_stop, "deck": prob.config_text()}
+        print(fn, os.path.getsize(fn))
+    meta["rz"] = {}
+    for name, prob in rz_cases().items():
+        st = orc.run_reference(prob, threads=1)
+        out = {k: st[k] for k in FIELDS + STRENGTH_FIELDS + ("node_mass", "mass")}
+        out["time"] = np.array(st["time"])
+        fn = os.path.join(HERE, "rz_%s.npz" % name)
+        np.savez_compressed(fn, **out)
+        meta["rz"][name] = {"file": os.path.basename(fn), "time": float(st["time"]),
+                            "cycles": prob.params.cycle_stop, "deck": prob.config_text()}
         print(fn, os.path.getsize(fn))
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(meta, f, indent=1, sort_keys=True)

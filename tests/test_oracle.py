@@ -147,3 +147,59 @@ def test_oracle_strength_needs_shear_modulus_column(oracle_built):
     prob.num_state_vars = 3
     with pytest.raises(ValueError):
         orc.Oracle(prob)
+
+
+def _rz_cases():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    return mg.rz_cases()
+
+
+@pytest.mark.parametrize("case", ["sedov_rz16", "noh_rz16", "noh_rz12_jp", "sedov_rz12_jp_hypo"])
+def test_oracle_rz_equals_reference_golden(oracle_built, case):
+    """2D-RZ: the C restatement of the num_dims == 2 branches (area-weighted
+    force with hoop terms, RZ volume and divergence, radius-weighted energy,
+    per-stage areal node mass and the axis fix) equals the reference run with
+    num_dims = 2, bit for bit, including node masses and corner forces."""
+    from oracle import orc
+    prob = _rz_cases()[case]
+    meta = json.load(open(os.path.join(GOLDEN, "golden.json")))["rz"][case]
+    assert prob.config_text() == meta["deck"]
+    ref = load_golden("rz_" + case)
+    o = orc.Oracle(prob)
+    o.run_cycles(prob.params.cycle_stop)
+    st = o.state()
+    assert st["time"] == float(ref["time"])
+    assert_bitwise(st, ref, FIELDS + ("corner_force", "div", "node_mass", "mass", "stress", "stress0"), label=case)
+
+
+def test_oracle_rz_energy_conserved(oracle_built):
+    from fierro_gb300 import problems
+    from oracle import orc
+    o = orc.Oracle(problems.sedov_rz(16, cycles=200))
+    ie0, ke0 = o.energy()
+    o.run_cycles(200)
+    ie1, ke1 = o.energy()
+    assert ke1 > 0.1 * ie0
+    assert abs((ie1 + ke1) - (ie0 + ke0)) <= 1e-12 * (ie0 + ke0)
+
+
+def test_oracle_rz_refuses_reference_defects(oracle_built):
+    """Inputs whose 2D branch in the reference reads or writes past an array
+    (hyper strength, spherical velocity fill, z-plane or sphere boundaries) are
+    refused rather than imitated."""
+    from fierro_gb300 import problems
+    from oracle import orc
+    p = problems.with_strength(problems.sedov_rz(4, cycles=2), "hyper", 1.0)
+    with pytest.raises(ValueError):
+        orc.Oracle(p)
+    p = problems.noh_rz(4, cycles=2)
+    p.fills[0].velocity = "spherical"
+    with pytest.raises(ValueError):
+        orc.Oracle(p)
+    p = problems.sedov_rz(4, cycles=2)
+    p.boundaries.append(problems.Boundary("z_plane", 0.0, "reflected"))
+    with pytest.raises(ValueError):
+        orc.Oracle(p)
