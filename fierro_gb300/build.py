@@ -3,6 +3,8 @@
 Translation units:
   csrc/sgh_kernels.cu  twice: exact arithmetic (-DFIERRO_FMA=0 --fmad=false) and
                        fused multiply-add (-DFIERRO_FMA=1 --fmad=true)
+  csrc/sgh_rz_kernels.cu the 2D-RZ quad kernels, twice in the same two modes
+  csrc/sgh_rz.cpp      2D-RZ topology, set-up, transfers and stage launches (g++)
   csrc/sgh_host.cpp    mesh topology, Morton renumbering, set-up (g++, OpenMP,
                        -ffp-contract=off so set-up doubles are uncontracted)
   csrc/sgh_capi.cpp    the C ABI (g++)
@@ -59,11 +61,16 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     if ptxas_info:
         nvcc_common += ["-Xptxas", "-v"]
     kern = os.path.join(CSRC, "sgh_kernels.cu")
+    rzk = os.path.join(CSRC, "sgh_rz_kernels.cu")
     units = [
         (os.path.join(OBJ, "sgh_kernels_exact.o"),
          nvcc_common + ["-DFIERRO_FMA=0", "--fmad=false", "-c", kern], [kern]),
         (os.path.join(OBJ, "sgh_kernels_fma.o"),
          nvcc_common + ["-DFIERRO_FMA=1", "--fmad=true", "-c", kern], [kern]),
+        (os.path.join(OBJ, "sgh_rz_kernels_exact.o"),
+         nvcc_common + ["-DFIERRO_FMA=0", "--fmad=false", "-c", rzk], [rzk]),
+        (os.path.join(OBJ, "sgh_rz_kernels_fma.o"),
+         nvcc_common + ["-DFIERRO_FMA=1", "--fmad=true", "-c", rzk], [rzk]),
     ]
     calib = os.path.join(CSRC, "sgh_calib.cu")
     units.append((os.path.join(OBJ, "sgh_calib.o"), nvcc_common + ["-c", calib], [calib]))
@@ -80,7 +87,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     units.append((os.path.join(OBJ, "sgh_noalloc.o"), nvcc_common + ["-c", noalloc], [noalloc]))
     gxx = ["g++", "-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wall", "-Wno-unknown-pragmas",
            "-I", os.path.join(CUDA_HOME, "include")] + inc
-    for name in ("sgh_host.cpp", "sgh_capi.cpp", "sgh_batch.cpp", "sgh_adjoint.cpp", "sgh_output.cpp"):
+    for name in ("sgh_host.cpp", "sgh_capi.cpp", "sgh_batch.cpp", "sgh_adjoint.cpp", "sgh_output.cpp", "sgh_rz.cpp"):
         src = os.path.join(CSRC, name)
         units.append((os.path.join(OBJ, name.replace(".cpp", ".o")), gxx + ["-c", src], [src]))
     jobs = []

@@ -344,6 +344,7 @@ extern "C" int fierro_adj_forward(fierro_sgh* h, const double* sie0, const doubl
     return set_error(FIERRO_ENOTSUP, "adj_forward: the adjoint differentiates the exact arithmetic mode only");
   if (h->strength)
     return set_error(FIERRO_ENOTSUP, "adj_forward: strength models are user code without a derivative");
+  if (h->dims == 2) return set_error(FIERRO_ENOTSUP, "adj_forward: hex meshes only");
   if (cycles < 1 || ckpt_every < 1 || ckpt_every > (1 << 20))
     return set_error(FIERRO_EINVAL, "adj_forward: need cycles >= 1 and 1 <= ckpt_every <= 2^20");
   const int k = (int)std::min<int64_t>(ckpt_every, cycles);

@@ -255,6 +255,8 @@ int create_impl(fierro_batch* b, const fierro_batch_instance* inst, int64_t n, i
     for (int64_t m = 0; m < I.num_materials; ++m)
       if (I.materials[m].eos_model != 0 || I.materials[m].strength_type != 0)
         return set_error(FIERRO_ENOTSUP, "batch: instance %lld: only ideal gas without strength", (long long)i);
+    if (mesh_dims(&I.mesh) == 2)
+      return set_error(FIERRO_ENOTSUP, "batch: instance %lld is a 2D-RZ mesh (hex meshes only)", (long long)i);
     int rc = build_topology(&I.mesh, I.boundaries, I.num_bcs, true, &b->topo[i]);
     if (rc) {
       std::string msg = fierro_last_error();

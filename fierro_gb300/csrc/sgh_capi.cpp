@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include "sgh_handle.h"
+#include "sgh_rz.h"
 #include "sgh_topo.h"
 #include "sgh_user_mat.cuh"
 
@@ -193,12 +194,20 @@ using namespace fierro::hd;
 
 namespace {
 
-// Stage s of a cycle whose start state is in bin c.
-void enqueue_stage(fierro_sgh* h, int c, int s) {
+// Stage s of a cycle whose start state is in bin c; with `ev`, an event is
+// recorded after each launch.
+int enqueue_stage_ev(fierro_sgh* h, int c, int s, cudaEvent_t* ev, size_t* k) {
+  if (h->dims == 2) return rz::enqueue_stage(h, c, s, ev, k);
   h->ks->force(stage_force_args(h, c, s), h->stream);
+  if (ev) CUDA_TRY(cudaEventRecord(ev[(*k)++], h->stream));
   h->ks->node(node_args(h, c, stage_alpha(h, s)), h->stream);
+  if (ev) CUDA_TRY(cudaEventRecord(ev[(*k)++], h->stream));
   h->ks->elem(stage_elem_args(h, c, s), (s == h->rk_num_stages - 1) ? 1 : 0, h->stream);
+  if (ev) CUDA_TRY(cudaEventRecord(ev[(*k)++], h->stream));
+  return FIERRO_OK;
 }
+
+void enqueue_stage(fierro_sgh* h, int c, int s) { enqueue_stage_ev(h, c, s, nullptr, nullptr); }
 
 void enqueue_dt(fierro_sgh* h) {
   DtArgs d{};
@@ -280,6 +289,8 @@ static int create_impl(fierro_sgh* h, const fierro_mesh* mesh, const fierro_mate
   if (fp_mode != FIERRO_FP_EXACT && fp_mode != FIERRO_FP_FMA)
     return set_error(FIERRO_EINVAL, "fp_mode %d unknown", fp_mode);
   if (num_materials < 1 || !materials) return set_error(FIERRO_EINVAL, "need at least one material");
+  TRY(check_mesh_header(mesh));
+  h->dims = mesh_dims(mesh);
   for (int64_t m = 0; m < num_materials; ++m) {
     if (materials[m].eos_model != 0) return set_error(FIERRO_ENOTSUP, "material %lld: only the ideal-gas EOS", (long long)m);
     if (materials[m].strength_type < 0 || materials[m].strength_type > 2)
@@ -290,8 +301,29 @@ static int create_impl(fierro_sgh* h, const fierro_mesh* mesh, const fierro_mate
   }
   int dev = 0;
   CUDA_TRY(cudaGetDevice(&dev));
-  TRY(check_mesh_header(mesh));
-  TRY(validate_bcs(boundaries, num_bcs));
+  TRY(h->dims == 2 ? validate_bcs_rz(boundaries, num_bcs) : validate_bcs(boundaries, num_bcs));
+  if (h->dims == 2) {
+    h->nn = mesh->num_nodes;
+    h->ne = mesh->num_elems;
+    h->nmat = (int)num_materials;
+    h->fp_mode = fp_mode;
+    h->ks = (fp_mode == FIERRO_FP_EXACT) ? &kernels_exact() : &kernels_fma();
+    h->lp = LoopParams{params->time_final, params->dt_max,  params->dt_min, params->dt_cfl,
+                       params->graphics_dt_ival, params->fuzz, params->small, params->graphics_cyc_ival};
+    h->rk_num_stages = (int)params->rk_num_stages;
+    h->dt_start = params->dt_start;
+    h->tiny = params->tiny;
+    if (stream) {
+      h->stream = static_cast<cudaStream_t>(stream);
+    } else {
+      CUDA_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+      h->own_stream = true;
+    }
+    TRY(rz::create(h, mesh, materials, num_materials, boundaries, num_bcs));
+    TRY(build_graphs(h));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return FIERRO_OK;
+  }
   {
     const char* env = std::getenv("FIERRO_STAGED_TRANSFERS");
     h->direct_host = xfer::direct_host_access() && !(env && env[0] == '1');
@@ -434,7 +466,8 @@ static int finish_set_state(fierro_sgh* h, double time_value, double graphics_ti
   h->enq_cycles = 0;
   h->stage = 0;
   // prime: corner normals, divergence and CFL partials of the uploaded state
-  h->ks->elem(elem_args(h, 0, 0, 1.0, 0), 2, h->stream);
+  if (h->dims == 2) TRY(rz::prime(h));
+  else h->ks->elem(elem_args(h, 0, 0, 1.0, 0), 2, h->stream);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   h->has_state = true;
@@ -477,6 +510,10 @@ static int set_state_impl(fierro_sgh* h, const fierro_sgh_state* s, double time_
   const HostTopo& t = h->topo;
   h->has_state = false;
   TRY(size_statev(h, nsv));
+  if (h->dims == 2) {
+    TRY(rz::set_state(h, s));
+    return finish_set_state(h, time_value, graphics_time, dt);
+  }
   if (h->direct_host) {
     // the GPU reads the caller's arrays and validates them in the same pass
     h->has_state = false;
@@ -590,6 +627,7 @@ extern "C" int fierro_sgh_get_state(fierro_sgh* h, fierro_sgh_state* s) {
   // the divergence the last executed stage used (reference elem_div)
   const long long stages_done = cyc * h->rk_num_stages + h->stage;
   const int qb = stages_done == 0 ? 1 : (int)((stages_done - 1) & 1);
+  if (h->dims == 2) return rz::get_state(h, s, bins, qb);
   if (h->direct_host) {
     // the kernels write the caller's arrays: make their pages resident first
     // (a GPU fault per untouched page costs far more than a host store per page)
@@ -723,14 +761,7 @@ extern "C" int fierro_sgh_run_timed(fierro_sgh* h, int64_t cycles, float* kernel
     const int c = (int)((h->base + h->enq_cycles) & 1);
     enqueue_dt(h);
     CUDA_TRY(cudaEventRecord(ev[k++], h->stream));
-    for (int s = 0; s < h->rk_num_stages; ++s) {
-      h->ks->force(stage_force_args(h, c, s), h->stream);
-      CUDA_TRY(cudaEventRecord(ev[k++], h->stream));
-      h->ks->node(node_args(h, c, stage_alpha(h, s)), h->stream);
-      CUDA_TRY(cudaEventRecord(ev[k++], h->stream));
-      h->ks->elem(stage_elem_args(h, c, s), (s == h->rk_num_stages - 1) ? 1 : 0, h->stream);
-      CUDA_TRY(cudaEventRecord(ev[k++], h->stream));
-    }
+    for (int s = 0; s < h->rk_num_stages; ++s) TRY(enqueue_stage_ev(h, c, s, ev.data(), &k));
     h->ks->end(h->d_ctrl, h->lp, h->stream);
     CUDA_TRY(cudaEventRecord(ev[k++], h->stream));
     h->enq_cycles++;
@@ -772,6 +803,7 @@ extern "C" int fierro_sgh_energy(fierro_sgh* h, double* ie, double* ke) {
   TRY(cycles_done(h, &cyc));
   const int c = bin_now(h, cyc);
   const int b1 = (h->stage == 0) ? c : (c ^ 1);
+  if (h->dims == 2) return rz::energy(h, b1, ie, ke);
   EnergyArgs a{};
   a.ne = (int)h->ne;
   a.nn = (int)h->nn;
@@ -797,6 +829,7 @@ extern "C" int fierro_sgh_device_view(fierro_sgh* h, fierro_device_view* v) {
   clear_error();
   if (!h || !v) return set_error(FIERRO_EINVAL, "handle or view is NULL");
   if (!h->has_state) return set_error(FIERRO_EINVAL, "device_view before set_state");
+  if (h->dims == 2) return set_error(FIERRO_ENOTSUP, "device_view: hex meshes only");
   if (h->stage != 0) return set_error(FIERRO_EINVAL, "device_view in the middle of a cycle");
   long long cyc = 0;
   TRY(cycles_done(h, &cyc));
@@ -829,7 +862,8 @@ extern "C" int fierro_sgh_device_view(fierro_sgh* h, fierro_device_view* v) {
 }
 
 extern "C" int64_t fierro_sgh_launches_per_cycle(const fierro_sgh* h) {
-  return h ? 2 + 3 * (int64_t)h->rk_num_stages : 0;
+  if (!h) return 0;
+  return 2 + (h->dims == 2 ? 4 : 3) * (int64_t)h->rk_num_stages;
 }
 
 extern "C" int64_t fierro_sgh_device_bytes(const fierro_sgh* h) { return h ? (int64_t)h->dev_bytes : 0; }

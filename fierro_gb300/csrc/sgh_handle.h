@@ -31,6 +31,7 @@
 namespace fierro {
 struct AdjState;
 struct OutputState;
+struct RzKernelSet;
 }
 
 struct fierro_sgh {
@@ -92,6 +93,17 @@ struct fierro_sgh {
   double* d_stress[2] = {};
   double* d_statev = nullptr;
   int64_t nsv = 0;
+  // 2D-RZ handles (num_dims == 2, sgh_rz.cpp): quad kernels, the stage-start
+  // radius and extensive mass per node, the boundary nodes for the axis fix
+  int dims = 3;
+  double tiny = 1.0e-12;
+  const fierro::RzKernelSet* rks = nullptr;
+  double* d_rad = nullptr;
+  double* d_node_ext = nullptr;
+  int* d_axis = nullptr;
+  int* d_axis_nin_start = nullptr;
+  int* d_axis_nin = nullptr;
+  int naxis = 0;
 };
 
 namespace fierro {

@@ -18,6 +18,7 @@
 #include "fierro_sgh.h"
 #include "sgh_hex.h"
 #include "sgh_internal.h"
+#include "sgh_rz.h"
 #include "sgh_setup.h"
 
 namespace fierro {
@@ -124,6 +125,8 @@ std::vector<uint64_t> morton_keys(const double* pts, int64_t n) {
 
 }  // namespace
 
+std::vector<int64_t> morton_order(const double* pts, int64_t n) { return radix_order(morton_keys(pts, n)); }
+
 int boundary_masks(const fierro_mesh* mesh, const fierro_boundary* bcs, int64_t num_bcs,
                    const double* coords, std::vector<uint8_t>* mask_ext,
                    std::vector<std::vector<int64_t>>* set_nodes) {
@@ -188,11 +191,14 @@ int boundary_masks(const fierro_mesh* mesh, const fierro_boundary* bcs, int64_t 
 
 int check_mesh_header(const fierro_mesh* m) {
   if (!m) return set_error(FIERRO_EINVAL, "mesh is NULL");
-  if (m->num_nodes < 8 || m->num_elems < 1)
-    return set_error(FIERRO_EINVAL, "mesh needs at least one hex (num_nodes=%lld num_elems=%lld)",
+  if (m->num_dims != 0 && m->num_dims != 2 && m->num_dims != 3)
+    return set_error(FIERRO_EINVAL, "mesh num_dims %lld: 3 (hex) or 2 (2D-RZ quads)", (long long)m->num_dims);
+  const int npe = mesh_dims(m) == 2 ? 4 : 8;
+  if (m->num_nodes < npe || m->num_elems < 1)
+    return set_error(FIERRO_EINVAL, "mesh needs at least one element (num_nodes=%lld num_elems=%lld)",
                      (long long)m->num_nodes, (long long)m->num_elems);
   if (!m->nodes_in_elem || !m->coords) return set_error(FIERRO_EINVAL, "mesh arrays are NULL");
-  if (m->num_elems * 8 >= (int64_t)INT32_MAX || m->num_nodes >= (int64_t)INT32_MAX)
+  if (m->num_elems * npe >= (int64_t)INT32_MAX || m->num_nodes >= (int64_t)INT32_MAX)
     return set_error(FIERRO_EINVAL, "mesh too large for 32-bit device indices");
   return FIERRO_OK;
 }
@@ -338,6 +344,9 @@ extern "C" int fierro_sgh_setup(const fierro_mesh* mesh, const fierro_material* 
   clear_error();
   int rc = check_mesh_header(mesh);
   if (rc) return rc;
+  if (mesh_dims(mesh) == 2)
+    return rz::setup(mesh, materials, num_materials, state_vars, num_state_vars, fills, num_fills, boundaries,
+                     num_bcs, out);
   rc = validate_bcs(boundaries, num_bcs);
   if (rc) return rc;
   if (!out || !out->node_coords || !out->node_vel || !out->node_mass || !out->elem_den || !out->elem_pres ||

@@ -33,10 +33,25 @@ struct HostTopo {
   std::vector<int32_t> eie;
   std::vector<uint8_t> bc_mask;    // [nn] bit d: velocity component d held at zero
   int max_corners_per_node = 0;
+  int npe = 8;                      // nodes per element: 8 hex, 4 quad (2D-RZ)
+  // 2D-RZ: the boundary nodes (mesh.h:592-645) and their edge neighbours
+  // (nodes_in_node, mesh.h:654-796), internal ids, for the axis mass fix
+  std::vector<int32_t> axis_nodes, axis_nin_start, axis_nin;
 };
 
-// Null pointers, sizes and the 32-bit index limit of a mesh (no per-element checks).
+// Indices of n points [n][3] in Morton order (21 bits per axis on the bounding
+// box; a stable sort, so equal keys keep their index order).
+std::vector<int64_t> morton_order(const double* pts, int64_t n);
+
+// The mesh's num_dims: 3 (hex) or 2 (2D-RZ quads); 0 reads as 3.
+inline int mesh_dims(const fierro_mesh* m) { return (m && m->num_dims == 2) ? 2 : 3; }
+
+// Null pointers, num_dims, sizes and the 32-bit index limit of a mesh (no
+// per-element checks).
 int check_mesh_header(const fierro_mesh* mesh);
+// 2D-RZ counterparts (sgh_rz.cpp): boundary deck checks and topology.
+int validate_bcs_rz(const fierro_boundary* bcs, int64_t num_bcs);
+int build_topology_rz(const fierro_mesh* mesh, const fierro_boundary* bcs, int64_t num_bcs, HostTopo* t);
 // Surface tags and condition kinds of a boundary deck.
 int validate_bcs(const fierro_boundary* bcs, int64_t num_bcs);
 

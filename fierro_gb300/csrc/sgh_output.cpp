@@ -355,6 +355,7 @@ extern "C" int fierro_sgh_set_output(fierro_sgh* h, const char* directory, int w
   if (!h) return set_error(FIERRO_EINVAL, "handle is NULL");
   output_release(h);
   if (!directory || what == 0) return fierro::rebuild_graphs(h);
+  if (h->dims == 2) return set_error(FIERRO_ENOTSUP, "set_output: graphics dumps of hex meshes only");
   if ((what & ~(FIERRO_OUTPUT_ENSIGHT | FIERRO_OUTPUT_STATE)) != 0 || slots < 2 || slots > 1024)
     return set_error(FIERRO_EINVAL, "set_output: unknown output kinds or slots outside 2..1024");
   OutputState* o = new (std::nothrow) OutputState();

@@ -58,7 +58,7 @@ class Params(C.Structure):
 
 class Mesh(C.Structure):
     _fields_ = [("num_nodes", C.c_int64), ("num_elems", C.c_int64), ("nodes_in_elem", C.c_void_p),
-                ("coords", C.c_void_p)]
+                ("coords", C.c_void_p), ("num_dims", C.c_int64)]
 
 
 class State(C.Structure):
@@ -137,7 +137,7 @@ def version() -> str:
 def c_mesh(mesh) -> tuple:
     nie = np.ascontiguousarray(mesh.nodes_in_elem, dtype=np.uint64)
     xyz = np.ascontiguousarray(mesh.coords, dtype=np.float64)
-    m = Mesh(mesh.num_nodes, mesh.num_elems, nie.ctypes.data, xyz.ctypes.data)
+    m = Mesh(mesh.num_nodes, mesh.num_elems, nie.ctypes.data, xyz.ctypes.data, mesh.dims)
     return m, (nie, xyz)
 
 
@@ -165,14 +165,16 @@ def c_params(problem: Problem) -> Params:
                   p.graphics_cyc_ival, p.cycle_stop, p.rk_num_stages, p.fuzz, p.tiny, p.small)
 
 
-def empty_state(nn: int, ne: int, nsv: int = 6, pinned: bool = False) -> Dict[str, np.ndarray]:
-    """Host arrays for one state in the reference layouts."""
+def empty_state(nn: int, ne: int, nsv: int = 6, pinned: bool = False, dims: int = 3) -> Dict[str, np.ndarray]:
+    """Host arrays for one state in the reference layouts (dims 2: the 2D-RZ
+    layouts with two components per node and four corners per element)."""
+    D, npe = dims, 2 ** dims
     return {
-        "node_coords": np.zeros((2, nn, 3)), "node_vel": np.zeros((2, nn, 3)), "node_mass": np.zeros(nn),
+        "node_coords": np.zeros((2, nn, D)), "node_vel": np.zeros((2, nn, D)), "node_mass": np.zeros(nn),
         "elem_den": np.zeros(ne), "elem_pres": np.zeros(ne), "elem_stress": np.zeros((2, ne, 3, 3)),
         "elem_sspd": np.zeros(ne), "elem_sie": np.zeros((2, ne)), "elem_vol": np.zeros(ne),
         "elem_div": np.zeros(ne), "elem_mass": np.zeros(ne), "elem_mat_id": np.zeros(ne, dtype=np.uint64),
-        "elem_statev": np.zeros((ne, nsv)), "corner_force": np.zeros((8 * ne, 3)),
+        "elem_statev": np.zeros((ne, nsv)), "corner_force": np.zeros((npe * ne, D)),
     }
 
 
@@ -190,7 +192,8 @@ def c_state(st: Dict[str, np.ndarray]) -> State:
 def setup(problem: Problem) -> Dict[str, np.ndarray]:
     """setup (setup.cpp:10-424) on the host: the initial state of a problem deck."""
     m, keep = c_mesh(problem.mesh)
-    st = empty_state(problem.mesh.num_nodes, problem.mesh.num_elems, problem.num_state_vars)
+    st = empty_state(problem.mesh.num_nodes, problem.mesh.num_elems, problem.num_state_vars,
+                     dims=problem.mesh.dims)
     sv = np.ascontiguousarray(problem.state_vars())
     _check(_lib.fierro_sgh_setup(C.byref(m), c_materials(problem), len(problem.materials), sv.ctypes.data,
                                  problem.num_state_vars, c_fills(problem), len(problem.fills),
@@ -251,7 +254,7 @@ class SGHSolver:
 
     def get_state(self, st: Optional[Dict[str, np.ndarray]] = None) -> Dict[str, np.ndarray]:
         if st is None:
-            st = empty_state(self.nn, self.ne, self.nsv)
+            st = empty_state(self.nn, self.ne, self.nsv, dims=self.problem.mesh.dims)
         _check(_lib.fierro_sgh_get_state(self.h, C.byref(c_state(st))))
         return st
 
@@ -272,7 +275,9 @@ class SGHSolver:
 
     def launch_names(self):
         S = self.problem.params.rk_num_stages
-        return ["k_dt"] + [n for s in range(S) for n in ("k_force", "k_node", "k_elem")] + ["k_end"]
+        stage = ("k_force", "k_node", "k_axis", "k_elem") if self.problem.mesh.dims == 2 else \
+            ("k_force", "k_node", "k_elem")
+        return ["k_dt"] + [n for s in range(S) for n in stage] + ["k_end"]
 
     def enqueue(self, cycles: int):
         _check(_lib.fierro_sgh_enqueue_cycles(self.h, cycles))

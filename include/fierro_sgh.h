@@ -91,12 +91,23 @@ typedef struct {
 } fierro_sgh_params;
 
 /* Mesh: num_nodes, num_elems and nodes_in_elem (mesh_t, mesh.h:68-817) plus the
- * initial coordinates [num_nodes][3] (node_coords bin 1 after read_mesh_ensight). */
+ * initial coordinates (node_coords bin 1 after read_mesh_ensight) and
+ * mesh_t::num_dims.  num_dims 3 (or 0): hexes, nodes_in_elem [Ne][8], coords
+ * [Nn][3].  num_dims 2: the 2D-RZ (axisymmetric) path, quads nodes_in_elem
+ * [Ne][4] counter-clockwise, coords [Nn][2] = (x axial, y radial); the state
+ * arrays then hold 2 components per node (node_coords, node_vel [2][Nn][2],
+ * corner_force [4Ne][2]).  On the 2D-RZ path: boundary surfaces x-plane,
+ * y-plane and cylinder (the reference's z-plane and sphere read a third
+ * coordinate 2D arrays do not have); no hyper strength models (update_state2D,
+ * properties.cpp:146-160, writes 3D normals into a 2D array); no spherical
+ * velocity fill (setup.cpp:272-296 reads a third coordinate); state transfers
+ * through the host; no graphics dumps, adjoint, batch or device view. */
 typedef struct {
   int64_t num_nodes;
   int64_t num_elems;
   const uint64_t* nodes_in_elem;
   const double* coords;
+  int64_t num_dims;
 } fierro_mesh;
 
 /* Host state in the reference layouts (see top of file).  For set_state the

@@ -147,3 +147,34 @@ def test_handle_without_gpu_reports_error(lib_built):
     with pytest.raises(sgh.FierroError) as ei:
         sgh.SGHSolver(_deck())
     assert ei.value.code in (sgh.FIERRO_ECUDA, sgh.FIERRO_ENOMEM)
+
+
+@pytest.mark.parametrize("case", ["sedov_rz12", "noh_rz10_jp"])
+def test_rz_setup_matches_oracle(lib_built, oracle_built, case):
+    """setup with num_dims == 2: RZ volumes, fills, radial velocities, boundary
+    conditions and the areal node masses from Barlow's corner areas equal the
+    2D-RZ restatement bit for bit."""
+    from fierro_gb300 import problems, sgh
+    from oracle import orc
+    prob = {"sedov_rz12": lambda: problems.sedov_rz(12),
+            "noh_rz10_jp": lambda: problems.noh_rz(10, jitter=0.1, seed=4, permute=True)}[case]()
+    st = sgh.setup(prob)
+    ref = orc.Oracle(prob).state()
+    got = {"coords": st["node_coords"][1], "vel": st["node_vel"][1], "den": st["elem_den"],
+           "pres": st["elem_pres"], "sie": st["elem_sie"][1], "sspd": st["elem_sspd"], "vol": st["elem_vol"],
+           "mass": st["elem_mass"], "node_mass": st["node_mass"], "coords0": st["node_coords"][0]}
+    assert_bitwise(got, ref, list(got), label=case)
+
+
+def test_rz_setup_rejects_reference_defects(lib_built):
+    from fierro_gb300 import problems, sgh
+    p = problems.noh_rz(4)
+    p.fills[0].velocity = "spherical"
+    with pytest.raises(sgh.FierroError) as ei:
+        sgh.setup(p)
+    assert ei.value.code == sgh.FIERRO_ENOTSUP
+    p = problems.sedov_rz(4)
+    p.boundaries.append(problems.Boundary("z_plane", 0.0, "reflected"))
+    with pytest.raises(sgh.FierroError) as ei:
+        sgh.setup(p)
+    assert ei.value.code == sgh.FIERRO_EINVAL

@@ -1,0 +1,136 @@
+"""2D-RZ (num_dims == 2) on the GPU: the quad kernels against the 2D-RZ
+restatement (bit for bit in exact mode) and against the reference's own runs
+(tests/golden/rz_*.npz, made with num_dims = 2 on the decks of the reference's
+RZ tests), energy conservation, the FMA mode, the hypo strength hook in RZ and
+the refusals of inputs the reference's 2D branch mishandles."""
+import importlib.util
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, assert_bitwise, assert_fields, load_golden
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("coords", "vel", "den", "pres", "sie", "sspd", "vol")
+EXTRA = ("corner_force", "div", "node_mass", "coords0", "vel0", "sie0", "stress", "stress0")
+CASES = ("sedov_rz16", "noh_rz16", "noh_rz12_jp", "sedov_rz12_jp_hypo")
+
+
+def _cases():
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    return mg.rz_cases()
+
+
+def _gpu(prob, cycles=None, stages=None, mode=0):
+    from fierro_gb300 import sgh
+    st = sgh.setup(prob)
+    with sgh.SGHSolver(prob, fp_mode=mode) as s:
+        s.set_state(st)
+        if stages is not None:
+            s.run_stages(stages)
+        else:
+            s.run(cycles)
+        out = s.get_state()
+        t = s.time()
+        en = s.energy()
+    return {"coords": out["node_coords"][1], "vel": out["node_vel"][1], "coords0": out["node_coords"][0],
+            "vel0": out["node_vel"][0], "den": out["elem_den"], "pres": out["elem_pres"],
+            "sie": out["elem_sie"][1], "sie0": out["elem_sie"][0], "sspd": out["elem_sspd"],
+            "vol": out["elem_vol"], "corner_force": out["corner_force"], "div": out["elem_div"],
+            "node_mass": out["node_mass"], "mass": out["elem_mass"], "stress": out["elem_stress"][1],
+            "stress0": out["elem_stress"][0], "time": t[0], "energy": en}
+
+
+def _oracle(prob, cycles=None, stages=None, variant="crpow"):
+    from oracle import orc
+    o = orc.Oracle(prob, variant=variant)
+    if stages is not None:
+        o.run_stages(stages)
+    else:
+        o.run_cycles(cycles)
+    st = o.state()
+    st["energy"] = o.energy()
+    return st
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("stages", [1, 2, 3])
+def test_rz_exact_bitwise_stages(oracle_built, lib_built, case, stages):
+    """After 1, 2 and 3 RK stages every field, both bins, the corner forces, the
+    divergence and the per-stage areal node masses (axis fix included) are
+    bit-identical to the restatement."""
+    prob = _cases()[case]
+    g = _gpu(prob, stages=stages)
+    r = _oracle(prob, stages=stages)
+    assert_bitwise(g, r, FIELDS + EXTRA, label="%s %d stages" % (case, stages))
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_rz_exact_bitwise_full_run(oracle_built, lib_built, case):
+    prob = _cases()[case]
+    g = _gpu(prob, cycles=prob.params.cycle_stop)
+    r = _oracle(prob, cycles=prob.params.cycle_stop)
+    assert g["time"] == r["time"]
+    assert_bitwise(g, r, FIELDS + EXTRA, label=case)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_rz_exact_vs_reference_golden(lib_built, case):
+    prob = _cases()[case]
+    ref = load_golden("rz_" + case)
+    g = _gpu(prob, cycles=prob.params.cycle_stop)
+    assert g["time"] == float(ref["time"])
+    assert_fields(g, ref, 1e-12, keys=FIELDS + ("node_mass",), label=case)
+
+
+def test_rz_energy_conserved(oracle_built, lib_built):
+    """IE + KE (KE = 1/2 sum m y |v|^2, sgh_solve.cpp:73-101) is conserved over
+    200 cycles of RZ Sedov, and the GPU tallies equal the restatement's."""
+    from fierro_gb300 import problems, sgh
+    prob = problems.sedov_rz(24, cycles=200)
+    st = sgh.setup(prob)
+    with sgh.SGHSolver(prob) as s:
+        s.set_state(st)
+        ie0, ke0 = s.energy()
+        s.run(200)
+        ie1, ke1 = s.energy()
+    assert ke1 > 0.1 * ie0
+    assert abs((ie1 + ke1) - (ie0 + ke0)) <= 1e-12 * (ie0 + ke0)
+    r = _oracle(prob, cycles=200)
+    assert abs(ie1 - r["energy"][0]) <= 1e-13 * ie0 and abs(ke1 - r["energy"][1]) <= 1e-13 * ie0
+
+
+def test_rz_fma_mode_within_tolerance(oracle_built, lib_built):
+    prob = _cases()["noh_rz12_jp"]
+    g = _gpu(prob, cycles=prob.params.cycle_stop, mode=1)
+    r = _oracle(prob, cycles=prob.params.cycle_stop)
+    assert_fields(g, r, 1e-9, keys=FIELDS + ("node_mass",), label="fma noh_rz12_jp")
+
+
+def test_rz_timed_launches(lib_built):
+    from fierro_gb300 import problems, sgh
+    prob = problems.noh_rz(16, cycles=10)
+    with sgh.SGHSolver(prob) as s:
+        s.set_state(sgh.setup(prob))
+        assert s.launches_per_cycle == 2 + 4 * prob.params.rk_num_stages
+        ran, total, kms = s.run_timed(3)
+        assert ran == 3 and total > 0 and len(kms) == len(s.launch_names())
+
+
+def test_rz_refusals(lib_built):
+    from fierro_gb300 import problems, sgh
+    p = problems.with_strength(problems.sedov_rz(4, cycles=2), "hyper", 1.0)
+    with pytest.raises(sgh.FierroError) as ei:
+        sgh.SGHSolver(p)
+    assert ei.value.code == sgh.FIERRO_ENOTSUP
+    p = problems.sedov_rz(6, cycles=2)
+    with sgh.SGHSolver(p) as s:
+        s.set_state(sgh.setup(p))
+        for call in (lambda: s.device_view(), lambda: s.set_output("/tmp"), lambda: s.adj_forward(cycles=1)):
+            with pytest.raises(sgh.FierroError) as ei:
+                call()
+            assert ei.value.code == sgh.FIERRO_ENOTSUP
