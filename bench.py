@@ -60,6 +60,10 @@ def parse(argv=None):
                     help="strength-model run: the workload with the shipped hypo-elastic model as a hypo or "
                          "hyper model on every element, against the same problem without strength")
     ap.add_argument("--shear-modulus", type=float, default=1.0)
+    ap.add_argument("--rz", action="store_true",
+                    help="2D-RZ run: jittered, permuted RZ Sedov on an n x n quad mesh (--rz-n)")
+    ap.add_argument("--rz-n", type=int, default=4096)
+    ap.add_argument("--rz-cpu-n", type=int, default=1024)
     return ap.parse_args(argv)
 
 
@@ -690,8 +694,99 @@ def strength_bench(args):
     print(json.dumps(line))
 
 
+def rz_alg_bytes(kind: str, nn: int, ne: int, nnz: int) -> float:
+    """Compulsory HBM bytes of one launch of each 2D-RZ kernel (FP64 state, int32
+    connectivity, every array touched counted once, gathers at perfect reuse)."""
+    if kind == "k_force":
+        return ne * (16 + 40 + 4 + 4 + 64) + 4 * nnz + nn * 32
+    if kind == "k_node":
+        return nn * (4 + 8 + 8 + 1 + 32 + 8 + 32 + 24 + 8) + ne * (16 + 64)
+    if kind == "k_elem":
+        return ne * (16 + 64 + 8 + 8 + 8 + 16 + 40) + nn * 56
+    return 0.0
+
+
+def rz_bench(args):
+    """The 2D-RZ path at scale: RZ Sedov (the deck of the reference's RZ test:
+    gamma 5/3, energy 0.49339 in the origin sphere of radius 1.2/64, the test's
+    source on its 64 x 64 mesh, four reflecting planes) on an n x n quad mesh of
+    [0,1.2]^2 with interior nodes jittered by U(-0.1h, 0.1h) and element and node
+    ids permuted from the seed, exact mode, per-launch CUDA events; the reference
+    CPU solver with num_dims = 2 on a bounded sample."""
+    import torch
+    from fierro_gb300 import problems, sgh
+    from oracle import build_ref, orc
+    torch.cuda.set_device(0)
+    mode = sgh.FP_EXACT if args.fp_mode == "exact" else sgh.FP_FMA
+    t0 = time.time()
+    prob = problems.sedov_rz(args.rz_n, jitter=0.1, seed=args.seed, permute=True, cycles=10 ** 9,
+                             source_radius=1.2 / 64)
+    st = sgh.setup(prob)
+    nn, ne = prob.mesh.num_nodes, prob.mesh.num_elems
+    with sgh.SGHSolver(prob, fp_mode=mode) as s:
+        s.set_state(st)
+        t_setup = time.time() - t0
+        s.run(args.warmup)
+        clocks = ClockSampler(0)
+        clocks.start()
+        ran, total_ms, kms = s.run_timed(args.steps)
+        ck = clocks.stop()
+        if ran != args.steps:
+            raise RuntimeError("only %d of %d cycles ran" % (ran, args.steps))
+        names = s.launch_names()
+        per = {}
+        for nm, ms in zip(names, kms):
+            per[nm] = per.get(nm, 0.0) + ms
+        launches = {nm: names.count(nm) * args.steps for nm in set(names)}
+        dev_bytes = s.device_bytes
+        launches_total = int(s.launches_per_cycle * args.steps)
+        ie, ke = s.energy()
+    nnz = 8 * ne  # a quad's node-sharing neighbours: 8 inside the mesh
+    dom = max(("k_force", "k_node", "k_elem"), key=lambda k: per[k])
+    dom_ms = per[dom] / launches[dom]
+    ab = rz_alg_bytes(dom, nn, ne, nnz)
+    hbm_peak, peak_kind = measure_peaks()
+    cpu = None
+    if not args.no_cpu_baseline:
+        try:
+            if not orc.reference_available("fierro_ref_fast"):
+                build_ref.build_reference()
+            sample = problems.sedov_rz(args.rz_cpu_n, jitter=0.1, seed=args.seed, permute=True,
+                                       source_radius=1.2 / 64)
+            cores = os.cpu_count() or 1
+            r = orc.run_reference(sample, cycles=args.cpu_cycles, kind="fierro_ref_fast", threads=cores, warmup=1)
+            cpu = {"value": sample.mesh.num_elems * args.cpu_cycles / r["calc_seconds"], "unit": UNIT, "cores": cores,
+                   "kind": "reference",
+                   "sample": "%d^2 jittered permuted RZ Sedov (%d quads), num_dims 2, %d cycles timed by the "
+                             "reference's own cycle-loop timer after 1 warm-up cycle, OMP_NUM_THREADS=%d"
+                             % (args.rz_cpu_n, sample.mesh.num_elems, args.cpu_cycles, cores)}
+        except Exception as exc:
+            cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "reference",
+                   "sample": "unavailable: " + str(exc).splitlines()[0]}
+    line = {"metric": "SGH element-cycles/s, 2D-RZ Sedov %d^2 quads, FP64 RK2" % args.rz_n,
+            "value": ne * args.steps / (total_ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "sedov_rz_%d^2_jitter0.1_permuted" % args.rz_n, "elements": ne, "nodes": nn,
+                       "source_radius": 1.2 / 64,
+                       "gamma": 5.0 / 3.0, "energy": 0.49339, "cfl": 0.4, "rk_stages": 2, "seed": args.seed,
+                       "fp_mode": args.fp_mode, "num_dims": 2,
+                       "l2": "inputs larger than L2 (device state %.1f GB vs 129 MB L2)" % (dev_bytes / 1e9)},
+            "gpu_launches": launches_total,
+            "kernels": {nm: {"launches": launches[nm], "ms": per[nm], "share": per[nm] / total_ms} for nm in per},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": ab / (dom_ms * 1e-3) / 1e9, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": ab / (dom_ms * 1e-3) / 1e9 / hbm_peak, "traffic": None,
+                         "peak_kind": peak_kind, "alg_bytes_per_launch": ab, "avg_launch_ms": dom_ms},
+            "energy": {"ie": ie, "ke": ke},
+            "cpu_baseline": cpu, "clocks": ck, "setup_seconds": t_setup, "device_bytes": dev_bytes}
+    print(json.dumps(line))
+
+
 def main(argv=None):
     args = parse(argv)
+    if args.rz:
+        rz_bench(args)
+        return
     if args.strength:
         strength_bench(args)
         return

@@ -76,7 +76,8 @@ void boundary_rz(const fierro_mesh* mesh, const fierro_boundary* bcs, int64_t nu
                  std::vector<uint8_t>* mask, std::vector<char>* on_bdy) {
   const int64_t nn = mesh->num_nodes, ne = mesh->num_elems;
   const uint64_t* nie = mesh->nodes_in_elem;
-  std::vector<int64_t> edges;  // e*4 + p of the boundary edges
+  std::vector<char> bdy_edge((size_t)ne * 4, 0);
+#pragma omp parallel for schedule(static)
   for (int64_t e = 0; e < ne; ++e)
     for (int p = 0; p < 4; ++p) {
       const uint64_t a = nie[e * 4 + kEdge[p][0]], b = nie[e * 4 + kEdge[p][1]];
@@ -85,8 +86,11 @@ void boundary_rz(const fierro_mesh* mesh, const fierro_boundary* bcs, int64_t nu
         const int64_t o = corners[k] / 4;
         if (o != e && elem_has_node(nie, o, b)) shared = true;
       }
-      if (!shared) edges.push_back(e * 4 + p);
+      bdy_edge[e * 4 + p] = !shared;
     }
+  std::vector<int64_t> edges;  // e*4 + p of the boundary edges
+  for (int64_t i = 0; i < ne * 4; ++i)
+    if (bdy_edge[i]) edges.push_back(i);
   mask->assign((size_t)nn, 0);
   on_bdy->assign((size_t)nn, 0);
   for (int64_t pe : edges) {
@@ -194,6 +198,7 @@ int build_topology_rz(const fierro_mesh* mesh, const fierro_boundary* bcs, int64
   for (int64_t i = 0; i < ne; ++i) t->elem_ext2int[t->elem_int2ext[i]] = i;
   for (int64_t i = 0; i < nn; ++i) t->node_ext2int[t->node_int2ext[i]] = i;
   t->nie.resize((size_t)ne * 4);
+#pragma omp parallel for schedule(static)
   for (int64_t e = 0; e < ne; ++e)
     for (int l = 0; l < 4; ++l) t->nie[e * 4 + l] = (int32_t)t->node_ext2int[nie[t->elem_int2ext[e] * 4 + l]];
   // ---- corner CSR per internal node, in ascending external element id
@@ -213,10 +218,7 @@ int build_topology_rz(const fierro_mesh* mesh, const fierro_boundary* bcs, int64
     }
   }
   // ---- neighbours: every other element sharing a node (mesh.h:249-338)
-  t->eie_start.assign((size_t)ne + 1, 0);
-  t->eie.clear();
-  for (int64_t e = 0; e < ne; ++e) {
-    int32_t buf[64];
+  auto neighbours = [&](int64_t e, int32_t* out) -> int {
     int k = 0;
     for (int l = 0; l < 4; ++l) {
       const int32_t n = t->nie[e * 4 + l];
@@ -225,13 +227,23 @@ int build_topology_rz(const fierro_mesh* mesh, const fierro_boundary* bcs, int64
         if (o == e) continue;
         bool seen = false;
         for (int i = 0; i < k; ++i)
-          if (buf[i] == o) seen = true;
-        if (!seen && k < 64) buf[k++] = o;
+          if (out[i] == o) seen = true;
+        if (!seen && k < 64) out[k++] = o;
       }
     }
-    t->eie.insert(t->eie.end(), buf, buf + k);
-    t->eie_start[e + 1] = (int32_t)t->eie.size();
+    return k;
+  };
+  std::vector<int32_t> cnt((size_t)ne);
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < ne; ++e) {
+    int32_t buf[64];
+    cnt[e] = neighbours(e, buf);
   }
+  t->eie_start.assign((size_t)ne + 1, 0);
+  for (int64_t e = 0; e < ne; ++e) t->eie_start[e + 1] = t->eie_start[e] + cnt[e];
+  t->eie.resize((size_t)t->eie_start[ne]);
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < ne; ++e) neighbours(e, t->eie.data() + t->eie_start[e]);
   // ---- boundary masks, boundary nodes and their edge neighbours
   std::vector<uint8_t> mask;
   std::vector<char> on_bdy;
@@ -653,6 +665,7 @@ int setup(const fierro_mesh* mesh, const fierro_material* materials, int64_t num
     }
   };
   // get_vol (geometry.cpp:238-251)
+#pragma omp parallel for schedule(static)
   for (int64_t e = 0; e < ne; ++e) {
     double x[4], y[4];
     gather(e, x, y);
@@ -671,6 +684,7 @@ int setup(const fierro_mesh* mesh, const fierro_material* materials, int64_t num
   // fills (setup.cpp:109-357) with the 2D centroid (z = 0)
   for (int64_t fi = 0; fi < num_fills; ++fi) {
     const fierro_mat_fill& F = fills[fi];
+#pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < ne; ++e) {
       double ec[3] = {0.0, 0.0, 0.0};
       for (int l = 0; l < 4; ++l) {
@@ -747,12 +761,14 @@ int setup(const fierro_mesh* mesh, const fierro_material* materials, int64_t num
   // corner masses from Barlow's corner areas, node mass summed in corner order
   // (setup.cpp:365-420)
   std::vector<double> cmass((size_t)ne * 4);
+#pragma omp parallel for schedule(static)
   for (int64_t e = 0; e < ne; ++e) {
     double x[4], y[4], ca[4];
     gather(e, x, y);
     corner_areas(x, y, ca);
     for (int l = 0; l < 4; ++l) cmass[e * 4 + l] = ca[l] * out->elem_den[e];
   }
+#pragma omp parallel for schedule(static)
   for (int64_t n = 0; n < nn; ++n) {
     double m = 0.0;
     for (int64_t k = start[n]; k < start[n + 1]; ++k) m += cmass[corners[k]];

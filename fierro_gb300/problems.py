@@ -218,15 +218,16 @@ def sedov_mixed_strength(n: int = 10, shear_modulus: float = 5.0, cycles: int = 
 
 def sedov_rz(n: int = 32, length: float = 1.2, energy: float = 0.49339, gamma: float = 5.0 / 3.0,
              cycles: int = 200, jitter: float = 0.0, seed: int = 0, permute: bool = False,
-             mesh: HexMesh | None = None, cfl: float = 0.4) -> Problem:
+             mesh: HexMesh | None = None, cfl: float = 0.4, source_radius: float | None = None) -> Problem:
     """2D-RZ Sedov blast, the deck of the reference's RZ test
     (tests-for-Explicit-Lagrange-Kokkos/input_for_SedovRZ_test.cpp): n x n quads on
     [0, length]^2 (x axial, y radial), gamma 5/3, rho 1, sie 1e-10, a sphere of
-    radius length/n at the origin holding sie = 0.5 energy / (rho pi r^3), four
-    reflecting planes."""
+    radius r (length/n, as the test's 1.2/64 on its 64 x 64 mesh, unless
+    source_radius is given) at the origin holding sie = 0.5 energy / (rho pi r^3),
+    four reflecting planes."""
     if mesh is None:
         mesh = quad_mesh(n, length=length, jitter=jitter, seed=seed, permute=permute, name="sedov_rz%d" % n)
-    r2 = length / n
+    r2 = length / n if source_radius is None else float(source_radius)
     vol = 3.141592653589793 * (r2 ** 3 - 0.0 ** 3)
     fills = [
         Fill("global", 0, den=1.0, sie=1.0e-10, velocity="cartesian"),
