@@ -99,6 +99,39 @@ __device__ __forceinline__ void rz_corner_areas(const double (&x)[4], const doub
   ca[3] = (5. * A41 + A12 + A23 + 5. * A34) / 12.;
 }
 
+// Without stress the hoop terms are tau(1,0) A_c / r = (+0 A_c) / r and
+// (tau(1,1) - tau(2,2)) A_c / r = ((0 - p) - (0 - p)) A_c / r: exactly +0.0
+// whenever p and the corner area A_c are finite.  A_c is finite unless one of
+// Heron's factors s - a, s - b, s - c of a centroid triangle rounds to zero or
+// below.  For a triangle of area T and semi-perimeter s, each factor is at least
+// T^2 / s^3 (the product of all three is T^2 / s and each is below s), while the
+// computed factors carry an absolute error of about 9 eps s (sides and s to a few
+// ulps each); so T > 3 sqrt(eps) s^2 ~ 3.2e-8 s^2 keeps every computed factor
+// positive.  With s <= P / 2 for the L1 perimeter P, |cross| = 2T > 1e-4 P^2 is
+// sufficient by more than three orders of magnitude, and its own rounding (a few
+// eps P^2) does not matter.  True for all four centroid triangles (and NaN-free
+// coordinates) means the corner areas need not be formed; otherwise they are,
+// as the reference does.
+__device__ __forceinline__ bool rz_corner_areas_finite(const double (&x)[4], const double (&y)[4]) {
+  double rc = 0.0, zc = 0.0;
+#pragma unroll
+  for (int l = 0; l < 4; ++l) {
+    rc = rc + 0.25 * y[l];
+    zc = zc + 0.25 * x[l];
+  }
+  bool ok = true;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int j = (i + 1) & 3;
+    const double d1x = x[i] - zc, d1y = y[i] - rc, d2x = x[j] - zc, d2y = y[j] - rc;
+    const double ex = x[j] - x[i], ey = y[j] - y[i];
+    const double cross = d1x * d2y - d1y * d2x;
+    const double P = fabs(d1x) + fabs(d1y) + fabs(d2x) + fabs(d2y) + fabs(ex) + fabs(ey);
+    ok = ok && (fabs(cross) > 1e-4 * P * P);
+  }
+  return ok;
+}
+
 __device__ __forceinline__ void gather4(const int* nie, int e, int (&nid)[4]) {
   const int4 q = __ldg(reinterpret_cast<const int4*>(nie) + e);
   nid[0] = q.x;
@@ -128,11 +161,12 @@ __global__ void __launch_bounds__(kRzBlock) k_force_rz(const RzForceArgs a) {
     u[l] = __ldg(a.u + nid[l]);
     v[l] = __ldg(a.v + nid[l]);
   }
-  double B[4][2], ca[4];
+  double B[4][2], ca[4] = {0.0, 0.0, 0.0, 0.0};
   rz_bmatrix(x, y, B);
   const double area = rz_area(x, y);
-  rz_corner_areas(x, y, ca);
   const double den = a.den[e], pres = a.pres[e], sspd = a.sspd[e], vol = a.vol[e], div = a.div[e];
+  const bool hoop_zero = !STRENGTH && isfinite(pres) && rz_corner_areas_finite(x, y);
+  if (!hoop_zero) rz_corner_areas(x, y, ca);
   const int mat = a.mat[e];
   const double* q = a.qtab + 4 * mat;
   const bool compress = div < 0;
@@ -223,8 +257,14 @@ __global__ void __launch_bounds__(kRzBlock) k_force_rz(const RzForceArgs a) {
     for (int d = 0; d < 2; ++d) f[d] = a0 * t[d] + a1 * t[3 + d] + pm * (vs[d] - vl[d]);
     const double r = y[l];
     if (r > 1e-14) {
-      f[0] = f[0] + t[3] * ca[l] / r;
-      f[1] = f[1] + (t[4] - t[8]) * ca[l] / r;
+      if (hoop_zero) {
+        // the terms' exact value (+0.0 turns a -0.0 force into +0.0, as adding them does)
+        f[0] = f[0] + 0.0;
+        f[1] = f[1] + 0.0;
+      } else {
+        f[0] = f[0] + t[3] * ca[l] / r;
+        f[1] = f[1] + (t[4] - t[8]) * ca[l] / r;
+      }
     }
     a.force[(size_t)(l * 2 + 0) * ne + e] = f[0];
     a.force[(size_t)(l * 2 + 1) * ne + e] = f[1];

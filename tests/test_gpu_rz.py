@@ -134,3 +134,18 @@ def test_rz_refusals(lib_built):
             with pytest.raises(sgh.FierroError) as ei:
                 call()
             assert ei.value.code == sgh.FIERRO_ENOTSUP
+
+
+@pytest.mark.parametrize("length", [(1.2, 1.2e-4), (1.2e-4, 1.2)])
+def test_rz_hoop_terms_on_thin_elements(oracle_built, lib_built, length):
+    """Quads with an aspect ratio of 5000 fail the corner-area finiteness test of
+    the gas force (|cross| > 1e-4 P^2), so the kernel forms Barlow's corner areas
+    and the hoop terms as the reference writes them; still bit-identical."""
+    from fierro_gb300 import mesh, problems
+    m = mesh.quad_mesh(10, 6, length=length, jitter=0.05, seed=3)
+    prob = problems.noh_rz(mesh=m, cycles=20)
+    prob.params.dt_start, prob.params.dt_min = 1e-9, 1e-12
+    g = _gpu(prob, cycles=20)
+    r = _oracle(prob, cycles=20)
+    assert np.isfinite(r["coords"]).all()
+    assert_bitwise(g, r, FIELDS + EXTRA, label="thin quads %s" % (length,))
