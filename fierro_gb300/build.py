@@ -17,6 +17,7 @@ Translation units:
   csrc/sgh_output.cpp  graphics dumps: snapshot ring, writer thread, reference file formats (g++)
   csrc/sgh_calib.cu    FP64 throughput calibration for the roofline
   csrc/sgh_noalloc.cu  energy tallies with static scratch (no allocation)
+  csrc/sgh_validate.cu device-topology invariant checks (fierro_sgh_validate)
 All compile in parallel; a unit is rebuilt only when it or a header changed.
 """
 from __future__ import annotations
@@ -83,6 +84,8 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     units.append((os.path.join(OBJ, "sgh_xfer.o"), nvcc_common + ["--fmad=false", "-c", xfer], [xfer]))
     adjk = os.path.join(CSRC, "sgh_adjoint.cu")
     units.append((os.path.join(OBJ, "sgh_adjoint_k.o"), nvcc_common + ["--fmad=false", "-c", adjk], [adjk]))
+    val = os.path.join(CSRC, "sgh_validate.cu")
+    units.append((os.path.join(OBJ, "sgh_validate.o"), nvcc_common + ["-c", val], [val]))
     noalloc = os.path.join(CSRC, "sgh_noalloc.cu")
     units.append((os.path.join(OBJ, "sgh_noalloc.o"), nvcc_common + ["-c", noalloc], [noalloc]))
     gxx = ["g++", "-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wall", "-Wno-unknown-pragmas",

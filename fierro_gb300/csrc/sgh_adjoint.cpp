@@ -337,6 +337,7 @@ int upload_seed(fierro_sgh* h, double* dst, const double* src, const std::vector
 extern "C" int fierro_adj_forward(fierro_sgh* h, const double* sie0, const double* gamma, int64_t cycles,
                                   int64_t ckpt_every, int64_t* cycles_run) {
   clear_error();
+  NvtxRange nvtx_("fierro_adj_forward");
   if (cycles_run) *cycles_run = 0;
   if (!h || !h->has_state) return set_error(FIERRO_EINVAL, "adj_forward before set_state");
   if (h->stage != 0) return set_error(FIERRO_EINVAL, "adj_forward: a cycle is partly run");
@@ -387,6 +388,7 @@ extern "C" int fierro_adj_forward(fierro_sgh* h, const double* sie0, const doubl
 extern "C" int fierro_adj_backward(fierro_sgh* h, const fierro_adj_seed* seed, double* sie0_bar, double* gamma_bar,
                                    double* vel0_bar) {
   clear_error();
+  NvtxRange nvtx_("fierro_adj_backward");
   if (!h || !h->adj || !h->adj->have_forward) return set_error(FIERRO_EINVAL, "adj_backward before adj_forward");
   AdjState* a = h->adj;
   long long cyc = 0;

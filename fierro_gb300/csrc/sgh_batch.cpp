@@ -411,6 +411,7 @@ extern "C" int fierro_batch_destroy(fierro_batch* b) {
 extern "C" int fierro_batch_create(const fierro_batch_instance* instances, int64_t num_instances, int fp_mode,
                                    void* stream, fierro_batch** out) {
   clear_error();
+  NvtxRange nvtx_("fierro_batch_create");
   if (!out) return set_error(FIERRO_EINVAL, "out is NULL");
   *out = nullptr;
   fierro_batch* b = new (std::nothrow) fierro_batch();
@@ -481,6 +482,7 @@ extern "C" int fierro_batch_set_state(fierro_batch* b, int64_t i, const fierro_s
 
 extern "C" int fierro_batch_run(fierro_batch* b, int64_t cycles) {
   clear_error();
+  NvtxRange nvtx_("fierro_batch_run");
   if (!b) return set_error(FIERRO_EINVAL, "batch is NULL");
   if (!b->started) {
     for (int64_t i = 0; i < b->n; ++i)

@@ -291,6 +291,10 @@ static int create_impl(fierro_sgh* h, const fierro_mesh* mesh, const fierro_mate
   if (num_materials < 1 || !materials) return set_error(FIERRO_EINVAL, "need at least one material");
   TRY(check_mesh_header(mesh));
   h->dims = mesh_dims(mesh);
+  {
+    const char* env = std::getenv("FIERRO_FAIL_ALLOC_AFTER");
+    h->alloc_limit = env ? std::strtoll(env, nullptr, 10) : -1;
+  }
   for (int64_t m = 0; m < num_materials; ++m) {
     if (materials[m].eos_model != 0) return set_error(FIERRO_ENOTSUP, "material %lld: only the ideal-gas EOS", (long long)m);
     if (materials[m].strength_type < 0 || materials[m].strength_type > 2)
@@ -439,6 +443,7 @@ extern "C" int fierro_sgh_create(const fierro_mesh* mesh, const fierro_material*
                                  const fierro_boundary* boundaries, int64_t num_bcs,
                                  const fierro_sgh_params* params, int fp_mode, void* stream, fierro_sgh** out) {
   clear_error();
+  NvtxRange nvtx_("fierro_sgh_create");
   if (!out) return set_error(FIERRO_EINVAL, "out is NULL");
   *out = nullptr;
   fierro_sgh* h = new (std::nothrow) fierro_sgh();
@@ -593,6 +598,7 @@ static int set_state_impl(fierro_sgh* h, const fierro_sgh_state* s, double time_
 
 extern "C" int fierro_sgh_set_state(fierro_sgh* h, const fierro_sgh_state* s) {
   clear_error();
+  NvtxRange nvtx_("fierro_sgh_set_state");
   if (!h) return set_error(FIERRO_EINVAL, "handle is NULL");
   return set_state_impl(h, s, 0.0, h->lp.graphics_dt_ival, h->dt_start);
 }
@@ -610,6 +616,7 @@ static void populate(double* p, size_t bytes) {
 
 extern "C" int fierro_sgh_get_state(fierro_sgh* h, fierro_sgh_state* s) {
   clear_error();
+  NvtxRange nvtx_("fierro_sgh_get_state");
   if (!h || !s) return set_error(FIERRO_EINVAL, "handle or state is NULL");
   if (!h->has_state) return set_error(FIERRO_EINVAL, "get_state before set_state");
   if (h->strength && s->elem_statev && s->num_state_vars != h->nsv)
@@ -682,6 +689,7 @@ extern "C" int fierro_sgh_get_state(fierro_sgh* h, fierro_sgh_state* s) {
 
 extern "C" int fierro_sgh_enqueue_cycles(fierro_sgh* h, int64_t cycles) {
   clear_error();
+  NvtxRange nvtx_("fierro_sgh_enqueue_cycles");
   if (!h || !h->has_state) return set_error(FIERRO_EINVAL, "enqueue before set_state");
   if (h->stage != 0) return set_error(FIERRO_EINVAL, "a cycle is partly run; finish it with run_stages");
   for (int64_t i = 0; i < cycles; ++i) {
@@ -712,6 +720,7 @@ static int realign(fierro_sgh* h) {
 
 extern "C" int fierro_sgh_run(fierro_sgh* h, int64_t cycles, int64_t* cycles_run) {
   clear_error();
+  NvtxRange nvtx_("fierro_sgh_run");
   if (!h || !h->has_state) return set_error(FIERRO_EINVAL, "run before set_state");
   long long before = 0;
   TRY(realign(h));
@@ -725,6 +734,7 @@ extern "C" int fierro_sgh_run(fierro_sgh* h, int64_t cycles, int64_t* cycles_run
 
 extern "C" int fierro_sgh_run_stages(fierro_sgh* h, int64_t stages) {
   clear_error();
+  NvtxRange nvtx_("fierro_sgh_run_stages");
   if (!h || !h->has_state) return set_error(FIERRO_EINVAL, "run_stages before set_state");
   TRY(realign(h));
   for (int64_t i = 0; i < stages; ++i) {
@@ -747,6 +757,7 @@ extern "C" int fierro_sgh_run_stages(fierro_sgh* h, int64_t stages) {
 extern "C" int fierro_sgh_run_timed(fierro_sgh* h, int64_t cycles, float* kernel_ms, float* total_ms,
                                     int64_t* cycles_run) {
   clear_error();
+  NvtxRange nvtx_("fierro_sgh_run_timed");
   if (!h || !h->has_state) return set_error(FIERRO_EINVAL, "run before set_state");
   if (h->stage != 0) return set_error(FIERRO_EINVAL, "a cycle is partly run; finish it with run_stages");
   TRY(realign(h));
@@ -798,6 +809,7 @@ extern "C" int fierro_sgh_time(fierro_sgh* h, double* time_value, double* dt, do
 
 extern "C" int fierro_sgh_energy(fierro_sgh* h, double* ie, double* ke) {
   clear_error();
+  NvtxRange nvtx_("fierro_sgh_energy");
   if (!h || !h->has_state) return set_error(FIERRO_EINVAL, "energy before set_state");
   long long cyc = 0;
   TRY(cycles_done(h, &cyc));
@@ -875,6 +887,7 @@ extern "C" int fierro_sgh_solve(const fierro_mesh* mesh, const fierro_material* 
                                 int64_t cycle_stop, int64_t rk_num_stages, double dt, double fuzz, double tiny,
                                 double small, int fp_mode, int64_t* cycles_run) {
   clear_error();
+  NvtxRange nvtx_("fierro_sgh_solve");
   if (!time_value || !graphics_time || !state) return set_error(FIERRO_EINVAL, "solve: NULL argument");
   fierro_sgh_params p{time_final, dt_max, dt_min, dt_cfl, dt, graphics_dt_ival, graphics_cyc_ival,
                       cycle_stop, rk_num_stages, fuzz, tiny, small};
@@ -891,4 +904,196 @@ extern "C" int fierro_sgh_solve(const fierro_mesh* mesh, const fierro_material* 
   fierro_sgh_destroy(h);
   if (rc) set_error(rc, "%s", msg.c_str());
   return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Checkpoint / restart: everything the cycle loop carries from one cycle to the
+// next, in the device numbering and bin roles, so a restarted loop continues
+// bit for bit.  The reference has no restart; the nearest it has is calling
+// sgh_solve again from the state the last call left, which restarts dt from
+// dt_start (fierro_sgh_set_state does the same).
+namespace {
+
+struct CkptHeader {
+  char magic[8];
+  uint32_t version, dims;
+  int64_t nn, ne, nsv, nmat, rk_num_stages, fp_mode, strength, topo_hash;
+  int64_t base, ncfl;
+};
+
+struct Block {
+  void* ptr;
+  size_t bytes;
+};
+
+uint64_t fnv1a(uint64_t h, const void* p, size_t n) {
+  const unsigned char* c = static_cast<const unsigned char*>(p);
+  for (size_t i = 0; i < n; ++i) h = (h ^ c[i]) * 1099511628211ULL;
+  return h;
+}
+
+// The device topology's fingerprint: connectivity, corner and neighbour lists
+// and boundary masks in the device numbering.
+uint64_t topo_hash(fierro_sgh* h) {
+  const HostTopo& t = h->topo;
+  uint64_t x = 1469598103934665603ULL;
+  if (!t.nie.empty()) {
+    x = fnv1a(x, t.nie.data(), t.nie.size() * sizeof(int32_t));
+    x = fnv1a(x, t.cin.data(), t.cin.size() * sizeof(int32_t));
+    x = fnv1a(x, t.eie.data(), t.eie.size() * sizeof(int32_t));
+    x = fnv1a(x, t.bc_mask.data(), t.bc_mask.size());
+    return x;
+  }
+  // topology built on the GPU (sgh_topo.cu): hash the device copies
+  const size_t npe = h->dims == 2 ? 4 : 8;
+  std::vector<int32_t> buf;
+  auto add = [&](const int* d, size_t n) {
+    buf.resize(std::max<size_t>(n, 1));
+    if (n) cudaMemcpy(buf.data(), d, n * sizeof(int32_t), cudaMemcpyDeviceToHost);
+    x = fnv1a(x, buf.data(), n * sizeof(int32_t));
+  };
+  add(h->d_nie, (size_t)h->ne * npe);
+  add(h->d_cin, (size_t)h->ne * npe);
+  add(h->d_eie, (size_t)h->nnz_eie);
+  std::vector<unsigned char> bc((size_t)h->nn);
+  cudaMemcpy(bc.data(), h->d_bc, bc.size(), cudaMemcpyDeviceToHost);
+  return fnv1a(x, bc.data(), bc.size());
+}
+
+std::vector<Block> ckpt_blocks(fierro_sgh* h) {
+  const size_t nn = (size_t)h->nn, ne = (size_t)h->ne, D = h->dims == 2 ? 2 : 3, d8 = sizeof(double);
+  std::vector<Block> b;
+  for (int bin = 0; bin < 2; ++bin)
+    for (size_t d = 0; d < D; ++d) {
+      b.push_back({h->d_x[bin][d], nn * d8});
+      b.push_back({h->d_v[bin][d], nn * d8});
+    }
+  for (int bin = 0; bin < 2; ++bin) {
+    b.push_back({h->d_sie[bin], ne * d8});
+    b.push_back({h->d_div[bin], ne * d8});
+  }
+  for (double* p : {h->d_den, h->d_pres, h->d_sspd, h->d_vol, h->d_elem_mass, h->d_gamma, h->d_csmin})
+    b.push_back({p, ne * d8});
+  b.push_back({h->d_mat, ne * sizeof(int)});
+  b.push_back({h->d_node_mass, nn * d8});
+  b.push_back({h->d_force, ne * (h->dims == 2 ? 8 : 24) * d8});
+  b.push_back({h->d_cfl, (size_t)h->ncfl * sizeof(long long)});
+  b.push_back({h->d_ctrl, sizeof(Ctrl)});
+  if (h->dims == 2) b.push_back({h->d_node_ext, nn * d8});
+  else b.push_back({h->d_bmat, ne * 24 * d8});
+  if (h->strength) {
+    b.push_back({h->d_stress[0], ne * 9 * d8});
+    b.push_back({h->d_stress[1], ne * 9 * d8});
+    b.push_back({h->d_statev, ne * (size_t)h->nsv * d8});
+  }
+  return b;
+}
+
+CkptHeader ckpt_header(fierro_sgh* h) {
+  CkptHeader hd{};
+  std::memcpy(hd.magic, "FSGHCKPT", 8);
+  hd.version = 1;
+  hd.dims = (uint32_t)h->dims;
+  hd.nn = h->nn;
+  hd.ne = h->ne;
+  hd.nsv = h->strength ? h->nsv : 0;
+  hd.nmat = h->nmat;
+  hd.rk_num_stages = h->rk_num_stages;
+  hd.fp_mode = h->fp_mode;
+  hd.strength = (h->strength ? 1 : 0) | (h->has_hyper ? 2 : 0);
+  hd.topo_hash = (int64_t)topo_hash(h);
+  hd.base = h->base;
+  hd.ncfl = h->ncfl;
+  return hd;
+}
+
+}  // namespace
+
+extern "C" int fierro_sgh_checkpoint(fierro_sgh* h, const char* path) {
+  clear_error();
+  NvtxRange nvtx_("fierro_sgh_checkpoint");
+  if (!h || !path) return set_error(FIERRO_EINVAL, "checkpoint: handle or path is NULL");
+  if (!h->has_state) return set_error(FIERRO_EINVAL, "checkpoint before set_state");
+  if (h->stage != 0) return set_error(FIERRO_EINVAL, "checkpoint in the middle of a cycle");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  TRY(check_status(h));
+  TRY(realign(h));
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return set_error(FIERRO_EINVAL, "checkpoint: cannot open %s for writing", path);
+  const CkptHeader hd = ckpt_header(h);
+  bool ok = std::fwrite(&hd, sizeof(hd), 1, f) == 1;
+  std::vector<char> buf;
+  for (const Block& b : ckpt_blocks(h)) {
+    if (!ok) break;
+    buf.resize(std::max<size_t>(b.bytes, 1));
+    cudaError_t err = cudaMemcpy(buf.data(), b.ptr, b.bytes, cudaMemcpyDeviceToHost);
+    if (err != cudaSuccess) {
+      std::fclose(f);
+      return set_error(FIERRO_ECUDA, "checkpoint: %s", cudaGetErrorString(err));
+    }
+    ok = std::fwrite(buf.data(), 1, b.bytes, f) == b.bytes;
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) return set_error(FIERRO_EINVAL, "checkpoint: writing %s failed", path);
+  return FIERRO_OK;
+}
+
+extern "C" int fierro_sgh_restart(fierro_sgh* h, const char* path) {
+  clear_error();
+  NvtxRange nvtx_("fierro_sgh_restart");
+  if (!h || !path) return set_error(FIERRO_EINVAL, "restart: handle or path is NULL");
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return set_error(FIERRO_EINVAL, "restart: cannot open %s", path);
+  CkptHeader hd{};
+  if (std::fread(&hd, sizeof(hd), 1, f) != 1 || std::memcmp(hd.magic, "FSGHCKPT", 8) != 0 || hd.version != 1) {
+    std::fclose(f);
+    return set_error(FIERRO_EINVAL, "restart: %s is not a checkpoint of this library", path);
+  }
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  h->has_state = false;
+  if (h->strength && hd.nsv >= kUserStrengthStateVars) {
+    const int rc = size_statev(h, hd.nsv);
+    if (rc) {
+      std::fclose(f);
+      return rc;
+    }
+  }
+  CkptHeader mine = ckpt_header(h);
+  mine.base = hd.base;
+  if (std::memcmp(&mine, &hd, sizeof(hd)) != 0) {
+    std::fclose(f);
+    return set_error(FIERRO_EINVAL, "restart: %s was written by a handle with another mesh, deck or parameters",
+                     path);
+  }
+  if (h->adj) adj_release(h);
+  output_reset(h);
+  std::vector<char> buf;
+  for (const Block& b : ckpt_blocks(h)) {
+    buf.resize(std::max<size_t>(b.bytes, 1));
+    if (std::fread(buf.data(), 1, b.bytes, f) != b.bytes) {
+      std::fclose(f);
+      return set_error(FIERRO_EINVAL, "restart: %s is truncated", path);
+    }
+    cudaError_t err = cudaMemcpy(b.ptr, buf.data(), b.bytes, cudaMemcpyHostToDevice);
+    if (err != cudaSuccess) {
+      std::fclose(f);
+      return set_error(FIERRO_ECUDA, "restart: %s", cudaGetErrorString(err));
+    }
+  }
+  std::fclose(f);
+  h->base = (int)hd.base;
+  h->stage = 0;
+  h->has_state = true;
+  TRY(realign(h));
+  return check_status(h);
+}
+
+extern "C" int fierro_sgh_status(fierro_sgh* h, uint32_t* flags) {
+  clear_error();
+  if (!h || !flags) return set_error(FIERRO_EINVAL, "handle or flags is NULL");
+  Ctrl c;
+  CUDA_TRY(cudaMemcpyAsync(&c, h->d_ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  *flags = c.status;
+  return FIERRO_OK;
 }

@@ -40,6 +40,7 @@ struct Ctrl {
 
 #define FIERRO_STATUS_BAD_VOLUME 1u  // non-positive or non-finite element volume
 #define FIERRO_STATUS_BAD_STATE 2u   // non-finite energy, pressure or velocity
+#define FIERRO_STATUS_DT_FLOOR 4u    // a CFL step fell below dt_min and dt was raised to it (warning)
 
 struct LoopParams {
   double time_final, dt_max, dt_min, dt_cfl, graphics_dt_ival, fuzz, small;

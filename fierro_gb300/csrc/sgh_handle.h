@@ -104,15 +104,24 @@ struct fierro_sgh {
   int* d_axis_nin_start = nullptr;
   int* d_axis_nin = nullptr;
   int naxis = 0;
+  // host-side fault injection: FIERRO_FAIL_ALLOC_AFTER=n makes the handle's
+  // device allocations after the first n fail as if the device were full
+  int64_t alloc_limit = -1;
+  int64_t alloc_count = 0;
 };
 
 namespace fierro {
+
 namespace hd {
 
 template <typename T>
 int dalloc(fierro_sgh* h, T** p, size_t count) {
   void* q = nullptr;
   size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+  if (h->alloc_limit >= 0 && h->alloc_count >= h->alloc_limit)
+    return set_error(FIERRO_ENOMEM, "cudaMalloc(%zu bytes): injected failure after %lld allocations", bytes,
+                     (long long)h->alloc_count);
+  h->alloc_count++;
   cudaError_t err = cudaMalloc(&q, bytes);
   if (err != cudaSuccess)
     return set_error(FIERRO_ENOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(err));

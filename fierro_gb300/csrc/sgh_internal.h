@@ -7,9 +7,20 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "fierro_sgh.h"
 
 namespace fierro {
+
+// An NVTX range around a C-ABI call: the call shows up by name on a profiler's
+// timeline; without an attached tool the push and pop do nothing.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Record an error for fierro_last_error() and return `code`.
 int set_error(int code, const char* fmt, ...);

@@ -440,6 +440,7 @@ __device__ __forceinline__ void dt_update(Ctrl* c, long long k, const LoopParams
   }
   double dt = c->dt * 1.1;
   double min_dt_calc = (k == 0x7FFFFFFFFFFFFFFFLL) ? 1.7976931348623157e308 : okey_decode(k);
+  if (min_dt_calc < lp.dt_min) c->status |= FIERRO_STATUS_DT_FLOOR;
   min_dt_calc = fmin(min_dt_calc, lp.dt_max);
   min_dt_calc = fmax(min_dt_calc, lp.dt_min);
   if (min_dt_calc < dt) dt = min_dt_calc;

@@ -324,6 +324,12 @@ int create(fierro_sgh* h, const fierro_mesh* mesh, const fierro_material* materi
     TRY(upload_raw(h, h->d_stype, st.data(), sizeof(int) * st.size()));
   }
   h->naxis = (int)t.axis_nodes.size();
+  TRY(dalloc(h, &h->d_elem_int2ext, ne));
+  {
+    std::vector<int32_t> m32(ne);
+    for (size_t j = 0; j < ne; ++j) m32[j] = (int32_t)t.elem_int2ext[j];
+    TRY(upload_raw(h, h->d_elem_int2ext, m32.data(), sizeof(int32_t) * ne));
+  }
   TRY(dalloc(h, &h->d_axis, t.axis_nodes.size()));
   TRY(dalloc(h, &h->d_axis_nin_start, t.axis_nin_start.size()));
   TRY(dalloc(h, &h->d_axis_nin, t.axis_nin.size()));

@@ -24,6 +24,7 @@ LIB_PATH = os.path.join(HERE, "libfierro_sgh.so")
 
 FIERRO_OK, FIERRO_EINVAL, FIERRO_ENOMEM, FIERRO_ECUDA, FIERRO_ENUMERIC, FIERRO_ETIMEDOUT, FIERRO_ENOTSUP = range(7)
 FP_EXACT, FP_FMA = 0, 1
+HEALTH_BAD_VOLUME, HEALTH_BAD_STATE, HEALTH_DT_FLOOR = 1, 2, 4
 OUTPUT_ENSIGHT, OUTPUT_STATE = 1, 2
 _ERRNAMES = {1: "EINVAL", 2: "ENOMEM", 3: "ECUDA", 4: "ENUMERIC", 5: "ETIMEDOUT", 6: "ENOTSUP"}
 
@@ -114,6 +115,10 @@ def _load():
     lib.fierro_adj_verify.argtypes = [vp, C.c_int]
     lib.fierro_adj_stats.argtypes = [vp, C.POINTER(i64), i64]
     lib.fierro_adj_release.argtypes = [vp]
+    lib.fierro_sgh_checkpoint.argtypes = [vp, C.c_char_p]
+    lib.fierro_sgh_restart.argtypes = [vp, C.c_char_p]
+    lib.fierro_sgh_validate.argtypes = [vp]
+    lib.fierro_sgh_status.argtypes = [vp, C.POINTER(C.c_uint32)]
     return lib
 
 
@@ -297,6 +302,24 @@ class SGHSolver:
         ie, ke = C.c_double(), C.c_double()
         _check(_lib.fierro_sgh_energy(self.h, C.byref(ie), C.byref(ke)))
         return ie.value, ke.value
+
+    def checkpoint(self, path: str):
+        """fierro_sgh_checkpoint: the loop state at this cycle boundary, to a file."""
+        _check(_lib.fierro_sgh_checkpoint(self.h, os.fsencode(path)))
+
+    def status(self) -> int:
+        """fierro_sgh_status: the run's health word (HEALTH_* bits)."""
+        f = C.c_uint32(0)
+        _check(_lib.fierro_sgh_status(self.h, C.byref(f)))
+        return f.value
+
+    def validate(self):
+        """fierro_sgh_validate: the device topology's invariants, checked on the GPU."""
+        _check(_lib.fierro_sgh_validate(self.h))
+
+    def restart(self, path: str):
+        """fierro_sgh_restart: continue from a checkpoint of the same problem."""
+        _check(_lib.fierro_sgh_restart(self.h, os.fsencode(path)))
 
     @property
     def launches_per_cycle(self) -> int:

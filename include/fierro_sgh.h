@@ -198,6 +198,38 @@ int fierro_sgh_energy(fierro_sgh* h, double* ie, double* ke);
 int fierro_sgh_run_timed(fierro_sgh* h, int64_t cycles, float* kernel_ms, float* total_ms, int64_t* cycles_run);
 /* Number of kernel launches one cycle enqueues (for launch accounting). */
 int64_t fierro_sgh_launches_per_cycle(const fierro_sgh* h);
+
+/* Checkpoint / restart (no counterpart in the reference, which can only call
+ * sgh_solve again from the state it left, restarting dt from dt_start).
+ * fierro_sgh_checkpoint writes, at a cycle boundary, everything the cycle loop
+ * carries into the next cycle (both state bins, the corner normals, divergences
+ * and CFL partial minima the next stage and dt step read, masses, stress and
+ * state variables, the loop scalars) to a file, with a fingerprint of the
+ * device topology.  fierro_sgh_restart loads it into a handle created from the
+ * same mesh, deck and parameters (FIERRO_EINVAL otherwise); the loop then
+ * continues bit for bit as if it had not stopped.  Graphics-dump and adjoint
+ * state are not part of a checkpoint. */
+int fierro_sgh_checkpoint(fierro_sgh* h, const char* path);
+int fierro_sgh_restart(fierro_sgh* h, const char* path);
+
+/* Checks the handle's device topology against the invariants the cycle kernels
+ * rely on (node ids in range and distinct per element; corner lists complete,
+ * each corner once, in the reference's summation order; neighbours share a
+ * node; boundary masks; 2D-RZ axis lists), on the GPU, range-checking every
+ * index before use.  FIERRO_OK, or FIERRO_EINVAL naming the first failing
+ * check.  A stand-in for a memory checker, which is not available here. */
+int fierro_sgh_validate(fierro_sgh* h);
+
+/* Health word of the run since set_state (the device writes it, never traps):
+ * FIERRO_HEALTH_BAD_VOLUME and FIERRO_HEALTH_BAD_STATE also make the run calls
+ * return FIERRO_ENUMERIC; FIERRO_HEALTH_DT_FLOOR is a warning: some element's CFL
+ * step fell below dt_min, and the time step was raised to dt_min as the
+ * reference's clamp does (time_integration.cpp:131-135), so the run may be
+ * unstable. */
+#define FIERRO_HEALTH_BAD_VOLUME 1u
+#define FIERRO_HEALTH_BAD_STATE 2u
+#define FIERRO_HEALTH_DT_FLOOR 4u
+int fierro_sgh_status(fierro_sgh* h, uint32_t* flags);
 /* Bytes of device memory the handle holds. */
 int64_t fierro_sgh_device_bytes(const fierro_sgh* h);
 

@@ -1,0 +1,70 @@
+"""Failure detection without a GPU fault: the device health word, the device
+topology checker, and host-injected allocation failures.  Nothing here traps,
+faults or hangs the GPU: failures are made on the host (an impossible dt floor,
+an allocation budget) and read back as status words and error codes."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_dt_floor_is_reported_not_fatal(lib_built):
+    """With dt_min above every CFL step the reference's clamp raises dt to dt_min
+    (time_integration.cpp:131-135); the run goes on, and the health word says so."""
+    from fierro_gb300 import problems, sgh
+    prob = problems.sedov(8, cycles=5)
+    with sgh.SGHSolver(prob) as s:
+        s.set_state(sgh.setup(prob))
+        s.run(3)
+        assert s.status() == 0
+    prob.params.dt_min = 1e-2
+    prob.params.dt_start = 1e-2
+    with sgh.SGHSolver(prob) as s:
+        s.set_state(sgh.setup(prob))
+        try:
+            s.run(3)
+        except sgh.FierroError:
+            pass  # the oversized steps may invert elements, which is reported separately
+        assert s.status() & sgh.HEALTH_DT_FLOOR
+
+
+def test_inverted_element_sets_bad_volume(lib_built):
+    from fierro_gb300 import problems, sgh
+    prob = problems.sedov(6, cycles=5)
+    st = sgh.setup(prob)
+    st["node_vel"][1][:, 0] = np.where(st["node_coords"][1][:, 0] > 0.5, -1.0e5, 1.0e5)
+    with sgh.SGHSolver(prob) as s:
+        s.set_state(st)
+        with pytest.raises(sgh.FierroError) as ei:
+            s.run(4)
+        assert ei.value.code == sgh.FIERRO_ENUMERIC
+        assert s.status() & sgh.HEALTH_BAD_VOLUME
+
+
+@pytest.mark.parametrize("case", ["sedov10_jp", "sedov10_jp_staged", "noh_rz12_jp", "sedov_rz9"])
+def test_device_topology_invariants(lib_built, monkeypatch, case):
+    from fierro_gb300 import problems, sgh
+    if case.endswith("staged"):
+        monkeypatch.setenv("FIERRO_STAGED_TRANSFERS", "1")
+    prob = {"sedov10_jp": lambda: problems.sedov(10, jitter=0.1, seed=3, permute=True),
+            "sedov10_jp_staged": lambda: problems.sedov(10, jitter=0.1, seed=3, permute=True),
+            "noh_rz12_jp": lambda: problems.noh_rz(12, jitter=0.1, seed=5, permute=True),
+            "sedov_rz9": lambda: problems.sedov_rz(9)}[case]()
+    with sgh.SGHSolver(prob) as s:
+        s.validate()
+
+
+@pytest.mark.parametrize("limit", [0, 1, 7, 20])
+def test_injected_allocation_failure(lib_built, monkeypatch, limit):
+    """Allocation n+1 fails: creation returns FIERRO_ENOMEM and releases what it
+    had; a handle created afterwards runs normally."""
+    from fierro_gb300 import problems, sgh
+    prob = problems.sedov(6, cycles=3)
+    monkeypatch.setenv("FIERRO_FAIL_ALLOC_AFTER", str(limit))
+    with pytest.raises(sgh.FierroError) as ei:
+        sgh.SGHSolver(prob)
+    assert ei.value.code == sgh.FIERRO_ENOMEM and "injected" in str(ei.value)
+    monkeypatch.delenv("FIERRO_FAIL_ALLOC_AFTER")
+    with sgh.SGHSolver(prob) as s:
+        s.set_state(sgh.setup(prob))
+        assert s.run(3) == 3
