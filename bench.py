@@ -60,6 +60,9 @@ def parse(argv=None):
                     help="strength-model run: the workload with the shipped hypo-elastic model as a hypo or "
                          "hyper model on every element, against the same problem without strength")
     ap.add_argument("--shear-modulus", type=float, default=1.0)
+    ap.add_argument("--configs", action="store_true",
+                    help="the small reference decks (Sedov 12^3 for 200 cycles, Noh 32^3 for 500) on the GPU "
+                         "and on the reference CPU solver (all host cores and one)")
     ap.add_argument("--rz", action="store_true",
                     help="2D-RZ run: jittered, permuted RZ Sedov on an n x n quad mesh (--rz-n)")
     ap.add_argument("--rz-n", type=int, default=4096)
@@ -782,8 +785,65 @@ def rz_bench(args):
     print(json.dumps(line))
 
 
+def configs_bench(args):
+    """Sedov 12^3 (200 cycles) and Noh 32^3 (500 cycles, stopping at time_final
+    after 325) on the shipped-mesh geometry: the run as graph replays
+    (fierro_sgh_run, median of three), the same with a CUDA event after every
+    launch, the one-shot fierro_sgh_solve with host buffers, and the reference
+    CPU solver on all host cores and on one (its own cycle-loop timer)."""
+    import torch
+    from fierro_gb300 import problems, sgh
+    from oracle import build_ref, orc
+    torch.cuda.set_device(0)
+    if not orc.reference_available("fierro_ref_fast"):
+        build_ref.build_reference()
+    out = {}
+    for name, prob in (("sedov12", problems.sedov(12, geo_digits=5)), ("noh32", problems.noh(32, geo_digits=5))):
+        cyc = prob.params.cycle_stop
+        ne = prob.mesh.num_elems
+        st = sgh.setup(prob)
+        with sgh.SGHSolver(prob) as s:
+            s.set_state(st)
+            s.run(3)
+            s.set_state(st)
+            ran, total_ms, _ = s.run_timed(cyc)
+            # the same run as graph replays (what fierro_sgh_run does), timed around
+            # the synchronised call; per-launch events above cost host time per launch
+            reps = []
+            for _ in range(3):
+                s.set_state(st)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                s.run(cyc)
+                reps.append(time.perf_counter() - t0)
+            graph_s = sorted(reps)[1]
+        host = {k: v.copy() for k, v in st.items()}
+        sgh.sgh_solve(prob, host)  # warm-up of the one-shot path
+        host = {k: v.copy() for k, v in st.items()}
+        t0 = time.perf_counter()
+        r = sgh.sgh_solve(prob, host)
+        one_shot = time.perf_counter() - t0
+        cores = os.cpu_count() or 1
+        ref_all = orc.run_reference(prob, kind="fierro_ref_fast", threads=cores)
+        ref_one = orc.run_reference(prob, kind="fierro_ref_fast", threads=1)
+        # the reference stops at time_final too; both runs take the same cycles
+        out[name] = {"elements": ne, "cycles": ran,
+                     "gpu_graph_element_cycles_per_s": ne * ran / graph_s, "gpu_graph_s": graph_s,
+                     "gpu_events_element_cycles_per_s": ne * ran / (total_ms * 1e-3), "gpu_events_ms": total_ms,
+                     "gpu_one_shot_element_cycles_per_s": ne * r["cycles"] / one_shot, "gpu_one_shot_s": one_shot,
+                     "cpu_element_cycles_per_s": ne * ran / ref_all["calc_seconds"], "cpu_cores": cores,
+                     "cpu_1core_element_cycles_per_s": ne * ran / ref_one["calc_seconds"],
+                     "time_final_gpu": r["time_value"], "time_final_cpu": ref_all["time"]}
+    print(json.dumps({"metric": "small reference decks: element-cycles/s, GPU and reference CPU", "unit": UNIT,
+                      "dtype": "f64", "data": "synthetic (generator equal to the shipped meshes)",
+                      "configs": out}))
+
+
 def main(argv=None):
     args = parse(argv)
+    if args.configs:
+        configs_bench(args)
+        return
     if args.rz:
         rz_bench(args)
         return
