@@ -178,3 +178,21 @@ def test_rz_setup_rejects_reference_defects(lib_built):
     with pytest.raises(sgh.FierroError) as ei:
         sgh.setup(p)
     assert ei.value.code == sgh.FIERRO_EINVAL
+
+
+@pytest.mark.parametrize("dims", [3, 2])
+def test_host_setup_random_decks(lib_built, oracle_built, dims):
+    """Host set-up of seeded random decks (uneven boxes, several materials, box /
+    sphere / cylinder fills, cartesian / radial / spherical velocities, fixed and
+    reflecting planes) equals the restatement's set-up bit for bit."""
+    from decks import random_deck
+    from fierro_gb300 import sgh
+    from oracle import orc
+    for seed in range(24):
+        prob = random_deck(seed, dims)
+        st = sgh.setup(prob)
+        r = orc.Oracle(prob).state()
+        got = {"coords": st["node_coords"][1], "vel": st["node_vel"][1], "den": st["elem_den"],
+               "pres": st["elem_pres"], "sie": st["elem_sie"][1], "sspd": st["elem_sspd"], "vol": st["elem_vol"],
+               "mass": st["elem_mass"], "node_mass": st["node_mass"]}
+        assert_bitwise(got, r, list(got), label="%s" % prob.name)
