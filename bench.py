@@ -744,6 +744,31 @@ def rz_bench(args):
         dev_bytes = s.device_bytes
         launches_total = int(s.launches_per_cycle * args.steps)
         ie, ke = s.energy()
+        # end to end through the C ABI with host buffers (staged transfers on this
+        # path): upload, the same K cycles, download; warm-up solve, median of three
+        host = {k: v.copy() for k, v in st.items()}
+        h2d = sum(st[k].nbytes for k in st if k not in ("corner_force",))
+        d2h = sum(host[k].nbytes for k in host if k not in ("elem_statev", "elem_mat_id"))
+        s.set_state(st)
+        s.run(1)
+        s.get_state(host)
+        trials = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            te0 = time.perf_counter()
+            s.set_state(st)
+            tu = time.perf_counter()
+            s.run(args.steps)
+            tr = time.perf_counter()
+            s.get_state(host)
+            te1 = time.perf_counter()
+            trials.append((te1 - te0, tu - te0, tr - tu, te1 - tr))
+        trials.sort()
+        med = trials[1]
+        e2e = {"value": ne * args.steps / med[0], "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
+               "d2h_bytes_per_step": d2h / args.steps, "upload_s": med[1], "run_s": med[2], "download_s": med[3],
+               "path": "fierro_sgh_set_state + fierro_sgh_run(K) + fierro_sgh_get_state with host buffers in the "
+                       "reference's 2D layouts (staged through pinned buffers on this path); median of three"}
     nnz = 8 * ne  # a quad's node-sharing neighbours: 8 inside the mesh
     dom = max(("k_force", "k_node", "k_elem"), key=lambda k: per[k])
     dom_ms = per[dom] / launches[dom]
@@ -775,7 +800,7 @@ def rz_bench(args):
                        "gamma": 5.0 / 3.0, "energy": 0.49339, "cfl": 0.4, "rk_stages": 2, "seed": args.seed,
                        "fp_mode": args.fp_mode, "num_dims": 2,
                        "l2": "inputs larger than L2 (device state %.1f GB vs 129 MB L2)" % (dev_bytes / 1e9)},
-            "gpu_launches": launches_total,
+            "gpu_launches": launches_total, "e2e": e2e,
             "kernels": {nm: {"launches": launches[nm], "ms": per[nm], "share": per[nm] / total_ms} for nm in per},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": ab / (dom_ms * 1e-3) / 1e9, "peak": hbm_peak,
                          "unit": "GB/s", "frac": ab / (dom_ms * 1e-3) / 1e9 / hbm_peak, "traffic": None,

@@ -149,3 +149,19 @@ def test_rz_hoop_terms_on_thin_elements(oracle_built, lib_built, length):
     r = _oracle(prob, cycles=20)
     assert np.isfinite(r["coords"]).all()
     assert_bitwise(g, r, FIELDS + EXTRA, label="thin quads %s" % (length,))
+
+
+def test_rz_one_shot_solve_equals_handle(oracle_built, lib_built):
+    """fierro_sgh_solve (create, upload, run, download, destroy in one call) on a
+    quad mesh returns what the persistent handle computes."""
+    from fierro_gb300 import sgh
+    prob = _cases()["noh_rz12_jp"]
+    st = sgh.setup(prob)
+    host = {k: v.copy() for k, v in st.items()}
+    r = sgh.sgh_solve(prob, host)
+    assert r["cycles"] == prob.params.cycle_stop
+    g = _gpu(prob, cycles=prob.params.cycle_stop)
+    assert r["time_value"] == g["time"]
+    for k, hk in (("coords", ("node_coords", 1)), ("vel", ("node_vel", 1)), ("sie", ("elem_sie", 1))):
+        assert np.array_equal(host[hk[0]][hk[1]], g[k]), k
+    assert np.array_equal(host["node_mass"], g["node_mass"])
