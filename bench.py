@@ -38,7 +38,11 @@ def parse(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=256, help="elements per edge of the Sedov box")
-    ap.add_argument("--fp-mode", default="exact", choices=["exact", "fma"])
+    ap.add_argument("--fp-mode", default="fma", choices=["exact", "fma"],
+                    help="fma (default): fused multiply-adds, within 1e-12 of the reference after one cycle "
+                         "and 1e-9 after a full run on the gated fields; exact: the reference's arithmetic bit "
+                         "for bit (also measured, as exact_mode, when the headline runs in fma)")
+    ap.add_argument("--no-exact-leg", action="store_true")
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--cpu-n", type=int, default=120, help="edge of the CPU baseline sample mesh")
     ap.add_argument("--cpu-cycles", type=int, default=6, help="timed cycles of the CPU baseline sample")
@@ -173,16 +177,21 @@ def alg_bytes(kind: str, nn: int, ne: int, nnz: int) -> float:
     return 0.0
 
 
-# Per-unit figures of the exact-mode kernels from the ncu capture summarised in
-# profiles/sgh_kernels_sedov64_ncu_full.md (64^3 case, above L2; per-element
-# DRAM bytes scale with the elements processed): FP64 thread instructions and
-# dram__bytes_read + dram__bytes_write per element of one launch.  k_elem is the
-# mean of its first-stage and last-stage (CFL) launches.
-NCU_PER_ELEM = {
+# Per-unit figures of the kernels from the ncu captures summarised in
+# profiles/sgh_kernels_sedov64_ncu_full.md (exact mode) and
+# profiles/sgh_kernels_sedov64_fma_ncu.md (FMA mode), 64^3 case, above L2;
+# per-element DRAM bytes scale with the elements processed: FP64 thread
+# instructions and dram__bytes_read + dram__bytes_write per element of one
+# launch.  k_elem is the mean of its first-stage and last-stage (CFL) launches.
+NCU_PER_ELEM = {"exact": {
     "k_force": {"fp64_ops": 138412032 / 262144, "dram_bytes": (104.519936e6 + 22.368256e6) / 262144},
     "k_elem": {"fp64_ops": (158072832 + 171509792) / 2 / 262144,
                "dram_bytes": (87.254784e6 + 25.970176e6 + 87.096064e6 + 26.185472e6) / 2 / 262144},
-}
+}, "fma": {
+    "k_force": {"fp64_ops": 117964811 / 262144, "dram_bytes": (104.57088e6 + 21.069312e6) / 262144},
+    "k_elem": {"fp64_ops": (130809856 + 143716888) / 2 / 262144,
+               "dram_bytes": (87.258368e6 + 24.943616e6 + 87.229952e6 + 25.808896e6) / 2 / 262144},
+}}
 
 
 def measure_peaks():
@@ -291,6 +300,7 @@ def ours(args):
     achieved = ab / (dom_ms * 1e-3) / 1e9
     cycle_bytes = sum(alg_bytes(k, nn, ne, nnz) * names.count(k) for k in ("k_force", "k_node", "k_elem"))
     cycle_ms = total_ms / args.steps
+    ncu = NCU_PER_ELEM[args.fp_mode]
 
     # end to end through the C ABI with host buffers: upload the state, run the
     # same K cycles, download the state (copies inside the timed region)
@@ -354,16 +364,16 @@ def ours(args):
         "roofline": {
             "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved / hbm_peak,
-            "traffic": NCU_PER_ELEM[dom]["dram_bytes"] * ne if dom in NCU_PER_ELEM else None,
+            "traffic": ncu[dom]["dram_bytes"] * ne if dom in ncu else None,
             "peak_kind": peak_kind, "alg_bytes_per_launch": ab, "avg_launch_ms": dom_ms,
             "cycle_alg_bytes": cycle_bytes, "cycle_hbm_gbs": cycle_bytes / (cycle_ms * 1e-3) / 1e9,
             "binding_pipe": "fp64",
-            "fp64": None if dom not in NCU_PER_ELEM or args.fp_mode != "exact" else {
-                "achieved": NCU_PER_ELEM[dom]["fp64_ops"] * ne / (dom_ms * 1e-3) / 1e9,
+            "fp64": None if dom not in ncu else {
+                "achieved": ncu[dom]["fp64_ops"] * ne / (dom_ms * 1e-3) / 1e9,
                 "peak": fp64_rate / 1e9, "unit": "G FP64 thread-instructions/s",
-                "frac": NCU_PER_ELEM[dom]["fp64_ops"] * ne / (dom_ms * 1e-3) / fp64_rate,
+                "frac": ncu[dom]["fp64_ops"] * ne / (dom_ms * 1e-3) / fp64_rate,
                 "peak_kind": "measured DFMA rate on this GPU (fierro_measure_fp64_rate)",
-                "ops_per_elem": NCU_PER_ELEM[dom]["fp64_ops"]},
+                "ops_per_elem": ncu[dom]["fp64_ops"]},
         },
         "kernels": {nm: {"launches": launches[nm], "ms": per[nm], "share": share[nm]} for nm in sorted(per)},
         "cpu_baseline": None if cpu is None else {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
@@ -371,8 +381,22 @@ def ours(args):
         "setup_seconds": t_setup,
         "device_bytes": solver.device_bytes,
     }
-    print(json.dumps(line))
     solver.close()
+    if args.fp_mode == "fma" and not args.no_exact_leg and world == 1:
+        # the same timed cycles in the exact mode (the reference's arithmetic bit
+        # for bit), for comparison
+        with sgh.SGHSolver(prob, fp_mode=sgh.FP_EXACT, stream=stream.cuda_stream) as sx:
+            sx.set_state(st)
+            sx.run(args.warmup)
+            ran_x, total_x, kms_x = sx.run_timed(args.steps)
+            names_x = sx.launch_names()
+        per_x = {}
+        for nm, ms in zip(names_x, kms_x):
+            per_x[nm] = per_x.get(nm, 0.0) + ms
+        line["exact_mode"] = {"value": ne * ran_x / (total_x * 1e-3), "ms_per_step": total_x / max(ran_x, 1),
+                              "kernels_ms_per_launch": {nm: per_x[nm] / (names_x.count(nm) * max(ran_x, 1))
+                                                        for nm in per_x}}
+    print(json.dumps(line))
 
 
 def solver_neighbor_count(prob) -> int:

@@ -2,6 +2,15 @@
 // Straight-line hex geometry; see the generator's docstring for the exactness argument.
 #pragma once
 
+// Separately rounded product and sum, also where the unit contracts (FIERRO_FMA=1).
+#if FIERRO_FMA
+#define FX_MUL(a, b) __dmul_rn((a), (b))
+#define FX_ADD(a, b) __dadd_rn((a), (b))
+#else
+#define FX_MUL(a, b) ((a) * (b))
+#define FX_ADD(a, b) ((a) + (b))
+#endif
+
 // In: x,y,z,u,v,w[8] (node lids 0..7).  Out: vol; bmat rows lid*3+dim at
 // bmat[row*ne + e]; Sx,Sy,Sz = sum_p u_p B(p,0), v_p B(p,1), w_p B(p,2) (p order).
 __device__ __forceinline__ void hex_geometry(const double* __restrict__ x, const double* __restrict__ y,
@@ -34,63 +43,63 @@ __device__ __forceinline__ void hex_geometry(const double* __restrict__ x, const
     const double cm21 = (((-z[1] - z[2]) + z[4]) + z[7]);  // pair (5,6)
     const double cm22 = (z[4] - z[6]);  // pair (5,7)
     const double cm23 = (((-z[2] - z[3]) + z[4]) + z[5]);  // pair (6,7)
-    const double pr0_0 = y[1] * cm0;
-    const double pr0_1 = y[2] * cm1;
-    const double pr0_2 = y[3] * cm2;
-    const double pr0_3 = y[4] * cm3;
-    const double pr0_4 = y[5] * cm4;
-    const double pr0_5 = y[7] * cm5;
-    const double pr1_0 = y[0] * (-cm0);
-    const double pr1_1 = y[2] * cm6;
-    const double pr1_2 = y[3] * cm7;
-    const double pr1_3 = y[4] * cm8;
-    const double pr1_4 = y[5] * cm9;
-    const double pr1_5 = y[6] * cm10;
-    const double pr2_0 = y[0] * (-cm1);
-    const double pr2_1 = y[1] * (-cm6);
-    const double pr2_2 = y[3] * cm11;
-    const double pr2_3 = y[5] * cm12;
-    const double pr2_4 = y[6] * cm13;
-    const double pr2_5 = y[7] * cm14;
-    const double pr3_0 = y[0] * (-cm2);
-    const double pr3_1 = y[1] * (-cm7);
-    const double pr3_2 = y[2] * (-cm11);
-    const double pr3_3 = y[4] * cm15;
-    const double pr3_4 = y[6] * cm16;
-    const double pr3_5 = y[7] * cm17;
-    const double pr4_0 = y[0] * (-cm3);
-    const double pr4_1 = y[1] * (-cm8);
-    const double pr4_2 = y[3] * (-cm15);
-    const double pr4_3 = y[5] * cm18;
-    const double pr4_4 = y[6] * cm19;
-    const double pr4_5 = y[7] * cm20;
-    const double pr5_0 = y[0] * (-cm4);
-    const double pr5_1 = y[1] * (-cm9);
-    const double pr5_2 = y[2] * (-cm12);
-    const double pr5_3 = y[4] * (-cm18);
-    const double pr5_4 = y[6] * cm21;
-    const double pr5_5 = y[7] * cm22;
-    const double pr6_0 = y[1] * (-cm10);
-    const double pr6_1 = y[2] * (-cm13);
-    const double pr6_2 = y[3] * (-cm16);
-    const double pr6_3 = y[4] * (-cm19);
-    const double pr6_4 = y[5] * (-cm21);
-    const double pr6_5 = y[7] * cm23;
-    const double pr7_0 = y[0] * (-cm5);
-    const double pr7_1 = y[2] * (-cm14);
-    const double pr7_2 = y[3] * (-cm17);
-    const double pr7_3 = y[4] * (-cm20);
-    const double pr7_4 = y[5] * (-cm22);
-    const double pr7_5 = y[6] * (-cm23);
-    const double vi0 = x[1] * (((((pr1_2 + pr1_3) + pr1_0) + pr1_5) + pr1_4) + pr1_1);
-    const double vi1 = x[7] * (((((pr7_0 + pr7_5) + pr7_1) + pr7_2) + pr7_4) + pr7_3);
-    const double vi2 = x[3] * (((((pr3_1 + pr3_5) + pr3_4) + pr3_2) + pr3_3) + pr3_0);
-    const double vi3 = x[5] * (((((pr5_0 + pr5_5) + pr5_2) + pr5_1) + pr5_3) + pr5_4);
-    const double vi4 = x[6] * (((((pr6_0 + pr6_5) + pr6_4) + pr6_3) + pr6_2) + pr6_1);
-    const double vi5 = x[0] * (((((pr0_1 + pr0_5) + pr0_4) + pr0_0) + pr0_2) + pr0_3);
-    const double vi6 = x[2] * (((((pr2_0 + pr2_3) + pr2_1) + pr2_5) + pr2_4) + pr2_2);
-    const double vi7 = x[4] * (((((pr4_1 + pr4_5) + pr4_2) + pr4_0) + pr4_4) + pr4_3);
-    vol = (((((((vi0 + vi1) + vi2) + vi3) + vi4) + vi5) + vi6) + vi7) * twelth;
+    const double pr0_0 = FX_MUL(y[1], cm0);
+    const double pr0_1 = FX_MUL(y[2], cm1);
+    const double pr0_2 = FX_MUL(y[3], cm2);
+    const double pr0_3 = FX_MUL(y[4], cm3);
+    const double pr0_4 = FX_MUL(y[5], cm4);
+    const double pr0_5 = FX_MUL(y[7], cm5);
+    const double pr1_0 = FX_MUL(y[0], (-cm0));
+    const double pr1_1 = FX_MUL(y[2], cm6);
+    const double pr1_2 = FX_MUL(y[3], cm7);
+    const double pr1_3 = FX_MUL(y[4], cm8);
+    const double pr1_4 = FX_MUL(y[5], cm9);
+    const double pr1_5 = FX_MUL(y[6], cm10);
+    const double pr2_0 = FX_MUL(y[0], (-cm1));
+    const double pr2_1 = FX_MUL(y[1], (-cm6));
+    const double pr2_2 = FX_MUL(y[3], cm11);
+    const double pr2_3 = FX_MUL(y[5], cm12);
+    const double pr2_4 = FX_MUL(y[6], cm13);
+    const double pr2_5 = FX_MUL(y[7], cm14);
+    const double pr3_0 = FX_MUL(y[0], (-cm2));
+    const double pr3_1 = FX_MUL(y[1], (-cm7));
+    const double pr3_2 = FX_MUL(y[2], (-cm11));
+    const double pr3_3 = FX_MUL(y[4], cm15);
+    const double pr3_4 = FX_MUL(y[6], cm16);
+    const double pr3_5 = FX_MUL(y[7], cm17);
+    const double pr4_0 = FX_MUL(y[0], (-cm3));
+    const double pr4_1 = FX_MUL(y[1], (-cm8));
+    const double pr4_2 = FX_MUL(y[3], (-cm15));
+    const double pr4_3 = FX_MUL(y[5], cm18);
+    const double pr4_4 = FX_MUL(y[6], cm19);
+    const double pr4_5 = FX_MUL(y[7], cm20);
+    const double pr5_0 = FX_MUL(y[0], (-cm4));
+    const double pr5_1 = FX_MUL(y[1], (-cm9));
+    const double pr5_2 = FX_MUL(y[2], (-cm12));
+    const double pr5_3 = FX_MUL(y[4], (-cm18));
+    const double pr5_4 = FX_MUL(y[6], cm21);
+    const double pr5_5 = FX_MUL(y[7], cm22);
+    const double pr6_0 = FX_MUL(y[1], (-cm10));
+    const double pr6_1 = FX_MUL(y[2], (-cm13));
+    const double pr6_2 = FX_MUL(y[3], (-cm16));
+    const double pr6_3 = FX_MUL(y[4], (-cm19));
+    const double pr6_4 = FX_MUL(y[5], (-cm21));
+    const double pr6_5 = FX_MUL(y[7], cm23);
+    const double pr7_0 = FX_MUL(y[0], (-cm5));
+    const double pr7_1 = FX_MUL(y[2], (-cm14));
+    const double pr7_2 = FX_MUL(y[3], (-cm17));
+    const double pr7_3 = FX_MUL(y[4], (-cm20));
+    const double pr7_4 = FX_MUL(y[5], (-cm22));
+    const double pr7_5 = FX_MUL(y[6], (-cm23));
+    const double vi0 = FX_MUL(x[1], FX_ADD(FX_ADD(FX_ADD(FX_ADD(FX_ADD(pr1_2, pr1_3), pr1_0), pr1_5), pr1_4), pr1_1));
+    const double vi1 = FX_MUL(x[7], FX_ADD(FX_ADD(FX_ADD(FX_ADD(FX_ADD(pr7_0, pr7_5), pr7_1), pr7_2), pr7_4), pr7_3));
+    const double vi2 = FX_MUL(x[3], FX_ADD(FX_ADD(FX_ADD(FX_ADD(FX_ADD(pr3_1, pr3_5), pr3_4), pr3_2), pr3_3), pr3_0));
+    const double vi3 = FX_MUL(x[5], FX_ADD(FX_ADD(FX_ADD(FX_ADD(FX_ADD(pr5_0, pr5_5), pr5_2), pr5_1), pr5_3), pr5_4));
+    const double vi4 = FX_MUL(x[6], FX_ADD(FX_ADD(FX_ADD(FX_ADD(FX_ADD(pr6_0, pr6_5), pr6_4), pr6_3), pr6_2), pr6_1));
+    const double vi5 = FX_MUL(x[0], FX_ADD(FX_ADD(FX_ADD(FX_ADD(FX_ADD(pr0_1, pr0_5), pr0_4), pr0_0), pr0_2), pr0_3));
+    const double vi6 = FX_MUL(x[2], FX_ADD(FX_ADD(FX_ADD(FX_ADD(FX_ADD(pr2_0, pr2_3), pr2_1), pr2_5), pr2_4), pr2_2));
+    const double vi7 = FX_MUL(x[4], FX_ADD(FX_ADD(FX_ADD(FX_ADD(FX_ADD(pr4_1, pr4_5), pr4_2), pr4_0), pr4_4), pr4_3));
+    vol = FX_MUL(FX_ADD(FX_ADD(FX_ADD(FX_ADD(FX_ADD(FX_ADD(FX_ADD(vi0, vi1), vi2), vi3), vi4), vi5), vi6), vi7), twelth);
     const double b0 = (((((pr0_0 + pr0_1) + pr0_2) + pr0_3) + pr0_4) + pr0_5) * twelth;
     bmat[(size_t)0 * ne + e] = b0;
     Sx = u[0] * b0;

@@ -7,7 +7,10 @@
 //       division and square root, so results match its uncontracted evaluation;
 //   FIERRO_FMA=1 with --fmad=true  -> fierro::fma_impl: the same schedule, the
 //       compiler free to fuse multiply-adds, and the per-node division by mass
-//       done through one reciprocal.
+//       done through one reciprocal -- except where the reference's sums cancel
+//       (the hex volume, the element power, the Riemann velocity), which stay
+//       separately rounded (FX_MUL / FX_ADD) so this mode keeps within 1e-12 of
+//       the reference after one cycle and 1e-9 after a full run.
 //
 // One cycle is 2 + 3*rk_num_stages launches:
 //   k_dt                    CFL minimum over the last stage's per-block partials,
@@ -129,24 +132,20 @@ __global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
     const double b1 = a.bmat[(size_t)(l * 3 + 1) * ne + e];
     const double b2 = a.bmat[(size_t)(l * 3 + 2) * ne + e];
     const double mu_term = muc * sqrt(b0 * b0 + b1 * b1 + b2 * b2);
-    s0 = s0 + mu_term * vu[l];
-    s1 = s1 + mu_term * vv[l];
-    s2 = s2 + mu_term * vw[l];
+    // the Riemann velocity's sums stay separately rounded in both modes: the
+    // force's (v* - v) and then the element power cancel, and a contracted v*
+    // would move a cold element's energy by ~1e-12 relative after one cycle
+    s0 = FX_ADD(s0, FX_MUL(mu_term, vu[l]));
+    s1 = FX_ADD(s1, FX_MUL(mu_term, vv[l]));
+    s2 = FX_ADD(s2, FX_MUL(mu_term, vw[l]));
     s3 = s3 + mu_term;
     mu[l] = mu_term;
   }
   double vstar0 = 0.0, vstar1 = 0.0, vstar2 = 0.0;
   if (s3 > a.fuzz) {
-#if FIERRO_FMA
-    const double rs = 1.0 / s3;
-    vstar0 = s0 * rs;
-    vstar1 = s1 * rs;
-    vstar2 = s2 * rs;
-#else
     vstar0 = s0 / s3;
     vstar1 = s1 / s3;
     vstar2 = s2 / s3;
-#endif
   }
   // shock detector (:287-315): r_face = 0.9 (div_nb + small) / (div + small) is
   // monotone in div_nb (non-decreasing for div + small > 0, non-increasing for < 0),
@@ -349,16 +348,18 @@ __global__ void __launch_bounds__(kElemBlock) k_elem(const ElemArgs a) {
     }
     double sie1 = 0.0;
     if (KIND != 2) {
-      // energy (energy_sgh.cpp:16-52): power = sum_c F_c . (v1 + v0)/2, lid-major
+      // energy (energy_sgh.cpp:16-52): power = sum_c F_c . (v1 + v0)/2, lid-major,
+      // separately rounded in both modes: where a cold element's heating nearly
+      // cancels its energy, a contracted sum would move sie by far more than an ulp
       double power = 0.0;
 #pragma unroll
       for (int l = 0; l < 8; ++l) {
-        power = power + a.force[(size_t)(l * 3 + 0) * ne + e] * __ldg(a.hx + nid[l]);
-        power = power + a.force[(size_t)(l * 3 + 1) * ne + e] * __ldg(a.hy + nid[l]);
-        power = power + a.force[(size_t)(l * 3 + 2) * ne + e] * __ldg(a.hz + nid[l]);
+        power = FX_ADD(power, FX_MUL(a.force[(size_t)(l * 3 + 0) * ne + e], __ldg(a.hx + nid[l])));
+        power = FX_ADD(power, FX_MUL(a.force[(size_t)(l * 3 + 1) * ne + e], __ldg(a.hy + nid[l])));
+        power = FX_ADD(power, FX_MUL(a.force[(size_t)(l * 3 + 2) * ne + e], __ldg(a.hz + nid[l])));
       }
       const double adt = a.rk_alpha * ctrl->dt;
-      sie1 = a.sie0[e] - adt / a.mass[e] * power;
+      sie1 = a.sie0[e] - FX_MUL(adt / a.mass[e], power);  // not fused: sie1 may cancel sie0
       a.sie1[e] = sie1;
     }
     double vol_geo, Sx, Sy, Sz;

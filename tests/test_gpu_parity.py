@@ -110,20 +110,41 @@ def test_exact_vs_reference_golden(lib_built, case, cycles, tol):
     assert_fields(g, ref, tol, FIELDS, label="%s c%d" % (case, cycles))
 
 
-@pytest.mark.parametrize("case", ["sedov12", "noh32"])
+GATED = ("coords", "vel", "den", "pres", "sie")  # positions, velocities, density, pressure, energy
+
+
+@pytest.mark.parametrize("case", ["sedov12", "noh32", "sedov16_jp", "noh12_jp"])
 def test_fma_mode_within_tolerance(oracle_built, lib_built, case):
-    """The opt-in fused-multiply-add mode rounds differently: after one cycle it
-    stays within 1e-11 (the sound speed of Noh's barely heated elements, where the
-    energy update cancels, is the worst field at ~1.2e-12); after the full run
-    within 1e-9.  The 1e-12 one-cycle gate is the exact mode's."""
+    """The fused-multiply-add mode meets the parity gates on the gated fields:
+    positions, velocities, density, pressure and energy within 1e-12 of the
+    reference's arithmetic after one RK2 cycle and within 1e-9 after the full
+    run (relative, floor 1e-3 of the field's peak).  The sums whose cancellation
+    would amplify contraction (hex volume, element power, Riemann velocity, the
+    energy update) stay separately rounded in this mode.  Sound speed is not a
+    gated field: in Noh's barely heated elements, whose energy is ill-conditioned
+    after one cycle, it stays within 2e-12."""
     prob = _cases()[case]()
     n = prob.params.cycle_stop
     g1 = _gpu_state(prob, cycles=1, mode=1)
     r1 = _oracle_state(prob, cycles=1)
-    assert_fields(g1, r1, 1e-11, FIELDS, label=case + " fma 1 cycle")
+    assert_fields(g1, r1, 1e-12, GATED, label=case + " fma 1 cycle")
+    assert_fields(g1, r1, 2e-12, ("sspd", "vol"), label=case + " fma 1 cycle")
     g = _gpu_state(prob, cycles=n, mode=1)
     r = _oracle_state(prob, cycles=n)
     assert_fields(g, r, 1e-9, FIELDS, label=case + " fma full")
+
+
+def test_fma_mode_gates_on_the_bench_mesh_family(lib_built):
+    """The benchmark's mesh family (jittered, permuted Sedov) at 64^3: the FMA
+    mode against the exact mode (the reference's arithmetic, bit for bit) after
+    one cycle and after 100."""
+    from fierro_gb300 import problems
+    prob = problems.sedov(64, jitter=0.1, seed=2024, permute=True, cycles=100)
+    for cyc, tol in ((1, 1e-12), (100, 1e-9)):
+        g = _gpu_state(prob, cycles=cyc, mode=1)
+        r = _gpu_state(prob, cycles=cyc, mode=0)
+        assert_fields(g, r, tol, GATED, label="sedov64 fma %d cycles" % cyc)
+        assert g["time"] == pytest.approx(r["time"], rel=1e-13)
 
 
 @pytest.mark.parametrize("case", ["sedov12", "noh32", "sedov16_jp"])
