@@ -263,6 +263,7 @@ int replay_segment(fierro_sgh* h, AdjState* a, int g, int n) {
       fa.small = h->lp.small;
       fa.tape = a->ftape + (size_t)j * kForceTapeRows * ne;
       fa.tape_sel = a->fsel + (size_t)j * ne;
+      fa.block = h->blk_force;
       h->ks->force_tape(fa, st);
       NodeArgs na{};
       na.nn = (int)nn;
@@ -289,6 +290,7 @@ int replay_segment(fierro_sgh* h, AdjState* a, int g, int n) {
       na.hz = sn.hz;
       na.ctrl = a->ctrl;
       na.rk_alpha = alpha;
+      na.block = h->blk_node;
       h->ks->node(na, st);
       ElemArgs ea{};
       ea.ne = (int)ne;
@@ -319,6 +321,7 @@ int replay_segment(fierro_sgh* h, AdjState* a, int g, int n) {
       ea.rk_alpha = alpha;
       ea.dt_cfl = h->lp.dt_cfl;
       ea.fuzz = h->lp.fuzz;
+      ea.block = h->blk_elem;
       h->ks->elem(ea, s == S - 1 ? 1 : 0, st);
     }
     h->ks->end(a->ctrl, h->lp, st);

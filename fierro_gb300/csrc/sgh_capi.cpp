@@ -85,6 +85,7 @@ ForceArgs force_args(fierro_sgh* h, int rb, int q) {
   a.ctrl = h->d_ctrl;
   a.fuzz = h->lp.fuzz;
   a.small = h->lp.small;
+  a.block = h->blk_force;
   return a;
 }
 
@@ -114,6 +115,7 @@ NodeArgs node_args(fierro_sgh* h, int c, double alpha) {
   a.hz = h->d_h[2];
   a.ctrl = h->d_ctrl;
   a.rk_alpha = alpha;
+  a.block = h->blk_node;
   return a;
 }
 
@@ -147,6 +149,7 @@ ElemArgs elem_args(fierro_sgh* h, int cur_bin, int c, double alpha, int div_out)
   a.rk_alpha = alpha;
   a.dt_cfl = h->lp.dt_cfl;
   a.fuzz = h->lp.fuzz;
+  a.block = h->blk_elem;
   return a;
 }
 
@@ -388,7 +391,10 @@ static int create_impl(fierro_sgh* h, const fierro_mesh* mesh, const fierro_mate
     for (int64_t m = 0; m < num_materials; ++m) st[m] = materials[m].strength_type;
     TRY(upload_raw(h, h->d_stype, st.data(), sizeof(int) * st.size()));
   }
-  h->ncfl = (int)((ne + kElemBlock - 1) / kElemBlock);
+  h->blk_elem = small_mesh_block(ne, kElemBlock);
+  h->blk_force = small_mesh_block(ne, kForceBlock);
+  h->blk_node = small_mesh_block(nn, kNodeBlock);
+  h->ncfl = (int)((ne + h->blk_elem - 1) / h->blk_elem);
   TRY(dalloc(h, &h->d_cfl, (size_t)h->ncfl));
   TRY(dalloc(h, &h->d_ctrl, 1));
   TRY(dalloc(h, &h->d_node_ext2int, nn));

@@ -77,6 +77,7 @@ struct ForceArgs {
   const double* sie0;  // cycle-start energy (the reference passes elem_sie bin 0)
   double rk_alpha;
   int copy_stress;     // stage 0: elements without a hypo model carry stress_cur over
+  int block;           // threads per block (0: kForceBlock)
 };
 
 // Rows of the force kernel's tape: mu[8], |v_l - v_avg|[8], v*[3], sum mu,
@@ -96,6 +97,7 @@ struct NodeArgs {
   const Ctrl* ctrl;
   const int* inst;  // batch only: instance of each node
   double rk_alpha;
+  int block;        // threads per block (0: kNodeBlock)
 };
 
 // kind: 0 = stage update, 1 = last stage of a cycle (adds the CFL partial
@@ -125,6 +127,7 @@ struct ElemArgs {
   const double* stress0;  // cycle-start stress(0)
   double* stress1;        // stress(1), updated in place
   double* statev;         // [nsv][ne]
+  int block;              // threads per block, one CFL partial per block (0: kElemBlock; a batch always uses it)
 };
 
 struct DtArgs {
@@ -163,6 +166,17 @@ constexpr int kElemBlock = 128;
 constexpr int kForceBlock = 128;
 constexpr int kNodeBlock = 256;
 constexpr int kEnergyBlock = 256;
+
+// Launch block for `n` threads of a kernel whose default block is `bs`: halved
+// (down to one warp) while the grid would have fewer than kMinBlocks blocks, so a
+// small mesh spreads over more SMs (each SM's FP64 rate, not the chip's, bounds
+// a kernel that occupies few of them).  It depends on n alone, so the number of
+// CFL partials (one per element block) is a property of the mesh.
+constexpr long long kMinBlocks = 304;  // two per SM of a 152-SM GB300
+inline int small_mesh_block(long long n, int bs) {
+  while (bs > 32 && (n + bs - 1) / bs < kMinBlocks) bs >>= 1;
+  return bs;
+}
 
 const KernelSet& kernels_exact();
 const KernelSet& kernels_fma();

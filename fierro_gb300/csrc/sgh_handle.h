@@ -62,7 +62,9 @@ struct fierro_sgh {
   double* d_sie[2] = {};
   double *d_bmat = nullptr, *d_force = nullptr;
   long long* d_cfl = nullptr;
-  int ncfl = 0;
+  int ncfl = 0;  // CFL partials: one per element block
+  // threads per block of the element, force and node kernels (small_mesh_block)
+  int blk_elem = fierro::kElemBlock, blk_force = fierro::kForceBlock, blk_node = fierro::kNodeBlock;
   fierro::Ctrl* d_ctrl = nullptr;
   double *d_energy_part = nullptr, *d_energy_out = nullptr;
   // pinned double buffer for permuted transfers

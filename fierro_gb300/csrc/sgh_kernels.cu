@@ -541,25 +541,34 @@ __global__ void k_energy_final(const EnergyArgs a, int nblocks) {
 // ---------------------------------------------------------------------------
 static unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
+// A block size below the default only lowers the threads per block (the
+// kernels' shared memory is sized for the default); a batch keeps the default,
+// as its instances' element ranges are padded to whole default blocks.
+static int block_or(int b, int def) { return (b >= 32 && b <= def && b % 32 == 0) ? b : def; }
+
 static void launch_force(const ForceArgs& a, cudaStream_t s) {
-  const unsigned g = blocks_for(a.ne, kForceBlock);
-  if (a.inst) k_force<true, false, false><<<g, kForceBlock, 0, s>>>(a);
-  else if (a.stress_out) k_force<false, false, true><<<g, kForceBlock, 0, s>>>(a);
-  else k_force<false, false, false><<<g, kForceBlock, 0, s>>>(a);
+  const int bs = a.inst ? kForceBlock : block_or(a.block, kForceBlock);
+  const unsigned g = blocks_for(a.ne, bs);
+  if (a.inst) k_force<true, false, false><<<g, bs, 0, s>>>(a);
+  else if (a.stress_out) k_force<false, false, true><<<g, bs, 0, s>>>(a);
+  else k_force<false, false, false><<<g, bs, 0, s>>>(a);
 }
 static void launch_force_tape(const ForceArgs& a, cudaStream_t s) {
-  k_force<false, true, false><<<blocks_for(a.ne, kForceBlock), kForceBlock, 0, s>>>(a);
+  const int bs = block_or(a.block, kForceBlock);
+  k_force<false, true, false><<<blocks_for(a.ne, bs), bs, 0, s>>>(a);
 }
 static void launch_node(const NodeArgs& a, cudaStream_t s) {
-  if (a.inst) k_node<true><<<blocks_for(a.nn, kNodeBlock), kNodeBlock, 0, s>>>(a);
-  else k_node<false><<<blocks_for(a.nn, kNodeBlock), kNodeBlock, 0, s>>>(a);
+  const int bs = a.inst ? kNodeBlock : block_or(a.block, kNodeBlock);
+  if (a.inst) k_node<true><<<blocks_for(a.nn, bs), bs, 0, s>>>(a);
+  else k_node<false><<<blocks_for(a.nn, bs), bs, 0, s>>>(a);
 }
 template <bool B, bool S>
 static void launch_elem_t(const ElemArgs& a, int kind, cudaStream_t s) {
-  const unsigned g = blocks_for(a.ne, kElemBlock);
-  if (kind == 0) k_elem<0, B, S><<<g, kElemBlock, 0, s>>>(a);
-  else if (kind == 1) k_elem<1, B, S><<<g, kElemBlock, 0, s>>>(a);
-  else k_elem<2, B, false><<<g, kElemBlock, 0, s>>>(a);
+  const int bs = B ? kElemBlock : block_or(a.block, kElemBlock);
+  const unsigned g = blocks_for(a.ne, bs);
+  if (kind == 0) k_elem<0, B, S><<<g, bs, 0, s>>>(a);
+  else if (kind == 1) k_elem<1, B, S><<<g, bs, 0, s>>>(a);
+  else k_elem<2, B, false><<<g, bs, 0, s>>>(a);
 }
 static void launch_elem(const ElemArgs& a, int kind, cudaStream_t s) {
   if (a.inst) launch_elem_t<true, false>(a, kind, s);
