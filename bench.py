@@ -31,6 +31,14 @@ METRIC = "SGH element-cycles/s, 256^3 perturbed Sedov, FP64 RK2"
 UNIT = "element-cycles/s"
 
 
+def metric_of(args) -> str:
+    """The headline metric; --problem noh measures the same quantity on the Noh
+    implosion (every node moving from the first cycle)."""
+    if getattr(args, "problem", "sedov") == "noh":
+        return "SGH element-cycles/s, %d^3 perturbed Noh, FP64 RK2" % args.n
+    return METRIC
+
+
 def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -38,6 +46,10 @@ def parse(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=256, help="elements per edge of the Sedov box")
+    ap.add_argument("--problem", default="sedov", choices=["sedov", "noh"],
+                    help="sedov (default): the blast from one corner element, the rest of the mesh at rest; "
+                         "noh: the implosion, every node moving from the first cycle (the kernels do the "
+                         "same work per element either way)")
     ap.add_argument("--fp-mode", default="fma", choices=["exact", "fma"],
                     help="fma (default): fused multiply-adds, within 1e-12 of the reference after one cycle "
                          "and 1e-9 after a full run on the gated fields; exact: the reference's arithmetic bit "
@@ -74,18 +86,24 @@ def parse(argv=None):
     return ap.parse_args(argv)
 
 
-def workload(n: int, seed: int):
+def workload(n: int, seed: int, problem: str = "sedov"):
     from fierro_gb300 import problems
+    if problem == "noh":
+        return problems.noh(n, length=1.0, jitter=0.1, seed=seed, permute=True, cycles=10 ** 9)
     return problems.sedov(n, length=1.2, energy=0.2467, gamma=1.4, jitter=0.1, seed=seed, permute=True,
                           cycles=10 ** 9)
 
 
 def config_of(args, n=None):
     n = args.n if n is None else n
-    return {"workload": "sedov3d_%d^3_jitter0.1_permuted" % n, "elements": n ** 3, "nodes": (n + 1) ** 3,
-            "gamma": 1.4, "energy": 0.2467, "cfl": 0.4, "rk_stages": 2, "seed": args.seed,
-            "parallelism": "replicas" if args.gpus > 1 else "single",
-            "l2": "inputs larger than L2 (device state > 10 GB vs 129 MB L2)"}
+    common = {"elements": n ** 3, "nodes": (n + 1) ** 3, "rk_stages": 2, "seed": args.seed,
+              "parallelism": "replicas" if args.gpus > 1 else "single",
+              "l2": "inputs larger than L2 (device state > 10 GB vs 129 MB L2)"}
+    if getattr(args, "problem", "sedov") == "noh":
+        return dict({"workload": "noh3d_%d^3_jitter0.1_permuted" % n, "gamma": 5.0 / 3.0, "speed": -1.0,
+                     "cfl": 0.3}, **common)
+    return dict({"workload": "sedov3d_%d^3_jitter0.1_permuted" % n, "gamma": 1.4, "energy": 0.2467,
+                 "cfl": 0.4}, **common)
 
 
 # ------------------------------------------------------------------ distributed
@@ -215,7 +233,7 @@ def run_reference_sample(args, n: int, cycles: int, warmup: int, strength: str |
         build_ref.build_reference()
     if not orc.reference_available("fierro_ref_fast"):
         raise RuntimeError("reference executable unavailable (no reference sources on this machine)")
-    prob = workload(n, args.seed)
+    prob = workload(n, args.seed, getattr(args, "problem", "sedov"))
     if strength:
         from fierro_gb300 import problems
         problems.with_strength(prob, strength, args.shear_modulus)
@@ -223,9 +241,10 @@ def run_reference_sample(args, n: int, cycles: int, warmup: int, strength: str |
     st = orc.run_reference(prob, cycles=cycles, kind="fierro_ref_fast", threads=cores, warmup=warmup)
     secs = st["calc_seconds"]
     return {"value": prob.mesh.num_elems * cycles / secs, "unit": UNIT, "cores": cores, "kind": "reference",
-            "sample": "%d^3 jittered permuted Sedov (%d elements), %d cycles timed by the reference's own "
+            "sample": "%d^3 jittered permuted %s (%d elements), %d cycles timed by the reference's own "
                       "cycle-loop timer after %d warm-up cycles, OMP_NUM_THREADS=%d" %
-                      (n, prob.mesh.num_elems, cycles, warmup, cores),
+                      (n, "Noh" if prob.name.startswith("noh") else "Sedov",
+                       prob.mesh.num_elems, cycles, warmup, cores),
             "seconds": secs}
 
 
@@ -238,7 +257,7 @@ def reference_arm(args):
     except Exception as exc:  # pragma: no cover - depends on the machine
         print(json.dumps({"impl": "reference", "unavailable": str(exc).splitlines()[0]}))
         return
-    line = {"impl": "reference", "metric": METRIC, "value": ref["value"], "unit": UNIT, "n_gpus": 0,
+    line = {"impl": "reference", "metric": metric_of(args), "value": ref["value"], "unit": UNIT, "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 * ref["seconds"] / max(1, args.steps), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -259,7 +278,7 @@ def ours(args):
     from fierro_gb300 import sgh
 
     t0 = time.time()
-    prob = workload(args.n, args.seed)
+    prob = workload(args.n, args.seed, args.problem)
     st = sgh.setup(prob)
     stream = torch.cuda.Stream()
     mode = sgh.FP_EXACT if args.fp_mode == "exact" else sgh.FP_FMA
@@ -355,7 +374,7 @@ def ours(args):
     if rank != 0:
         return
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "metric": metric_of(args), "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": dict(config_of(args), fp_mode=args.fp_mode),
