@@ -195,20 +195,21 @@ def alg_bytes(kind: str, nn: int, ne: int, nnz: int) -> float:
     return 0.0
 
 
-# Per-unit figures of the kernels from the ncu captures summarised in
+# Per-element figures of the kernels from ncu.  FP64 thread instructions per
+# element of one launch: the 64^3 captures summarised in
 # profiles/sgh_kernels_sedov64_ncu_full.md (exact mode) and
-# profiles/sgh_kernels_sedov64_fma_ncu.md (FMA mode), 64^3 case, above L2;
-# per-element DRAM bytes scale with the elements processed: FP64 thread
-# instructions and dram__bytes_read + dram__bytes_write per element of one
-# launch.  k_elem is the mean of its first-stage and last-stage (CFL) launches.
+# profiles/sgh_kernels_sedov64_fma_ncu.md (FMA mode).  DRAM bytes
+# (dram__bytes_read + dram__bytes_write) per element of one launch: the
+# one-pass capture of the 256^3 bench workload itself
+# (profiles/sgh_dram_sedov256.md; the memory traffic is the same in both
+# modes).  k_elem is the mean of its first-stage and last-stage (CFL) launches.
+DRAM_PER_ELEM_256 = {"k_force": 10053043883 / 16777216, "k_elem": 9796794624 / 16777216}
 NCU_PER_ELEM = {"exact": {
-    "k_force": {"fp64_ops": 138412032 / 262144, "dram_bytes": (104.519936e6 + 22.368256e6) / 262144},
-    "k_elem": {"fp64_ops": (158072832 + 171509792) / 2 / 262144,
-               "dram_bytes": (87.254784e6 + 25.970176e6 + 87.096064e6 + 26.185472e6) / 2 / 262144},
+    "k_force": {"fp64_ops": 138412032 / 262144, "dram_bytes": DRAM_PER_ELEM_256["k_force"]},
+    "k_elem": {"fp64_ops": (158072832 + 171509792) / 2 / 262144, "dram_bytes": DRAM_PER_ELEM_256["k_elem"]},
 }, "fma": {
-    "k_force": {"fp64_ops": 117964811 / 262144, "dram_bytes": (104.57088e6 + 21.069312e6) / 262144},
-    "k_elem": {"fp64_ops": (130809856 + 143716888) / 2 / 262144,
-               "dram_bytes": (87.258368e6 + 24.943616e6 + 87.229952e6 + 25.808896e6) / 2 / 262144},
+    "k_force": {"fp64_ops": 117964811 / 262144, "dram_bytes": DRAM_PER_ELEM_256["k_force"]},
+    "k_elem": {"fp64_ops": (130809856 + 143716888) / 2 / 262144, "dram_bytes": DRAM_PER_ELEM_256["k_elem"]},
 }}
 
 
