@@ -92,6 +92,35 @@ def test_setup_rejects_corrupt_meshes(lib_built):
         assert msg
 
 
+def test_setup_rejects_bad_mesh_headers(lib_built):
+    """Empty meshes, fewer nodes than one element needs, an unknown dimension and
+    meshes past the 32-bit device index range are refused from the header alone
+    (the arrays are not read)."""
+    from fierro_gb300 import sgh
+    prob = _deck()
+    nie = np.ascontiguousarray(prob.mesh.nodes_in_elem, dtype=np.uint64).copy()
+    xyz = np.ascontiguousarray(prob.mesh.coords, dtype=np.float64).copy()
+    st = sgh.empty_state(prob.mesh.num_nodes, prob.mesh.num_elems, prob.num_state_vars)
+    sv = np.ascontiguousarray(prob.state_vars())
+    cases = [(prob.mesh.num_nodes, 0, 0, "at least one element"),
+             (7, 1, 0, "at least one element"),
+             (prob.mesh.num_nodes, prob.mesh.num_elems, 1, "num_dims"),
+             (prob.mesh.num_nodes, 2 ** 28, 0, "32-bit"),
+             (2 ** 31, prob.mesh.num_elems, 0, "32-bit")]
+    for nn, ne, dims, text in cases:
+        m = sgh.Mesh(nn, ne, nie.ctypes.data, xyz.ctypes.data, dims)
+        rc = sgh.lib().fierro_sgh_setup(C.byref(m), sgh.c_materials(prob), len(prob.materials), sv.ctypes.data,
+                                        prob.num_state_vars, sgh.c_fills(prob), len(prob.fills),
+                                        sgh.c_boundaries(prob), len(prob.boundaries), C.byref(sgh.c_state(st)))
+        msg = sgh.lib().fierro_last_error().decode()
+        assert rc == sgh.FIERRO_EINVAL and text in msg, (nn, ne, dims, rc, msg)
+    m = sgh.Mesh(prob.mesh.num_nodes, prob.mesh.num_elems, None, xyz.ctypes.data, 0)
+    rc = sgh.lib().fierro_sgh_setup(C.byref(m), sgh.c_materials(prob), len(prob.materials), sv.ctypes.data,
+                                    prob.num_state_vars, sgh.c_fills(prob), len(prob.fills),
+                                    sgh.c_boundaries(prob), len(prob.boundaries), C.byref(sgh.c_state(st)))
+    assert rc == sgh.FIERRO_EINVAL and "NULL" in sgh.lib().fierro_last_error().decode()
+
+
 def test_setup_rejects_unsupported_models(lib_built):
     from fierro_gb300 import sgh
     prob = _deck()
