@@ -184,6 +184,39 @@ def noh(n: int = 32, length: float = 1.0, gamma: float = 5.0 / 3.0, speed: float
     return Problem("noh", mesh, [mat], fills, _planes_at_zero(), params)
 
 
+def taylor_anvil(mesh: HexMesh, cycles: int = 300) -> Problem:
+    """Taylor anvil 3D, the deck of the reference's own test
+    (tests-for-Explicit-Lagrange-Kokkos/input_for_TaylorAnvil3D_test.cpp:112-160,
+    mesh Explicit-Lagrange/meshes/mesh_z_taylorAnvil.geo, a quarter rod on an
+    O-grid): gamma 5/3 gas, rho=1, sie=1e-9, every node moving at w=-1 into the
+    reflecting plane z=0, symmetry planes x=0 and y=0; time_final 25."""
+    fills = [Fill("global", 0, den=1.0, sie=1.0e-9, velocity="cartesian", u=0.0, v=0.0, w=-1.0)]
+    params = Params(time_final=25.0, dt_cfl=0.4, cycle_stop=cycles)
+    mat = Material(q1=1.0, q1ex=1.0, q2=1.3333, q2ex=0.0, gamma=5.0 / 3.0, csmin=1.0e-14, cv=1.0)
+    return Problem("taylor_anvil", mesh, [mat], fills, _planes_at_zero(), params)
+
+
+def triple_point(mesh: HexMesh, cycles: int = 400) -> Problem:
+    """Triple point, the deck of the reference's input.cpp:482-593: gamma 5/3,
+    rho=1 / sie=2.5 everywhere, then the box x in [1, 7], y in [0, 1.5] at rho=1,
+    sie=0.25 and the box x in [1, 7], y in [1.5, 3] at rho=0.1, sie=2.5 (the
+    deck's three fills; its num_fills of 2 would drop the third); reflecting planes
+    on the six faces of the mesh's bounding box (the deck's x plane sits at 6.0,
+    "some meshes are 7 and others are 6": the far planes here are the mesh's own
+    extents); time_final 4."""
+    lo, hi = mesh.coords.min(axis=0), mesh.coords.max(axis=0)
+    fills = [
+        Fill("global", 0, den=1.0, sie=2.5, velocity="cartesian"),
+        Fill("box", 0, x1=1.0, x2=7.0, y1=0.0, y2=1.5, z1=0.0, z2=1.0, den=1.0, sie=0.25, velocity="cartesian"),
+        Fill("box", 0, x1=1.0, x2=7.0, y1=1.5, y2=3.0, z1=0.0, z2=1.0, den=0.1, sie=2.5, velocity="cartesian"),
+    ]
+    bcs = [Boundary("x_plane", float(lo[0])), Boundary("y_plane", float(lo[1])), Boundary("z_plane", float(lo[2])),
+           Boundary("x_plane", float(hi[0])), Boundary("y_plane", float(hi[1])), Boundary("z_plane", float(hi[2]))]
+    params = Params(time_final=4.0, dt_cfl=0.4, cycle_stop=cycles)
+    mat = Material(q1=1.0, q1ex=1.0, q2=1.3333, q2ex=0.0, gamma=5.0 / 3.0, csmin=1.0e-14, cv=1.0)
+    return Problem("triple_point", mesh, [mat], fills, bcs, params)
+
+
 def with_strength(problem: Problem, kind: str = "hypo", shear_modulus: float = 1.0) -> Problem:
     """The deck with every material given a strength model: ``kind`` is "hypo" or
     "hyper" (strength_type 1 or 2) and the shipped linear hypo-elastic model

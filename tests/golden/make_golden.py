@@ -17,8 +17,16 @@ model of oracle/ref/ref_user_mat.cpp assigned through material_t::strength_model
 on meshes from the box generator, and also store the stress bins and the
 element state variables.
 
+Unstructured-mesh cases (geo_*.npz) run the reference, with its own EnSight
+reader, on two more meshes it ships: mesh_z_taylorAnvil.geo (a quarter rod on an
+O-grid, nodes of valence 3 and 6) with the deck of its Taylor-anvil test
+(tests-for-Explicit-Lagrange-Kokkos/input_for_TaylorAnvil3D_test.cpp), and
+mesh_triple_30x18.geo with the triple-point deck of input.cpp.  These fixtures
+also carry the mesh (geo_<case>_mesh.npz: coordinates and 0-based connectivity
+as read from the .geo), so the tests run without the reference tree.
+
 Run from the repository root (needs the reference tree):
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [boxes strength rz geo]   (default: all)
 """
 import hashlib
 import json
@@ -64,15 +72,55 @@ def rz_cases():
     }
 
 
-def main():
+def geo_cases():
+    """Decks on shipped unstructured meshes: name -> (.geo file, deck builder, cycle counts)."""
+    from fierro_gb300 import problems
+    return {
+        "taylor_anvil": ("mesh_z_taylorAnvil.geo", problems.taylor_anvil, [1, 300]),
+        "triple_point": ("mesh_triple_30x18.geo", problems.triple_point, [1, 400]),
+    }
+
+
+def geo_problem(name: str, cycles: int):
+    """The deck of a geo case on the mesh stored beside the fixtures."""
+    from fierro_gb300 import mesh
+    m = np.load(os.path.join(HERE, "geo_%s_mesh.npz" % name))
+    hm = mesh.HexMesh(np.array(m["coords"]), np.array(m["nodes_in_elem"], dtype=np.int64), name=name)
+    return geo_cases()[name][1](hm, cycles=cycles)
+
+
+def make_geo(meta):
+    from fierro_gb300 import mesh
+    from oracle import orc
+    meta["geo"] = {}
+    for name, (geo, builder, cycles) in geo_cases().items():
+        path = os.path.join(MESHES, geo)
+        g = mesh.read_geo(path)
+        fn = os.path.join(HERE, "geo_%s_mesh.npz" % name)
+        np.savez_compressed(fn, coords=g.coords, nodes_in_elem=g.nodes_in_elem.astype(np.int32))
+        meta["geo"][name] = {"geo": geo, "mesh_file": os.path.basename(fn), "num_nodes": g.num_nodes,
+                             "num_elems": g.num_elems, "coords_sha256": digest(g.coords)}
+        for c in cycles:
+            prob = builder(g, cycles=c)
+            st = orc.run_reference(prob, cycles=c, kind="fierro_ref_geo", geo_path=path, threads=1)
+            out = {k: st[k] for k in FIELDS}
+            out["time"] = np.array(st["time"])
+            out["node_mass"] = st["node_mass"]
+            out["mass"] = st["mass"]
+            fo = os.path.join(HERE, "geo_%s_c%d.npz" % (name, c))
+            np.savez_compressed(fo, **out)
+            meta["geo"][name]["c%d" % c] = {"file": os.path.basename(fo), "time": float(st["time"]),
+                                            "deck": prob.config_text()}
+            print(fo, os.path.getsize(fo))
+
+
+def make_boxes(meta):
     from fierro_gb300 import mesh, problems
-    from oracle import build_ref, orc
-    build_ref.build_reference()
+    from oracle import orc
     cases = [
         ("sedov12", "mesh_12x12x12.geo", problems.sedov(12, geo_digits=5), [1, 200]),
         ("noh32", "mesh_Box_32.geo", problems.noh(32, geo_digits=5), [1, 500]),
     ]
-    meta = {}
     for name, geo, prob, cycles in cases:
         path = os.path.join(MESHES, geo)
         g = mesh.read_geo(path)
@@ -89,6 +137,10 @@ def main():
             np.savez_compressed(fn, **out)
             meta[name]["c%d" % c] = {"file": os.path.basename(fn), "time": float(st["time"])}
             print(fn, os.path.getsize(fn))
+
+
+def make_strength(meta):
+    from oracle import orc
     meta["strength"] = {}
     for name, prob in strength_cases().items():
         st = orc.run_reference(prob, threads=1)
@@ -99,6 +151,10 @@ def main():
         meta["strength"][name] = {"file": os.path.basename(fn), "time": float(st["time"]),
                                   "cycles": prob.params.cycle_stop, "deck": prob.config_text()}
         print(fn, os.path.getsize(fn))
+
+
+def make_rz(meta):
+    from oracle import orc
     meta["rz"] = {}
     for name, prob in rz_cases().items():
         st = orc.run_reference(prob, threads=1)
@@ -109,9 +165,19 @@ def main():
         meta["rz"][name] = {"file": os.path.basename(fn), "time": float(st["time"]),
                             "cycles": prob.params.cycle_stop, "deck": prob.config_text()}
         print(fn, os.path.getsize(fn))
-    with open(os.path.join(HERE, "golden.json"), "w") as f:
+
+
+def main(groups=("boxes", "strength", "rz", "geo")):
+    from oracle import build_ref
+    build_ref.build_reference()
+    meta_path = os.path.join(HERE, "golden.json")
+    meta = json.load(open(meta_path)) if os.path.exists(meta_path) else {}
+    makers = {"boxes": make_boxes, "strength": make_strength, "rz": make_rz, "geo": make_geo}
+    for g in groups:
+        makers[g](meta)
+    with open(meta_path, "w") as f:
         json.dump(meta, f, indent=1, sort_keys=True)
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]) or ("boxes", "strength", "rz", "geo"))
