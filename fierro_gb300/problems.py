@@ -217,6 +217,24 @@ def triple_point(mesh: HexMesh, cycles: int = 400) -> Problem:
     return Problem("triple_point", mesh, [mat], fills, bcs, params)
 
 
+def taylor_anvil_rz(nx: int = 40, ny: int = 4, length=(38.1, 3.81), cycles: int = 300, jitter: float = 0.0,
+                    seed: int = 0, permute: bool = False, mesh: HexMesh | None = None) -> Problem:
+    """2D-RZ Taylor anvil, the deck of the reference's own test
+    (tests-for-Explicit-Lagrange-Kokkos/input_for_TaylorAnvilRZ_test.cpp:112-151;
+    its mesh_taylorAnvil_2D_RZ.geo is not in the tree, so the rod is an nx x ny
+    quad mesh with the 3D rod's length and radius, x axial, y radial): gamma 5/3
+    gas, rho=1, sie=1e-9, every node moving at u=-1 into the reflecting plane
+    x=0, the axis y=0 reflecting; time_final 25."""
+    if mesh is None:
+        mesh = quad_mesh(nx, ny, length=length, jitter=jitter, seed=seed, permute=permute,
+                         name="taylor_anvil_rz%dx%d" % (nx, ny))
+    fills = [Fill("global", 0, den=1.0, sie=1.0e-9, velocity="cartesian", u=-1.0, v=0.0)]
+    params = Params(time_final=25.0, dt_cfl=0.4, cycle_stop=cycles)
+    mat = Material(q1=1.0, q1ex=1.0, q2=1.3333, q2ex=0.0, gamma=5.0 / 3.0, csmin=1.0e-14, cv=1.0)
+    bcs = [Boundary("x_plane", 0.0, "reflected"), Boundary("y_plane", 0.0, "reflected")]
+    return Problem("taylor_anvil_rz", mesh, [mat], fills, bcs, params)
+
+
 def with_strength(problem: Problem, kind: str = "hypo", shear_modulus: float = 1.0) -> Problem:
     """The deck with every material given a strength model: ``kind`` is "hypo" or
     "hyper" (strength_type 1 or 2) and the shipped linear hypo-elastic model

@@ -15,7 +15,7 @@ pytestmark = pytest.mark.gpu
 
 FIELDS = ("coords", "vel", "den", "pres", "sie", "sspd", "vol")
 EXTRA = ("corner_force", "div", "node_mass", "coords0", "vel0", "sie0", "stress", "stress0")
-CASES = ("sedov_rz16", "noh_rz16", "noh_rz12_jp", "sedov_rz12_jp_hypo")
+CASES = ("sedov_rz16", "noh_rz16", "noh_rz12_jp", "sedov_rz12_jp_hypo", "taylor_anvil_rz80x8_p")
 
 
 def _cases():
@@ -165,3 +165,20 @@ def test_rz_one_shot_solve_equals_handle(oracle_built, lib_built):
     for k, hk in (("coords", ("node_coords", 1)), ("vel", ("node_vel", 1)), ("sie", ("elem_sie", 1))):
         assert np.array_equal(host[hk[0]][hk[1]], g[k]), k
     assert np.array_equal(host["node_mass"], g["node_mass"])
+
+
+def test_rz_taylor_anvil_cooling_is_reported(oracle_built, lib_built):
+    """On the RZ Taylor anvil the scheme itself cools a cold element below zero
+    energy near t = 1.1 (the restatement, like the reference, then produces a
+    NaN sound speed); the GPU follows it bit for bit up to that cycle and the run
+    call reports FIERRO_ENUMERIC instead of continuing silently."""
+    from fierro_gb300 import problems, sgh
+    prob = problems.taylor_anvil_rz(40, 4, seed=8, permute=True, cycles=300)
+    g = _gpu(prob, cycles=160)
+    r = _oracle(prob, cycles=160)
+    assert_bitwise(g, r, FIELDS, label="taylor anvil rz 160")
+    with sgh.SGHSolver(prob) as s:
+        s.set_state(sgh.setup(prob))
+        with pytest.raises(sgh.FierroError) as ei:
+            s.run(300)
+        assert ei.value.code == sgh.FIERRO_ENUMERIC

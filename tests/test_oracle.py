@@ -157,7 +157,8 @@ def _rz_cases():
     return mg.rz_cases()
 
 
-@pytest.mark.parametrize("case", ["sedov_rz16", "noh_rz16", "noh_rz12_jp", "sedov_rz12_jp_hypo"])
+@pytest.mark.parametrize("case", ["sedov_rz16", "noh_rz16", "noh_rz12_jp", "sedov_rz12_jp_hypo",
+                                  "taylor_anvil_rz80x8_p"])
 def test_oracle_rz_equals_reference_golden(oracle_built, case):
     """2D-RZ: the C restatement of the num_dims == 2 branches (area-weighted
     force with hoop terms, RZ volume and divergence, radius-weighted energy,
