@@ -458,12 +458,13 @@ def batch_bench(args):
     probs = batch_workload(args.instances, args.seed, args.batch_cycles)
     states = [sgh.setup(p) for p in probs]
     ne_tot = sum(p.mesh.num_elems for p in probs)
-    with sgh.Batch(probs[:2]) as w:  # load the batch kernels
+    mode = sgh.FP_EXACT if args.fp_mode == "exact" else sgh.FP_FMA
+    with sgh.Batch(probs[:2], fp_mode=mode) as w:  # load the batch kernels
         w.set_state(0, states[0])
         w.set_state(1, states[1])
         w.run(3)
     stream = torch.cuda.Stream()
-    b = sgh.Batch(probs, stream=stream.cuda_stream)
+    b = sgh.Batch(probs, fp_mode=mode, stream=stream.cuda_stream)
     for i, st in enumerate(states):
         b.set_state(i, st)
     torch.cuda.synchronize()
@@ -475,7 +476,7 @@ def batch_bench(args):
     # the same instances one after another through the single-problem solver
     t_loop = 0.0
     for p, st in zip(probs, states):
-        with sgh.SGHSolver(p) as s:
+        with sgh.SGHSolver(p, fp_mode=mode) as s:
             s.set_state(st)
             torch.cuda.synchronize()
             t1 = time.perf_counter()
@@ -490,7 +491,7 @@ def batch_bench(args):
             "element_cycles_per_s": sum(p.mesh.num_elems * c for p, c in zip(probs, cycles_done)) / t_batch,
             "instances_stopped_early": int(sum(c < args.batch_cycles for c in cycles_done)),
             "config": {"workload": "ensemble", "instances": n, "cycles": args.batch_cycles, "seed": args.seed,
-                       "launches_per_cycle": 8, "timing": "host wall clock around fierro_batch_run / "
+                       "fp_mode": args.fp_mode, "launches_per_cycle": 8, "timing": "host wall clock around fierro_batch_run / "
                        "fierro_sgh_run (each synchronises)"}}
     print(json.dumps(line))
 
