@@ -104,11 +104,18 @@ def test_rz_energy_conserved(oracle_built, lib_built):
     assert abs(ie1 - r["energy"][0]) <= 1e-13 * ie0 and abs(ke1 - r["energy"][1]) <= 1e-13 * ie0
 
 
-def test_rz_fma_mode_within_tolerance(oracle_built, lib_built):
-    prob = _cases()["noh_rz12_jp"]
+@pytest.mark.parametrize("case", CASES)
+def test_rz_fma_mode_within_tolerance(oracle_built, lib_built, case):
+    """FMA mode in 2D-RZ: the gated fields within 1e-12 of the reference's
+    arithmetic after one cycle and 1e-9 after the full run."""
+    gated = ("coords", "vel", "den", "pres", "sie")
+    prob = _cases()[case]
+    g1 = _gpu(prob, cycles=1, mode=1)
+    r1 = _oracle(prob, cycles=1)
+    assert_fields(g1, r1, 1e-12, keys=gated, label="fma %s 1 cycle" % case)
     g = _gpu(prob, cycles=prob.params.cycle_stop, mode=1)
     r = _oracle(prob, cycles=prob.params.cycle_stop)
-    assert_fields(g, r, 1e-9, keys=FIELDS + ("node_mass",), label="fma noh_rz12_jp")
+    assert_fields(g, r, 1e-9, keys=FIELDS + ("node_mass",), label="fma %s" % case)
 
 
 def test_rz_timed_launches(lib_built):
@@ -182,3 +189,15 @@ def test_rz_taylor_anvil_cooling_is_reported(oracle_built, lib_built):
         with pytest.raises(sgh.FierroError) as ei:
             s.run(300)
         assert ei.value.code == sgh.FIERRO_ENUMERIC
+
+
+def test_rz_fma_mode_gates_on_the_bench_mesh_family(lib_built):
+    """The RZ benchmark's mesh family (jittered, permuted RZ Sedov, source radius
+    1.2/64) at 1024^2: the FMA mode against the exact mode (the reference's
+    arithmetic bit for bit) after one cycle (1e-12) and after 20 (1e-9)."""
+    from fierro_gb300 import problems
+    prob = problems.sedov_rz(1024, jitter=0.1, seed=2024, permute=True, cycles=20, source_radius=1.2 / 64)
+    for cyc, tol in ((1, 1e-12), (20, 1e-9)):
+        g = _gpu(prob, cycles=cyc, mode=1)
+        r = _gpu(prob, cycles=cyc, mode=0)
+        assert_fields(g, r, tol, keys=("coords", "vel", "den", "pres", "sie"), label="rz1024 fma %d" % cyc)

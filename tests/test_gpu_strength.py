@@ -96,11 +96,19 @@ def test_exact_vs_reference_golden(lib_built, case):
     assert_fields(g, ref, 1e-9, keys=FIELDS + ("stress", "stress0"), label=case)
 
 
-def test_fma_mode_within_tolerance(oracle_built, lib_built):
-    prob = _cases()["sedov10_mixed"]
+@pytest.mark.parametrize("case", CASES)
+def test_fma_mode_within_tolerance(oracle_built, lib_built, case):
+    """FMA mode with strength: positions, velocities, density, pressure and
+    energy within 1e-12 of the reference's arithmetic after one cycle and 1e-9
+    after the full run."""
+    gated = ("coords", "vel", "den", "pres", "sie")
+    prob = _cases()[case]
+    g1 = _gpu(prob, cycles=1, mode=1)
+    r1 = _oracle(prob, cycles=1)
+    assert_fields(g1, r1, 1e-12, keys=gated, label="fma %s 1 cycle" % case)
     g = _gpu(prob, cycles=prob.params.cycle_stop, mode=1)
     r = _oracle(prob, cycles=prob.params.cycle_stop)
-    assert_fields(g, r, 1e-9, keys=FIELDS + ("stress",), label="fma sedov10_mixed")
+    assert_fields(g, r, 1e-9, keys=FIELDS + ("stress",), label="fma %s" % case)
 
 
 def test_nonzero_initial_stress_and_history(oracle_built, lib_built):
