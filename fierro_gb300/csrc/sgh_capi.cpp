@@ -521,7 +521,7 @@ static int set_state_impl(fierro_sgh* h, const fierro_sgh_state* s, double time_
   const HostTopo& t = h->topo;
   h->has_state = false;
   TRY(size_statev(h, nsv));
-  if (h->dims == 2) {
+  if (h->dims == 2 && !h->direct_host) {
     TRY(rz::set_state(h, s));
     return finish_set_state(h, time_value, graphics_time, dt);
   }
@@ -640,19 +640,20 @@ extern "C" int fierro_sgh_get_state(fierro_sgh* h, fierro_sgh_state* s) {
   // the divergence the last executed stage used (reference elem_div)
   const long long stages_done = cyc * h->rk_num_stages + h->stage;
   const int qb = stages_done == 0 ? 1 : (int)((stages_done - 1) & 1);
-  if (h->dims == 2) return rz::get_state(h, s, bins, qb);
+  if (h->dims == 2 && !h->direct_host) return rz::get_state(h, s, bins, qb);
   if (h->direct_host) {
     // the kernels write the caller's arrays: make their pages resident first
     // (a GPU fault per untouched page costs far more than a host store per page)
     const size_t nb = sizeof(double);
-    populate(s->node_coords, nb * nn * 6);
-    populate(s->node_vel, nb * nn * 6);
+    const size_t D = h->dims == 2 ? 2 : 3;
+    populate(s->node_coords, nb * nn * 2 * D);
+    populate(s->node_vel, nb * nn * 2 * D);
     populate(s->node_mass, nb * nn);
     populate(s->elem_sie, nb * ne * 2);
     double* e1[] = {s->elem_den, s->elem_pres, s->elem_sspd, s->elem_vol, s->elem_div, s->elem_mass};
     for (double* p : e1) populate(p, nb * ne);
     populate(s->elem_stress, nb * ne * 18);
-    populate(s->corner_force, nb * ne * 24);
+    populate(s->corner_force, nb * ne * (D == 2 ? 8 : 24));
     if (h->strength) populate(s->elem_statev, nb * ne * (size_t)h->nsv);
     return xfer::download_state(h, s, bins, qb);
   }

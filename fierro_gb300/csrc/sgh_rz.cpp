@@ -6,6 +6,7 @@
 // Compiled with -ffp-contract=off so the set-up doubles are uncontracted.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <vector>
@@ -13,6 +14,7 @@
 #include "sgh_handle.h"
 #include "sgh_rz.h"
 #include "sgh_user_mat.cuh"
+#include "sgh_xfer.h"
 
 namespace fierro {
 
@@ -282,7 +284,12 @@ int create(fierro_sgh* h, const fierro_mesh* mesh, const fierro_material* materi
     return set_error(FIERRO_ENOTSUP, "hyper strength models on a 2D-RZ mesh: the reference's update_state2D "
                      "(properties.cpp:146-160) writes 3D corner normals into a 2D array");
   TRY(build_topology_rz(mesh, boundaries, num_bcs, &h->topo));
-  h->direct_host = false;
+  {
+    // set/get_state through the transfer kernels (sgh_xfer.cu) where the GPU
+    // dereferences host memory, staged through pinned buffers otherwise
+    const char* env = std::getenv("FIERRO_STAGED_TRANSFERS");
+    h->direct_host = xfer::direct_host_access() && !(env && env[0] == '1');
+  }
   h->rks = (h->fp_mode == FIERRO_FP_EXACT) ? &rz_kernels_exact() : &rz_kernels_fma();
   const size_t nn = (size_t)h->nn, ne = (size_t)h->ne;
   const HostTopo& t = h->topo;
@@ -329,6 +336,17 @@ int create(fierro_sgh* h, const fierro_mesh* mesh, const fierro_material* materi
     std::vector<int32_t> m32(ne);
     for (size_t j = 0; j < ne; ++j) m32[j] = (int32_t)t.elem_int2ext[j];
     TRY(upload_raw(h, h->d_elem_int2ext, m32.data(), sizeof(int32_t) * ne));
+  }
+  if (h->direct_host) {
+    // caller -> internal maps and the validation word of the transfer kernels
+    TRY(dalloc(h, &h->d_node_ext2int, nn));
+    TRY(dalloc(h, &h->d_elem_ext2int, ne));
+    TRY(dalloc(h, &h->d_xfer, 1));
+    std::vector<int32_t> m32(std::max(nn, ne));
+    for (size_t j = 0; j < nn; ++j) m32[j] = (int32_t)t.node_ext2int[j];
+    TRY(upload_raw(h, h->d_node_ext2int, m32.data(), sizeof(int32_t) * nn));
+    for (size_t j = 0; j < ne; ++j) m32[j] = (int32_t)t.elem_ext2int[j];
+    TRY(upload_raw(h, h->d_elem_ext2int, m32.data(), sizeof(int32_t) * ne));
   }
   TRY(dalloc(h, &h->d_axis, t.axis_nodes.size()));
   TRY(dalloc(h, &h->d_axis_nin_start, t.axis_nin_start.size()));

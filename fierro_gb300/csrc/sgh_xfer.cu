@@ -30,9 +30,9 @@ __device__ __forceinline__ void flag(XferStatus* st, int which, long long idx) {
 }
 
 struct NodeUp {
-  int nn;
+  int nn, dims;                        // dims: 3 (hex) or 2 (2D-RZ quads)
   const int* ext2int;
-  const double *coords, *vel, *mass;  // [2][nn][3], [2][nn][3], [nn]
+  const double *coords, *vel, *mass;  // [2][nn][dims], [2][nn][dims], [nn]
   double* x[2][3];                     // device bin b receives reference bin b ^ 1
   double* v[2][3];
   double* node_mass;
@@ -45,18 +45,18 @@ __global__ void __launch_bounds__(kBlock) k_up_nodes(const NodeUp a) {
   const int j = j0 + threadIdx.x;
   const int cnt = min(kBlock, a.nn - j0);
   const int i = j < a.nn ? a.ext2int[j] : 0;
+  const int D = a.dims;
   for (int what = 0; what < 2; ++what) {
     const double* in = what == 0 ? a.coords : a.vel;
     for (int rb = 0; rb < 2; ++rb) {
-      const double* src = in + ((size_t)rb * a.nn + j0) * 3;
+      const double* src = in + ((size_t)rb * a.nn + j0) * D;
       __syncthreads();
-      for (int k = threadIdx.x; k < cnt * 3; k += kBlock) buf[k] = src[k];
+      for (int k = threadIdx.x; k < cnt * D; k += kBlock) buf[k] = src[k];
       __syncthreads();
       if (j < a.nn)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          if (what == 0) a.x[rb ^ 1][d][i] = buf[threadIdx.x * 3 + d];
-          else a.v[rb ^ 1][d][i] = buf[threadIdx.x * 3 + d];
+        for (int d = 0; d < D; ++d) {
+          if (what == 0) a.x[rb ^ 1][d][i] = buf[threadIdx.x * D + d];
+          else a.v[rb ^ 1][d][i] = buf[threadIdx.x * D + d];
         }
     }
   }
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(kBlock) k_check_zero(const double* p, long lon
 }
 
 struct NodeDown {
-  int nn;
+  int nn, dims;
   const int* ext2int;
   double *coords, *vel, *mass;  // may be null
   const double* x[2][3];        // reference bin rb comes from device bin bins[rb]
@@ -142,23 +142,24 @@ __global__ void __launch_bounds__(kBlock) k_down_nodes(const NodeDown a) {
   const int cnt = min(kBlock, a.nn - j0);
   const int i = j < a.nn ? a.ext2int[j] : 0;
   if (a.mass && j < a.nn) a.mass[j] = a.node_mass[i];
+  const int D = a.dims;
   for (int what = 0; what < 2; ++what) {
     double* out = what == 0 ? a.coords : a.vel;
     if (!out) continue;
     for (int rb = 0; rb < 2; ++rb) {
       __syncthreads();
       if (j < a.nn)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) buf[threadIdx.x * 3 + d] = what == 0 ? a.x[rb][d][i] : a.v[rb][d][i];
+        for (int d = 0; d < D; ++d) buf[threadIdx.x * D + d] = what == 0 ? a.x[rb][d][i] : a.v[rb][d][i];
       __syncthreads();
-      double* o = out + ((size_t)rb * a.nn + j0) * 3;
-      for (int k = threadIdx.x; k < cnt * 3; k += kBlock) o[k] = buf[k];
+      double* o = out + ((size_t)rb * a.nn + j0) * D;
+      for (int k = threadIdx.x; k < cnt * D; k += kBlock) o[k] = buf[k];
     }
   }
 }
 
 struct ElemDown {
   int ne, nsv;
+  int force_rows;  // corner-force values per element: 24 (hex) or 8 (quad)
   const int* ext2int;
   double *sie, *den, *pres, *sspd, *vol, *div, *mass, *stress, *corner_force, *statev;  // may be null
   const double* d_sie[2];  // reference bin rb
@@ -205,20 +206,22 @@ __global__ void __launch_bounds__(kBlock) k_down_elems(const ElemDown a) {
   }
 }
 
-// Corner forces, device [lid*3+dim][e] -> reference [(E*8+lid)*3+dim], 64
-// elements (1536 values) per block staged in shared memory.
+// Corner forces, device [lid*dims+dim][e] -> reference [(E*npe+lid)*dims+dim]
+// (R = npe*dims = 24 or 8 values per element), 64 elements per block staged in
+// shared memory.
 constexpr int kForceChunk = 64;
 __global__ void __launch_bounds__(kBlock) k_down_force(const ElemDown a) {
   __shared__ double buf[kForceChunk * 24];
+  const int R = a.force_rows;
   const int E0 = blockIdx.x * kForceChunk;
   const int cnt = min(kForceChunk, a.ne - E0);
-  for (int k = threadIdx.x; k < cnt * 24; k += kBlock) {
-    const int E = E0 + k / 24, r = k % 24;
+  for (int k = threadIdx.x; k < cnt * R; k += kBlock) {
+    const int E = E0 + k / R, r = k % R;
     buf[k] = a.d_force[(size_t)r * a.ne + a.ext2int[E]];
   }
   __syncthreads();
-  double* o = a.corner_force + (size_t)E0 * 24;
-  for (int k = threadIdx.x; k < cnt * 24; k += kBlock) o[k] = buf[k];
+  double* o = a.corner_force + (size_t)E0 * R;
+  for (int k = threadIdx.x; k < cnt * R; k += kBlock) o[k] = buf[k];
 }
 
 // Snapshot of the state for a graphics dump, in the caller's numbering, with
@@ -310,14 +313,16 @@ int upload_state(fierro_sgh* h, const fierro_sgh_state* s, XferStatus* host_stat
   init.flags = 0;
   for (int k = 0; k < XferStatus::COUNT; ++k) init.first[k] = LLONG_MAX;
   CUDA_TRY(cudaMemcpyAsync(h->d_xfer, &init, sizeof(init), cudaMemcpyHostToDevice, stream));
+  const int D = h->dims == 2 ? 2 : 3;
   NodeUp nu{};
   nu.nn = nn;
+  nu.dims = D;
   nu.ext2int = h->d_node_ext2int;
   nu.coords = s->node_coords;
   nu.vel = s->node_vel;
   nu.mass = s->node_mass;
   for (int b = 0; b < 2; ++b)
-    for (int d = 0; d < 3; ++d) {
+    for (int d = 0; d < D; ++d) {
       nu.x[b][d] = h->d_x[b][d];
       nu.v[b][d] = h->d_v[b][d];
     }
@@ -378,15 +383,17 @@ int upload_state(fierro_sgh* h, const fierro_sgh_state* s, XferStatus* host_stat
 int download_state(fierro_sgh* h, fierro_sgh_state* s, const int bins[2], int div_buffer) {
   const int nn = (int)h->nn, ne = (int)h->ne;
   cudaStream_t stream = h->stream;
+  const int D = h->dims == 2 ? 2 : 3;
   if (s->node_coords || s->node_vel || s->node_mass) {
     NodeDown nd{};
     nd.nn = nn;
+    nd.dims = D;
     nd.ext2int = h->d_node_ext2int;
     nd.coords = s->node_coords;
     nd.vel = s->node_vel;
     nd.mass = s->node_mass;
     for (int rb = 0; rb < 2; ++rb)
-      for (int d = 0; d < 3; ++d) {
+      for (int d = 0; d < D; ++d) {
         nd.x[rb][d] = h->d_x[bins[rb]][d];
         nd.v[rb][d] = h->d_v[bins[rb]][d];
       }
@@ -395,6 +402,7 @@ int download_state(fierro_sgh* h, fierro_sgh_state* s, const int bins[2], int di
   }
   ElemDown ed{};
   ed.ne = ne;
+  ed.force_rows = D == 2 ? 8 : 24;
   ed.ext2int = h->d_elem_ext2int;
   ed.sie = s->elem_sie;
   ed.den = s->elem_den;
