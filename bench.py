@@ -813,7 +813,8 @@ def rz_bench(args):
         e2e = {"value": ne * args.steps / med[0], "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
                "d2h_bytes_per_step": d2h / args.steps, "upload_s": med[1], "run_s": med[2], "download_s": med[3],
                "path": "fierro_sgh_set_state + fierro_sgh_run(K) + fierro_sgh_get_state with host buffers in the "
-                       "reference's 2D layouts (staged through pinned buffers on this path); median of three"}
+                       "reference's 2D layouts (the GPU reading and writing the host arrays over NVLink-C2C); "
+                       "median of three"}
     nnz = 8 * ne  # a quad's node-sharing neighbours: 8 inside the mesh
     dom = max(("k_force", "k_node", "k_elem"), key=lambda k: per[k])
     dom_ms = per[dom] / launches[dom]
