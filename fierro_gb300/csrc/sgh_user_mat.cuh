@@ -1,5 +1,5 @@
 // User strength model: the role of the reference's user_strength_model
-// (user_mat.cpp:57-97), compiled into the cycle kernels.  Replace the body of
+// (user_mat.cpp:50-84), compiled into the cycle kernels.  Replace the body of
 // user_strength_model and rebuild the library to run another model; the call
 // sites and the arguments stay.
 //

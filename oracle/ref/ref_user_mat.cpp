@@ -1,6 +1,6 @@
 // The test strength model handed to the reference through material_t's
 // strength_model pointer (state.h:150-164), in the role of the reference's
-// user_strength_model (user_mat.cpp:57-97), which is an empty stub.  Linked only
+// user_strength_model (user_mat.cpp:50-84), which is an empty stub.  Linked only
 // into the reference oracle executables (oracle/build_ref.py); the deck keyword
 // "strength <mat_id> <type>" of oracle/ref/ref_input.cpp selects it.
 //
