@@ -66,7 +66,7 @@ class SGHFunction:
 
 def eos_state(state0: dict, sie0: np.ndarray, gamma: np.ndarray) -> dict:
     """A copy of a set-up state with sie replaced and pressure / sound speed
-    recomputed by the ideal-gas EOS (eos.cpp:85-98), for the oracle."""
+    recomputed by the ideal-gas EOS (eos.cpp:35-43), for the oracle."""
     st = {k: v.copy() for k, v in state0.items()}
     st["elem_sie"][:] = sie0[None, :]
     st["elem_statev"][:, 0] = gamma

@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(kElemBlock) k_elem(const ElemArgs a) {
     double sspd;
     if (KIND != 2) {
       a.vol[e] = vol;
-      // update_state (properties.cpp:39, eos.cpp:85-98)
+      // update_state (properties.cpp:39, 98-109; ideal_gas eos.cpp:35-43)
       const double den = a.mass[e] / vol;
       if (STRENGTH) {
         const int mat = a.mat[e];
