@@ -57,6 +57,29 @@ def test_reference_arm_line():
     assert line["e2e"]["h2d_bytes_per_step"] == 0
 
 
+def test_reference_arm_two_ranks_prints_once():
+    """Under torchrun with two ranks (gloo here) rank 0 alone runs the reference
+    arm and prints its line; rank 1 exits 0 without output."""
+    import socket
+    from oracle import orc
+    if not orc.reference_available("fierro_ref_fast"):
+        from oracle import build_ref
+        if build_ref.build_reference() is None:
+            pytest.skip("reference sources unavailable")
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    p = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+                        "--master-addr", "127.0.0.1", "--master-port", str(port),
+                        os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2", "--cpu-n", "8",
+                        "--steps", "1", "--warmup", "0"], capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [ln for ln in p.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, p.stdout
+    assert json.loads(lines[0])["impl"] == "reference"
+
+
 def test_alg_bytes_model():
     import bench
     n = 64
