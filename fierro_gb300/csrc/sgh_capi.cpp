@@ -508,6 +508,27 @@ static int size_statev(fierro_sgh* h, int64_t nsv) {
   return build_graphs(h);
 }
 
+// The first index of a non-zero value (-1 if none), over all host threads.
+static long long first_nonzero(const double* p, int64_t n) {
+  long long first = -1;
+#pragma omp parallel
+  {
+    long long mine = -1;
+#pragma omp for schedule(static)
+    for (int64_t i = 0; i < n; ++i)
+      if (p[i] != 0.0 && mine < 0) mine = i;
+#pragma omp critical
+    if (mine >= 0 && (first < 0 || mine < first)) first = mine;
+  }
+  return first;
+}
+
+// p[0..n) = 0.0, over all host threads.
+static void zero_parallel(double* p, size_t n) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < (int64_t)n; ++i) p[i] = 0.0;
+}
+
 static int set_state_impl(fierro_sgh* h, const fierro_sgh_state* s, double time_value, double graphics_time,
                           double dt) {
   if (!s || !s->node_coords || !s->node_vel || !s->node_mass || !s->elem_den || !s->elem_pres || !s->elem_sspd ||
@@ -531,7 +552,18 @@ static int set_state_impl(fierro_sgh* h, const fierro_sgh_state* s, double time_
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     output_reset(h);
     XferStatus xs{};
-    TRY(xfer::upload_state(h, s, &xs));
+    // a gas-only handle needs the caller's stress to be zero: the host checks it
+    // while the GPU reads the rest of the state
+    const bool host_check = s->elem_stress && !h->strength;
+    fierro_sgh_state sg = *s;
+    if (host_check) sg.elem_stress = nullptr;
+    TRY(xfer::upload_state(h, &sg, &xs, false));
+    const long long nonzero = host_check ? first_nonzero(s->elem_stress, ne * 18) : -1;
+    TRY(xfer::finish_upload(h, &xs));
+    if (nonzero >= 0) {
+      xs.flags |= 1u << XferStatus::STRESS;
+      xs.first[XferStatus::STRESS] = nonzero;
+    }
     if (xs.flags & (1u << XferStatus::STRESS))
       return set_error(FIERRO_ENOTSUP, "set_state: non-zero stress (value %lld) needs a handle with a strength "
                        "material", xs.first[XferStatus::STRESS]);
@@ -652,10 +684,18 @@ extern "C" int fierro_sgh_get_state(fierro_sgh* h, fierro_sgh_state* s) {
     populate(s->elem_sie, nb * ne * 2);
     double* e1[] = {s->elem_den, s->elem_pres, s->elem_sspd, s->elem_vol, s->elem_div, s->elem_mass};
     for (double* p : e1) populate(p, nb * ne);
-    populate(s->elem_stress, nb * ne * 18);
     populate(s->corner_force, nb * ne * (D == 2 ? 8 : 24));
     if (h->strength) populate(s->elem_statev, nb * ne * (size_t)h->nsv);
-    return xfer::download_state(h, s, bins, qb);
+    // a gas-only handle's stress is zero: the host writes it while the GPU
+    // writes the rest
+    const bool host_zero = s->elem_stress && !h->strength;
+    if (!host_zero) populate(s->elem_stress, nb * ne * 18);
+    fierro_sgh_state sg = *s;
+    if (host_zero) sg.elem_stress = nullptr;
+    TRY(xfer::download_state(h, &sg, bins, qb, false));
+    if (host_zero) zero_parallel(s->elem_stress, (size_t)ne * 18);
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return FIERRO_OK;
   }
   for (int rb = 0; rb < 2; ++rb)
     for (int d = 0; d < 3; ++d) {

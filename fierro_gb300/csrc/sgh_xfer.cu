@@ -306,7 +306,7 @@ bool direct_host_access() {
   return v != 0;
 }
 
-int upload_state(fierro_sgh* h, const fierro_sgh_state* s, XferStatus* host_status) {
+int upload_state(fierro_sgh* h, const fierro_sgh_state* s, XferStatus* host_status, bool wait) {
   const int nn = (int)h->nn, ne = (int)h->ne;
   cudaStream_t stream = h->stream;
   XferStatus init{};
@@ -375,12 +375,16 @@ int upload_state(fierro_sgh* h, const fierro_sgh_state* s, XferStatus* host_stat
     k_check_zero<<<sms * 8, kBlock, 0, stream>>>(s->elem_stress, (long long)ne * 18, h->d_xfer);
   }
   CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaMemcpyAsync(host_status, h->d_xfer, sizeof(XferStatus), cudaMemcpyDeviceToHost, stream));
-  CUDA_TRY(cudaStreamSynchronize(stream));
+  return wait ? finish_upload(h, host_status) : FIERRO_OK;
+}
+
+int finish_upload(fierro_sgh* h, XferStatus* host_status) {
+  CUDA_TRY(cudaMemcpyAsync(host_status, h->d_xfer, sizeof(XferStatus), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
   return FIERRO_OK;
 }
 
-int download_state(fierro_sgh* h, fierro_sgh_state* s, const int bins[2], int div_buffer) {
+int download_state(fierro_sgh* h, fierro_sgh_state* s, const int bins[2], int div_buffer, bool wait) {
   const int nn = (int)h->nn, ne = (int)h->ne;
   cudaStream_t stream = h->stream;
   const int D = h->dims == 2 ? 2 : 3;
@@ -432,7 +436,7 @@ int download_state(fierro_sgh* h, fierro_sgh_state* s, const int bins[2], int di
   k_down_elems<<<blocks(ne), kBlock, 0, stream>>>(ed);
   if (s->corner_force) k_down_force<<<(unsigned)((ne + kForceChunk - 1) / kForceChunk), kBlock, 0, stream>>>(ed);
   CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaStreamSynchronize(stream));
+  if (wait) CUDA_TRY(cudaStreamSynchronize(stream));
   return FIERRO_OK;
 }
 

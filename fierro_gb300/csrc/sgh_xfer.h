@@ -29,12 +29,17 @@ bool direct_host_access();
 // validation result; the state on the device is the caller's even when a check
 // failed (the caller then discards it).  A strength handle also takes the stress
 // bins and all num_state_vars state variables (h->d_statev sized for them).
-int upload_state(fierro_sgh* h, const fierro_sgh_state* s, XferStatus* status);
+// With wait == false the transfers are only enqueued on the handle's stream and
+// `status` is not written: the caller does host work meanwhile, then calls
+// finish_upload.
+int upload_state(fierro_sgh* h, const fierro_sgh_state* s, XferStatus* status, bool wait = true);
+int finish_upload(fierro_sgh* h, XferStatus* status);
 // Writes the handle's state into the non-null fields of `s`: reference bin rb
 // from device bin bins[rb]; elem_div from divergence buffer div_buffer.  On a
 // handle with strength materials the stress bins and the state variables come
 // from the device; otherwise the stress is zero and elem_statev is not written.
-int download_state(fierro_sgh* h, fierro_sgh_state* s, const int bins[2], int div_buffer);
+// wait == false: enqueued only; the caller synchronises the handle's stream.
+int download_state(fierro_sgh* h, fierro_sgh_state* s, const int bins[2], int div_buffer, bool wait = true);
 
 // Graphics-dump snapshots (write_outputs, outputs.cpp:10-506): one slot of the
 // device ring holds, in the caller's numbering, node rows x, y, z, u, v, w
