@@ -235,6 +235,26 @@ def taylor_anvil_rz(nx: int = 40, ny: int = 4, length=(38.1, 3.81), cycles: int 
     return Problem("taylor_anvil_rz", mesh, [mat], fills, bcs, params)
 
 
+def sod_rz(nx: int = 100, ny: int = 2, cycles: int = 400, jitter: float = 0.0, seed: int = 0,
+           permute: bool = False, mesh: HexMesh | None = None) -> Problem:
+    """Sod shock tube along the axis in 2D-RZ, the SodZ deck of the reference's
+    input.cpp:393-478: gamma 1.4, rho=1 and sie=2.5 everywhere, then rho=0.125 (same
+    sie) in the box x in [0.5, 1]; reflecting planes x=0, y=0, x=1 and y=0.1 on an
+    nx x ny quad mesh of [0, 1] x [0, 0.1] (x axial, y radial); time_final 0.2."""
+    if mesh is None:
+        mesh = quad_mesh(nx, ny, length=(1.0, 0.1), jitter=jitter, seed=seed, permute=permute,
+                         name="sod_rz%dx%d" % (nx, ny))
+    fills = [
+        Fill("global", 0, den=1.0, sie=2.5, velocity="cartesian"),
+        Fill("box", 0, x1=0.5, x2=1.0, y1=0.0, y2=1.0, z1=0.0, z2=1.0, den=0.125, sie=2.5, velocity="cartesian"),
+    ]
+    params = Params(time_final=0.2, dt_cfl=0.4, cycle_stop=cycles)
+    mat = Material(q1=1.0, q1ex=1.0, q2=1.3333, q2ex=0.0, gamma=1.4, csmin=1.0e-14, cv=1.0)
+    bcs = [Boundary("x_plane", 0.0, "reflected"), Boundary("y_plane", 0.0, "reflected"),
+           Boundary("x_plane", 1.0, "reflected"), Boundary("y_plane", 0.1, "reflected")]
+    return Problem("sod_rz", mesh, [mat], fills, bcs, params)
+
+
 def with_strength(problem: Problem, kind: str = "hypo", shear_modulus: float = 1.0) -> Problem:
     """The deck with every material given a strength model: ``kind`` is "hypo" or
     "hyper" (strength_type 1 or 2) and the shipped linear hypo-elastic model

@@ -72,6 +72,7 @@ def rz_cases():
         # 150 cycles (t = 0.93): the scheme itself (reference and restatement alike)
         # drives a cold element's energy negative near t = 1.1-1.3 on this deck
         "taylor_anvil_rz80x8_p": problems.taylor_anvil_rz(80, 8, seed=8, permute=True, cycles=150),
+        "sod_rz100x2_p": problems.sod_rz(100, 2, seed=4, permute=True, cycles=400),
     }
 
 

@@ -15,7 +15,7 @@ pytestmark = pytest.mark.gpu
 
 FIELDS = ("coords", "vel", "den", "pres", "sie", "sspd", "vol")
 EXTRA = ("corner_force", "div", "node_mass", "coords0", "vel0", "sie0", "stress", "stress0")
-CASES = ("sedov_rz16", "noh_rz16", "noh_rz12_jp", "sedov_rz12_jp_hypo", "taylor_anvil_rz80x8_p")
+CASES = ("sedov_rz16", "noh_rz16", "noh_rz12_jp", "sedov_rz12_jp_hypo", "taylor_anvil_rz80x8_p", "sod_rz100x2_p")
 
 
 def _cases():

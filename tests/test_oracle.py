@@ -158,7 +158,7 @@ def _rz_cases():
 
 
 @pytest.mark.parametrize("case", ["sedov_rz16", "noh_rz16", "noh_rz12_jp", "sedov_rz12_jp_hypo",
-                                  "taylor_anvil_rz80x8_p"])
+                                  "taylor_anvil_rz80x8_p", "sod_rz100x2_p"])
 def test_oracle_rz_equals_reference_golden(oracle_built, case):
     """2D-RZ: the C restatement of the num_dims == 2 branches (area-weighted
     force with hoop terms, RZ volume and divergence, radius-weighted energy,
