@@ -255,6 +255,25 @@ def sod_rz(nx: int = 100, ny: int = 2, cycles: int = 400, jitter: float = 0.0, s
     return Problem("sod_rz", mesh, [mat], fills, bcs, params)
 
 
+def sod_3d(mesh: HexMesh, cycles: int = 400) -> Problem:
+    """Sod shock tube along x on a hex mesh of [0, 1] x [0, w] x [0, w]: the values
+    of the SodZ deck (input.cpp:393-478: gamma 1.4, rho=1 and sie=2.5, then rho=0.125
+    in x in [0.5, 1]) in 3D, with reflecting planes on the six faces of the mesh's
+    bounding box; time_final 0.2.  On the reference's skewed Saltzman mesh
+    (Explicit-Lagrange/meshes/mesh_Saltzman.geo) it exercises non-orthogonal hexes."""
+    lo, hi = mesh.coords.min(axis=0), mesh.coords.max(axis=0)
+    fills = [
+        Fill("global", 0, den=1.0, sie=2.5, velocity="cartesian"),
+        Fill("box", 0, x1=0.5, x2=1.0, y1=float(lo[1]), y2=float(hi[1]), z1=float(lo[2]), z2=float(hi[2]),
+             den=0.125, sie=2.5, velocity="cartesian"),
+    ]
+    bcs = [Boundary("x_plane", float(lo[0])), Boundary("y_plane", float(lo[1])), Boundary("z_plane", float(lo[2])),
+           Boundary("x_plane", float(hi[0])), Boundary("y_plane", float(hi[1])), Boundary("z_plane", float(hi[2]))]
+    params = Params(time_final=0.2, dt_cfl=0.4, cycle_stop=cycles)
+    mat = Material(q1=1.0, q1ex=1.0, q2=1.3333, q2ex=0.0, gamma=1.4, csmin=1.0e-14, cv=1.0)
+    return Problem("sod_3d", mesh, [mat], fills, bcs, params)
+
+
 def with_strength(problem: Problem, kind: str = "hypo", shear_modulus: float = 1.0) -> Problem:
     """The deck with every material given a strength model: ``kind`` is "hypo" or
     "hyper" (strength_type 1 or 2) and the shipped linear hypo-elastic model

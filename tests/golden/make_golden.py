@@ -21,12 +21,13 @@ Unstructured-mesh cases (geo_*.npz) run the reference, with its own EnSight
 reader, on two more meshes it ships: mesh_z_taylorAnvil.geo (a quarter rod on an
 O-grid, nodes of valence 3 and 6) with the deck of its Taylor-anvil test
 (tests-for-Explicit-Lagrange-Kokkos/input_for_TaylorAnvil3D_test.cpp), and
-mesh_triple_30x18.geo with the triple-point deck of input.cpp.  These fixtures
+mesh_triple_30x18.geo with the triple-point deck of input.cpp, and the skewed
+Saltzman mesh (mesh_Saltzman.geo) with the SodZ values in 3D.  These fixtures
 also carry the mesh (geo_<case>_mesh.npz: coordinates and 0-based connectivity
 as read from the .geo), so the tests run without the reference tree.
 
 Run from the repository root (needs the reference tree):
-    python tests/golden/make_golden.py [boxes strength rz geo rz:<case>]   (default: all)
+    python tests/golden/make_golden.py [boxes strength rz geo rz:<case> geo:<case>]   (default: all)
 """
 import hashlib
 import json
@@ -82,6 +83,7 @@ def geo_cases():
     return {
         "taylor_anvil": ("mesh_z_taylorAnvil.geo", problems.taylor_anvil, [1, 300]),
         "triple_point": ("mesh_triple_30x18.geo", problems.triple_point, [1, 400]),
+        "sod_saltzman": ("mesh_Saltzman.geo", problems.sod_3d, [1, 400]),
     }
 
 
@@ -93,11 +95,13 @@ def geo_problem(name: str, cycles: int):
     return geo_cases()[name][1](hm, cycles=cycles)
 
 
-def make_geo(meta):
+def make_geo(meta, names=None):
     from fierro_gb300 import mesh
     from oracle import orc
-    meta["geo"] = {}
+    meta.setdefault("geo", {})
     for name, (geo, builder, cycles) in geo_cases().items():
+        if names and name not in names:
+            continue
         path = os.path.join(MESHES, geo)
         g = mesh.read_geo(path)
         fn = os.path.join(HERE, "geo_%s_mesh.npz" % name)
@@ -182,6 +186,8 @@ def main(groups=("boxes", "strength", "rz", "geo")):
     for g in groups:
         if g.startswith("rz:"):  # one 2D-RZ case by name
             make_rz(meta, names=[g[3:]])
+        elif g.startswith("geo:"):  # one shipped-mesh case by name
+            make_geo(meta, names=[g[4:]])
         else:
             makers[g](meta)
     with open(meta_path, "w") as f:

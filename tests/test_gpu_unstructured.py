@@ -1,10 +1,11 @@
 """GPU parity on unstructured meshes the reference ships (tests/golden/geo_*):
 the Taylor-anvil rod, an O-grid with nodes of valence 3 and 6 (corner lists of
 3 and 6 corners, irregular neighbour lists), under the deck of the reference's
-own Taylor-anvil test, and the triple-point box with three fills and six
-reflecting planes.  Exact mode against the restatement bit for bit (stages and
-full runs) and against the reference's outputs; FMA mode within the parity
-gates; energy conserved."""
+own Taylor-anvil test, the triple-point box with three fills and six
+reflecting planes, and the skewed Saltzman mesh under a Sod shock tube.  Exact
+mode against the restatement bit for bit (stages and full runs) and against the
+reference's outputs; FMA mode within the parity gates (one bounded exception,
+see test_fma_mode_within_gates); energy conserved."""
 import importlib.util
 import os
 
@@ -15,7 +16,7 @@ from conftest import GOLDEN, assert_bitwise, assert_fields, load_golden
 pytestmark = pytest.mark.gpu
 
 FIELDS = ("coords", "vel", "den", "pres", "sie", "sspd", "vol")
-CASES = [("taylor_anvil", 300), ("triple_point", 400)]
+CASES = [("taylor_anvil", 300), ("triple_point", 400), ("sod_saltzman", 400)]
 
 
 def _problem(name, cycles):
@@ -89,11 +90,25 @@ def test_exact_vs_reference_golden(lib_built, name, cycles):
 
 @pytest.mark.parametrize("name,cycles", CASES)
 def test_fma_mode_within_gates(lib_built, name, cycles):
+    """The gated fields within 1e-12 after one cycle and 1e-9 after the full run
+    (pointwise, floor 1e-3 of the field's peak).  One exception, measured and
+    bounded here: after one cycle of Sod on the skewed Saltzman mesh the velocity of
+    the elements at rest is rounding noise in both codes (the corner normals of a
+    node's elements cancel only up to rounding under a uniform pressure), ~2e-17
+    against a 1.7e-3 peak; the FMA mode's normals round differently, so that noise
+    differs: 1.2e-11 against the 1e-3 floor, 1.2e-14 of the peak."""
+    import numpy as np
     for c, tol in ((1, 1e-12), (cycles, 1e-9)):
         prob = _problem(name, c)
         ref = load_golden("geo_%s_c%d" % (name, c))
         g = _gpu(prob, cycles=c, mode=1)
-        assert_fields(g, ref, tol, keys=("coords", "vel", "den", "pres", "sie"), label="fma %s c%d" % (name, c))
+        if name == "sod_saltzman" and c == 1:
+            assert_fields(g, ref, tol, keys=("coords", "den", "pres", "sie"), label="fma %s c%d" % (name, c))
+            dv = np.max(np.abs(g["vel"] - ref["vel"]))
+            assert dv <= 1e-12 * np.max(np.abs(ref["vel"]))
+            assert_fields(g, ref, 2e-11, keys=("vel",), label="fma %s c%d (noise)" % (name, c))
+        else:
+            assert_fields(g, ref, tol, keys=("coords", "vel", "den", "pres", "sie"), label="fma %s c%d" % (name, c))
 
 
 @pytest.mark.parametrize("name,cycles", CASES)
