@@ -32,7 +32,6 @@
 // of two state bins.  Nothing is accumulated with atomics: every output has one
 // writer and every reduction has a fixed order.
 #include <cstdint>
-#include <cstdio>
 
 #include "sgh_device.h"
 
