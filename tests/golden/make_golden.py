@@ -22,7 +22,8 @@ reader, on two more meshes it ships: mesh_z_taylorAnvil.geo (a quarter rod on an
 O-grid, nodes of valence 3 and 6) with the deck of its Taylor-anvil test
 (tests-for-Explicit-Lagrange-Kokkos/input_for_TaylorAnvil3D_test.cpp), and
 mesh_triple_30x18.geo with the triple-point deck of input.cpp, and the skewed
-Saltzman mesh (mesh_Saltzman.geo) with the SodZ values in 3D.  These fixtures
+Saltzman mesh (mesh_Saltzman.geo) with the SodZ values in 3D, and the small
+O-grid rod mesh-TA-rod.geo with the Taylor-anvil deck.  These fixtures
 also carry the mesh (geo_<case>_mesh.npz: coordinates and 0-based connectivity
 as read from the .geo), so the tests run without the reference tree.
 
@@ -84,6 +85,7 @@ def geo_cases():
         "taylor_anvil": ("mesh_z_taylorAnvil.geo", problems.taylor_anvil, [1, 300]),
         "triple_point": ("mesh_triple_30x18.geo", problems.triple_point, [1, 400]),
         "sod_saltzman": ("mesh_Saltzman.geo", problems.sod_3d, [1, 400]),
+        "taylor_anvil_small_rod": ("mesh-TA-rod.geo", problems.taylor_anvil, [1, 200]),
     }
 
 

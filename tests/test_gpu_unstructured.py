@@ -16,7 +16,7 @@ from conftest import GOLDEN, assert_bitwise, assert_fields, load_golden
 pytestmark = pytest.mark.gpu
 
 FIELDS = ("coords", "vel", "den", "pres", "sie", "sspd", "vol")
-CASES = [("taylor_anvil", 300), ("triple_point", 400), ("sod_saltzman", 400)]
+CASES = [("taylor_anvil", 300), ("triple_point", 400), ("sod_saltzman", 400), ("taylor_anvil_small_rod", 200)]
 
 
 def _problem(name, cycles):

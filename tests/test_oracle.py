@@ -216,7 +216,8 @@ def _geo(name, cycles):
 
 @pytest.mark.parametrize("name,cycles", [("taylor_anvil", 1), ("taylor_anvil", 300),
                                          ("triple_point", 1), ("triple_point", 400),
-                                         ("sod_saltzman", 1), ("sod_saltzman", 400)])
+                                         ("sod_saltzman", 1), ("sod_saltzman", 400),
+                                         ("taylor_anvil_small_rod", 1), ("taylor_anvil_small_rod", 200)])
 def test_oracle_equals_reference_on_shipped_unstructured_meshes(oracle_built, name, cycles):
     """The restatement equals the reference bit for bit on two more meshes the
     reference ships: the Taylor-anvil rod (an O-grid with nodes of valence 3 and
