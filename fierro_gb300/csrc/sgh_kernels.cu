@@ -276,12 +276,27 @@ __global__ void __launch_bounds__(kNodeBlock) k_node(const NodeArgs a) {
   const size_t ne = (size_t)a.ne;
   double f0 = 0.0, f1 = 0.0, f2 = 0.0;
   const int c0 = a.cin_start[n], c1 = a.cin_start[n + 1];
-  for (int c = c0; c < c1; ++c) {
-    const int cid = __ldg(a.cin + c);
-    const int e = cid >> 3, l = cid & 7;
-    f0 = f0 + __ldg(a.force + (size_t)(l * 3 + 0) * ne + e);
-    f1 = f1 + __ldg(a.force + (size_t)(l * 3 + 1) * ne + e);
-    f2 = f2 + __ldg(a.force + (size_t)(l * 3 + 2) * ne + e);
+  // corners four at a time: the corner ids, then the twelve force loads, are
+  // issued before the sums, which keep the corner order
+  for (int base = c0; base < c1; base += 4) {
+    const int cnt = min(4, c1 - base);
+    int cid[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) cid[k] = k < cnt ? __ldg(a.cin + base + k) : 0;
+    double g[4][3];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int e = cid[k] >> 3, l = cid[k] & 7;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) g[k][d] = k < cnt ? __ldg(a.force + (size_t)(l * 3 + d) * ne + e) : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (k < cnt) {
+        f0 = f0 + g[k][0];
+        f1 = f1 + g[k][1];
+        f2 = f2 + g[k][2];
+      }
   }
   const double adt = a.rk_alpha * ctrl->dt;
   const double m = a.node_mass[n];
