@@ -59,6 +59,15 @@ def parse(argv=None):
     ap.add_argument("--cpu-n", type=int, default=120, help="edge of the CPU baseline sample mesh")
     ap.add_argument("--cpu-cycles", type=int, default=6, help="timed cycles of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cpu-1thread", action="store_true",
+                    help="skip the reference's one-thread figure on the CPU sample")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the parity leg (the GPU in both modes against the reference's own solver on the "
+                         "CPU sample's deck, after one cycle and after K)")
+    ap.add_argument("--no-batch-leg", action="store_true",
+                    help="skip the batched-ensemble object of the default line")
+    ap.add_argument("--no-adjoint-leg", action="store_true",
+                    help="skip the discrete-adjoint object of the default line")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--batch", action="store_true",
                     help="run the batched-ensemble benchmark instead (instances/s vs looping the plain solver)")
@@ -202,14 +211,13 @@ def alg_bytes(kind: str, nn: int, ne: int, nnz: int) -> float:
     return 0.0
 
 
-# Per-element figures of the kernels from ncu.  FP64 thread instructions per
-# element of one launch: the 64^3 captures summarised in
-# profiles/sgh_kernels_sedov64_ncu_full.md (exact mode) and
-# profiles/sgh_kernels_sedov64_fma_ncu.md (FMA mode).  DRAM bytes
-# (dram__bytes_read + dram__bytes_write) per element of one launch: the
-# one-pass capture of the 256^3 bench workload itself
-# (profiles/sgh_dram_sedov256.md; the memory traffic is the same in both
-# modes).  k_elem is the mean of its first-stage and last-stage (CFL) launches.
+# Per-element figures of the kernels from ncu captures of the jittered Sedov
+# 64^3 case (one kernel, three launches, --clock-control none).  FP64 thread
+# instructions per element of one launch, exact and FMA modes.  DRAM bytes
+# (dram__bytes_read + dram__bytes_write) per element of one launch, scaled from
+# 64^3 to 256^3 by the element count (the kernels stream their arrays once, so
+# the traffic grows with the elements); the memory traffic is the same in both
+# modes.  k_elem is the mean of its first-stage and last-stage (CFL) launches.
 DRAM_PER_ELEM_256 = {"k_force": 10053043883 / 16777216, "k_elem": 9796794624 / 16777216}
 NCU_PER_ELEM = {"exact": {
     "k_force": {"fp64_ops": 138412032 / 262144, "dram_bytes": DRAM_PER_ELEM_256["k_force"]},
@@ -231,11 +239,33 @@ def measure_peaks():
 
 
 # ------------------------------------------------------------------ CPU reference
-def run_reference_sample(args, n: int, cycles: int, warmup: int, strength: str | None = None) -> dict:
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else platform)."""
+    try:
+        p = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, timeout=10)
+        for line in p.stdout.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def run_reference_sample(args, n: int, cycles: int, warmup: int, strength: str | None = None,
+                         threads: int | None = None) -> dict:
     """The reference's own SGH solver (compiled from its sources against the
-    MATAR/Kokkos stand-in, OpenMP on every host core) on a bounded sample of the
-    workload: the same jittered, permuted Sedov problem on an n^3 mesh (with the
-    test strength model on every material when `strength` is given)."""
+    MATAR/Kokkos stand-in, OpenMP on every host core unless `threads` is given)
+    on a bounded sample of the workload: the same jittered, permuted Sedov
+    problem on an n^3 mesh (with the test strength model on every material when
+    `strength` is given)."""
     from oracle import build_ref, orc
     if not orc.reference_available("fierro_ref_fast"):
         build_ref.build_reference()
@@ -245,7 +275,7 @@ def run_reference_sample(args, n: int, cycles: int, warmup: int, strength: str |
     if strength:
         from fierro_gb300 import problems
         problems.with_strength(prob, strength, args.shear_modulus)
-    cores = os.cpu_count() or 1
+    cores = threads or os.cpu_count() or 1
     st = orc.run_reference(prob, cycles=cycles, kind="fierro_ref_fast", threads=cores, warmup=warmup)
     secs = st["calc_seconds"]
     return {"value": prob.mesh.num_elems * cycles / secs, "unit": UNIT, "cores": cores, "kind": "reference",
@@ -253,7 +283,92 @@ def run_reference_sample(args, n: int, cycles: int, warmup: int, strength: str |
                       "cycle-loop timer after %d warm-up cycles, OMP_NUM_THREADS=%d" %
                       (n, "Noh" if prob.name.startswith("noh") else "Sedov",
                        prob.mesh.num_elems, cycles, warmup, cores),
-            "seconds": secs}
+            "seconds": secs, "cpu_model": cpu_model()}
+
+
+# ------------------------------------------------------------------ parity
+PARITY_FIELDS = ("coords", "vel", "den", "pres", "sie")
+POSITIVE_FIELDS = ("den", "pres", "sie")
+
+
+def parity_error(got, ref, floor: float = 1e-3) -> float:
+    """max |got - ref| / max(|ref|, floor * max|ref|): pointwise relative error,
+    values below `floor` of the field's peak compared at that scale."""
+    import numpy as np
+    got = np.asarray(got, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    scale = float(np.max(np.abs(ref))) if ref.size else 0.0
+    if scale == 0.0:
+        return float(np.max(np.abs(got))) if got.size else 0.0
+    return float(np.max(np.abs(got - ref) / np.maximum(np.abs(ref), floor * scale)))
+
+
+def parity_error_tight(got, ref, key: str) -> float:
+    """The tight metric: purely relative for the positive fields (density,
+    pressure, energy: a 1e-10 background value is compared at its own scale),
+    floor 1e-9 of the peak for positions and velocities."""
+    import numpy as np
+    if key in POSITIVE_FIELDS:
+        got = np.asarray(got, dtype=np.float64)
+        ref = np.asarray(ref, dtype=np.float64)
+        return float(np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)))
+    return parity_error(got, ref, 1e-9)
+
+
+def parity_leg(args, stream) -> dict:
+    """The GPU's state, in both arithmetic modes, against the reference's own
+    solver (its sources compiled with -ffp-contract=off, the uncontracted
+    arithmetic the reference specifies, OpenMP on every host core) on the same
+    jittered, permuted deck at the CPU sample's size, after one RK2 cycle and
+    after the bench's K cycles: the largest pointwise error of positions,
+    velocities, density, pressure and energy in both metrics, and how many values
+    differ at all.  The gates are 1e-12 after one cycle and 1e-9 after K."""
+    import numpy as np
+    from fierro_gb300 import sgh
+    from oracle import build_ref, orc
+    if not orc.reference_available("fierro_ref"):
+        build_ref.build_reference()
+    if not orc.reference_available("fierro_ref"):
+        raise RuntimeError("reference executable unavailable (no reference sources on this machine)")
+    n, K = args.cpu_n, max(2, args.steps)
+    prob = workload(n, args.seed, args.problem)
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    refs = {c: orc.run_reference(prob, cycles=c, kind="fierro_ref", threads=cores) for c in (1, K)}
+    t_ref = time.perf_counter() - t0
+    st = sgh.setup(prob)
+    out = {"deck": "%d^3 jittered permuted %s, seed %d (the workload's family at the CPU sample's size)"
+                   % (n, "Noh" if args.problem == "noh" else "Sedov", args.seed),
+           "reference": "the reference's own SGH solver, sources compiled unmodified with -ffp-contract=off "
+                        "(oracle/_ref/fierro_ref)",
+           "cycles": [1, K], "gates": {"1": 1e-12, str(K): 1e-9},
+           "metrics": {"max_err": "max |gpu - ref| / max(|ref|, 1e-3 max|ref|)",
+                       "max_err_tight": "density, pressure, energy: max |gpu - ref| / |ref|; positions, "
+                                        "velocities: floor 1e-9 max|ref|"},
+           "reference_seconds": t_ref}
+    ok = True
+    for mode_name, mode in (("exact", sgh.FP_EXACT), ("fma", sgh.FP_FMA)):
+        res = {}
+        with sgh.SGHSolver(prob, fp_mode=mode, stream=stream.cuda_stream) as s:
+            s.set_state(st)
+            done = 0
+            for c in (1, K):
+                s.run(c - done)
+                done = c
+                g = sgh.compared_fields(s.get_state())
+                r = refs[c]
+                gate = 1e-12 if c == 1 else 1e-9
+                e = {k: parity_error(g[k], r[k]) for k in PARITY_FIELDS}
+                et = {k: parity_error_tight(g[k], r[k], k) for k in PARITY_FIELDS}
+                res["%d_cycles" % c] = {
+                    "max_err": e, "max_err_tight": et,
+                    "values_differing": {k: int(np.sum(np.asarray(g[k]) != np.asarray(r[k]))) for k in PARITY_FIELDS},
+                    "time_rel_err": abs(s.time()[0] - r["time"]) / abs(r["time"]),
+                    "within_gate": bool(max(e.values()) <= gate and max(et.values()) <= gate)}
+                ok = ok and res["%d_cycles" % c]["within_gate"]
+        out[mode_name] = res
+    out["all_within_gates"] = ok
+    return out
 
 
 def reference_arm(args):
@@ -378,6 +493,20 @@ def ours(args):
         except Exception as exc:
             cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "reference",
                    "sample": "unavailable: " + str(exc).splitlines()[0]}
+        if cpu.get("value") and not args.no_cpu_1thread:
+            # the same sample on one host thread (two timed cycles after one warm-up)
+            try:
+                one = run_reference_sample(args, args.cpu_n, 2, 1, threads=1)
+                cpu["one_thread"] = {"value": one["value"], "unit": UNIT, "cores": 1, "sample": one["sample"]}
+            except Exception as exc:
+                cpu["one_thread"] = {"value": None, "sample": "unavailable: " + str(exc).splitlines()[0]}
+
+    parity = None
+    if rank == 0 and world == 1 and not args.no_parity:
+        try:
+            parity = parity_leg(args, stream)
+        except Exception as exc:
+            parity = {"unavailable": str(exc).splitlines()[0]}
 
     if rank != 0:
         return
@@ -403,7 +532,9 @@ def ours(args):
                 "ops_per_elem": ncu[dom]["fp64_ops"]},
         },
         "kernels": {nm: {"launches": launches[nm], "ms": per[nm], "share": share[nm]} for nm in sorted(per)},
-        "cpu_baseline": None if cpu is None else {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "cpu_baseline": None if cpu is None else {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample",
+                                                                     "cpu_model", "one_thread") if k in cpu},
+        "parity": parity,
         "clocks": ck,
         "setup_seconds": t_setup,
         "device_bytes": solver.device_bytes,
@@ -423,6 +554,19 @@ def ours(args):
         line["exact_mode"] = {"value": ne * ran_x / (total_x * 1e-3), "ms_per_step": total_x / max(ran_x, 1),
                               "kernels_ms_per_launch": {nm: per_x[nm] / (names_x.count(nm) * max(ran_x, 1))
                                                         for nm in per_x}}
+    # the other two measured forms of the path, in the same run: the batched
+    # ensemble (512 instances against looping the plain solver) and the discrete
+    # adjoint (cost against the plain forward, gradient against differences)
+    if world == 1 and not args.no_batch_leg:
+        try:
+            line["batch"] = batch_measure(args, modes=("fma", "exact"))
+        except Exception as exc:
+            line["batch"] = {"unavailable": str(exc).splitlines()[0]}
+    if world == 1 and not args.no_adjoint_leg:
+        try:
+            line["adjoint"] = adjoint_measure(args, compact=True)
+        except Exception as exc:
+            line["adjoint"] = {"unavailable": str(exc).splitlines()[0]}
     print(json.dumps(line))
 
 
@@ -458,52 +602,76 @@ def batch_workload(n_inst: int, seed: int, cycles: int):
     return out
 
 
-def batch_bench(args):
+def batch_measure(args, modes=None) -> dict:
+    """Config 4: the ensemble through fierro_batch_run against looping the plain
+    solver over the same instances, in each arithmetic mode of `modes`, with the
+    clocks sampled over the timed runs."""
     import torch
     from fierro_gb300 import sgh
     torch.cuda.set_device(0)
+    modes = modes or (args.fp_mode,)
     probs = batch_workload(args.instances, args.seed, args.batch_cycles)
     states = [sgh.setup(p) for p in probs]
     ne_tot = sum(p.mesh.num_elems for p in probs)
-    mode = sgh.FP_EXACT if args.fp_mode == "exact" else sgh.FP_FMA
-    with sgh.Batch(probs[:2], fp_mode=mode) as w:  # load the batch kernels
-        w.set_state(0, states[0])
-        w.set_state(1, states[1])
-        w.run(3)
-    stream = torch.cuda.Stream()
-    b = sgh.Batch(probs, fp_mode=mode, stream=stream.cuda_stream)
-    for i, st in enumerate(states):
-        b.set_state(i, st)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    b.run(args.batch_cycles)
-    t_batch = time.perf_counter() - t0
-    cycles_done = [b.time(i)[2] for i in range(len(probs))]
-    b.close()
-    # the same instances one after another through the single-problem solver
-    t_loop = 0.0
-    for p, st in zip(probs, states):
-        with sgh.SGHSolver(p, fp_mode=mode) as s:
-            s.set_state(st)
-            torch.cuda.synchronize()
-            t1 = time.perf_counter()
-            s.run(args.batch_cycles)
-            t_loop += time.perf_counter() - t1
     n = len(probs)
-    line = {"metric": "batched SGH ensemble instances/s (%d Sedov/Noh instances, n~U{8..48}, %d cycles each)"
-                      % (n, args.batch_cycles),
-            "value": n / t_batch, "unit": "instances/s", "higher_is_better": True, "dtype": "f64",
-            "data": "synthetic", "loop_value": n / t_loop, "speedup_vs_loop": t_loop / t_batch,
-            "batch_seconds": t_batch, "loop_seconds": t_loop, "elements_total": ne_tot,
-            "element_cycles_per_s": sum(p.mesh.num_elems * c for p, c in zip(probs, cycles_done)) / t_batch,
-            "instances_stopped_early": int(sum(c < args.batch_cycles for c in cycles_done)),
-            "config": {"workload": "ensemble", "instances": n, "cycles": args.batch_cycles, "seed": args.seed,
-                       "fp_mode": args.fp_mode, "launches_per_cycle": 8, "timing": "host wall clock around fierro_batch_run / "
-                       "fierro_sgh_run (each synchronises)"}}
+    out = {"metric": "batched SGH ensemble instances/s (%d Sedov/Noh instances, n~U{8..48}, %d cycles each)"
+                     % (n, args.batch_cycles), "unit": "instances/s", "elements_total": ne_tot,
+           "config": {"workload": "ensemble", "instances": n, "cycles": args.batch_cycles, "seed": args.seed,
+                      "launches_per_cycle": 8, "timing": "host wall clock around fierro_batch_run / "
+                      "fierro_sgh_run (each synchronises)"}}
+    clocks = ClockSampler(0)
+    clocks.start()
+    for mname in modes:
+        mode = sgh.FP_EXACT if mname == "exact" else sgh.FP_FMA
+        with sgh.Batch(probs[:2], fp_mode=mode) as w:  # load the batch kernels
+            w.set_state(0, states[0])
+            w.set_state(1, states[1])
+            w.run(3)
+        stream = torch.cuda.Stream()
+        b = sgh.Batch(probs, fp_mode=mode, stream=stream.cuda_stream)
+        for i, st in enumerate(states):
+            b.set_state(i, st)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.run(args.batch_cycles)
+        t_batch = time.perf_counter() - t0
+        cycles_done = [b.time(i)[2] for i in range(n)]
+        b.close()
+        # the same instances one after another through the single-problem solver
+        t_loop = 0.0
+        for p, st in zip(probs, states):
+            with sgh.SGHSolver(p, fp_mode=mode) as s1:
+                s1.set_state(st)
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                s1.run(args.batch_cycles)
+                t_loop += time.perf_counter() - t1
+        out[mname] = {"value": n / t_batch, "loop_value": n / t_loop, "speedup_vs_loop": t_loop / t_batch,
+                      "batch_seconds": t_batch, "loop_seconds": t_loop,
+                      "element_cycles_per_s": sum(p.mesh.num_elems * c for p, c in zip(probs, cycles_done)) / t_batch,
+                      "instances_stopped_early": int(sum(c < args.batch_cycles for c in cycles_done))}
+    out["clocks"] = clocks.stop()
+    return out
+
+
+def batch_bench(args):
+    m = batch_measure(args)
+    r = m[args.fp_mode]
+    line = {"metric": m["metric"], "value": r["value"], "unit": "instances/s", "higher_is_better": True,
+            "dtype": "f64", "data": "synthetic", "loop_value": r["loop_value"],
+            "speedup_vs_loop": r["speedup_vs_loop"], "batch_seconds": r["batch_seconds"],
+            "loop_seconds": r["loop_seconds"], "elements_total": m["elements_total"],
+            "element_cycles_per_s": r["element_cycles_per_s"],
+            "instances_stopped_early": r["instances_stopped_early"],
+            "config": dict(m["config"], fp_mode=args.fp_mode), "clocks": m["clocks"]}
     print(json.dumps(line))
 
 
 def adjoint_bench(args):
+    print(json.dumps(adjoint_measure(args)))
+
+
+def adjoint_measure(args, compact: bool = False) -> dict:
     """Discrete adjoint of 400 RK2 cycles of jittered Sedov 64^3: cost of the
     checkpointed forward and of the backward against the plain forward, and the
     gradient against central differences of the GPU forward along seeded
@@ -524,6 +692,8 @@ def adjoint_bench(args):
     vstats = s.adj_stats()
     s.adj_verify(False)
     t_plain, t_fwd, t_bwd = [], [], []
+    clocks = ClockSampler(0)
+    clocks.start()
     for _ in range(max(args.steps, 1) if args.steps < 5 else 3):
         s.set_state(dm.state0)
         s.synchronize()
@@ -538,8 +708,28 @@ def adjoint_bench(args):
         sb2, gb2, _ = s.adj_backward(den=seed)
         t_bwd.append(time.perf_counter() - t0)
     tp, tf, tb = min(t_plain), min(t_fwd), min(t_bwd)
-    dirs = []
+    # the frozen-branch check: central differences (step 1e-6) of the forward
+    # with the base run's switch decisions held, along the seeded directions
+    Jf, sbf, gbf, _ = dm.gradient_frozen()
+    frozen = []
     for d_sie, d_g in dm.directions(args.adj_dirs, seed=args.seed):
+        ad = float(np.dot(sbf, d_sie) + np.sum(gbf) * d_g)
+        fd = dm.fd(d_sie, d_g, h=1e-6)
+        frozen.append({"ad": ad, "fd": fd, "rel": abs(fd - ad) / abs(fd)})
+    dm.unfreeze()
+    relf = np.array([d["rel"] for d in frozen]) if frozen else np.zeros(0)
+    fd_frozen = {"directions": len(frozen), "step": 1e-6,
+                 "max_rel": float(relf.max()) if relf.size else None,
+                 "median_rel": float(np.median(relf)) if relf.size else None,
+                 "within_1e-6": int((relf <= 1e-6).sum()),
+                 "gradient_equals_plain": bool(np.array_equal(sbf, sb) and np.array_equal(gbf, gb)),
+                 "what": "central differences of the frozen-branch forward (fierro_adj_branches FREEZE: the "
+                         "limiter neighbour and clamps, Mach switch, compression sign, Riemann-velocity guard, "
+                         "CFL element and node pair, dt growth cap and clamps held at the base run's decisions)"}
+    if not compact:
+        fd_frozen["per_direction"] = frozen
+    dirs = []
+    for d_sie, d_g in ([] if compact else dm.directions(args.adj_dirs, seed=args.seed)):
         ad = float(np.dot(sb, d_sie) + np.sum(gb) * d_g)
         fd6 = dm.fd(d_sie, d_g, h=1e-6)
         est, h, spread, _ = dm.fd_consistent(d_sie, d_g)
@@ -563,7 +753,8 @@ def adjoint_bench(args):
         J12, sb12, gb12, _ = dm12.gradient()
         orc_rel = []
         try:
-            f = dm12.oracle_forward()
+            from oracle import orc
+            f = orc.density_mismatch_forward(dm12)
             for d_sie, d_g in dm12.directions(3, seed=args.seed):
                 ad = float(np.dot(sb12, d_sie) + np.sum(gb12) * d_g)
                 fd = dm12.fd(d_sie, d_g, h=1e-6, forward=f)
@@ -579,6 +770,7 @@ def adjoint_bench(args):
                           "other": vstats["dt_other_cycles"]},
             "adjoint_device_bytes": vstats["device_bytes"], "tape_bytes": vstats["tape_bytes"],
             "checkpoint_bytes": vstats["ckpt_bytes"],
+            "fd_frozen": fd_frozen,
             "fd_check": fd_check,
             "oracle_fd_check_12cubed_100cycles": orc_rel,
             "config": {"workload": "adjoint sedov%d jitter0.1 seed7" % n, "cycles": cyc, "ckpt_every": k,
@@ -587,7 +779,8 @@ def adjoint_bench(args):
                        "the reported step is the one agreeing best with the next smaller step",
                        "timing": "host wall clock around fierro_sgh_run / fierro_adj_forward / "
                        "fierro_adj_backward (each synchronises), best of 3"}}
-    print(json.dumps(line))
+    line["clocks"] = clocks.stop()
+    return line
 
 
 def outputs_bench(args):
@@ -638,9 +831,9 @@ def outputs_bench(args):
     print(json.dumps(line))
 
 
-# The same per-element counters for the strength instantiations, from the capture
-# summarised in profiles/strength_kernels_sedov64_ncu_full.md (64^3, exact mode,
-# mean of the two RK-stage launches): hypo k_force<0,0,1>, hyper k_elem<*,0,1>.
+# The same per-element counters for the strength instantiations, from an ncu
+# capture of the 64^3 case (exact mode, mean of the two RK-stage launches): hypo
+# k_force<0,0,1>, hyper k_elem<*,0,1>.
 NCU_PER_ELEM_STRENGTH = {
     ("hypo", "k_force"): {"fp64_ops": (233308160 + 214695936) / 2 / 262144,
                           "dram_bytes": (125.731072e6 + 36.583424e6 + 145.0176e6 + 37.52832e6) / 2 / 262144},

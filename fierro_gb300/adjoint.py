@@ -5,7 +5,9 @@
   element), outputs the final element density, pressure and sie.
 * ``DensityMismatch`` -- J = sum_e M_e (rho_e - rho_target_e)^2 at the final
   state, its gradient through the adjoint, and central finite differences of
-  the same forward along seeded directions (the gradient check).
+  the same forward along seeded directions (the gradient check), optionally of
+  the frozen-branch forward (the forward's switches held at the base run's
+  decisions, so the differences do not straddle them).
 
 The parameters enter the way fierro_adj_forward defines them: the initial
 state's sie is replaced and pressure / sound speed are recomputed from it with
@@ -113,6 +115,21 @@ class DensityMismatch:
         sb, gb, vb = self.solver.adj_backward(den=seed)
         return J, sb, gb, vb
 
+    def gradient_frozen(self, sie0=None, gamma=None):
+        """gradient() with the forward's branch decisions recorded, after which
+        every forward() of this object runs with them frozen (the frozen-branch
+        forward, fierro_adj_branches): central differences of that forward are
+        the derivative the adjoint computes, not a secant across a switch."""
+        s = self.solver
+        s.adj_branches(sgh.ADJ_BRANCHES_RECORD)
+        out = self.gradient(sie0, gamma)
+        s.adj_branches(sgh.ADJ_BRANCHES_FREEZE)
+        return out
+
+    def unfreeze(self):
+        """Plain forwards again (frees the branch record)."""
+        self.solver.adj_branches(sgh.ADJ_BRANCHES_OFF)
+
     def directions(self, n: int, seed: int = 2024):
         """Seeded directions: sie0 scaled per element by U(-1,1) (relative to its
         value, so the 1e-10 background and the blast element move alike) and a
@@ -145,24 +162,6 @@ class DensityMismatch:
             if best is None or spread < best[2]:
                 best = (a, steps[i], spread)
         return best[0], best[1], best[2], list(zip(steps, vals))
-
-    def oracle_forward(self, variant: str = "libm"):
-        """J through the CPU oracle (the reference's algorithm, C restatement):
-        a callable (sie0, gamma) -> J for fd(..., forward=...)."""
-        from oracle import orc
-
-        def f(sie0, gamma):
-            o = orc.Oracle(self.problem, variant=variant)
-            st = eos_state(self.state0, np.asarray(sie0, dtype=np.float64),
-                           np.broadcast_to(np.asarray(gamma, dtype=np.float64), self.sie0.shape).copy())
-            o.set(orc.ORC_ELEM_SIE, st["elem_sie"])
-            o.set(orc.ORC_ELEM_PRES, st["elem_pres"])
-            o.set(orc.ORC_ELEM_SSPD, st["elem_sspd"])
-            o.set(orc.ORC_ELEM_STATEV, st["elem_statev"])
-            o.run_cycles(self.cycles)
-            return self.value(o.get(orc.ORC_ELEM_DEN))
-
-        return f
 
 
 def sedov_target(n: int, cycles: int, jitter: float = 0.1, seed: int = 7, energy: float = 0.3, **kw):

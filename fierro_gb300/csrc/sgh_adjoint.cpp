@@ -63,6 +63,32 @@ void adj_release(fierro_sgh* h) {
   h->adj = nullptr;
 }
 
+// The branch decisions of one forward run (the base trajectory), cycle by cycle:
+// per RK stage and element the corner force's branch bits and limiter neighbour,
+// per cycle the time step's inputs, its CFL element and node pair.  A forward
+// run in freeze mode takes every decision from here instead of deciding it.
+struct AdjBranches {
+  int mode = FIERRO_ADJ_BRANCHES_OFF;
+  long long cycles = 0;      // cycles of the recorded run (0: nothing recorded yet)
+  long long cap = 0;         // cycles the buffers hold
+  int S = 0;
+  int64_t ne = 0;
+  unsigned char* flags = nullptr;  // [cap][S][ne]
+  int* sel = nullptr;              // [cap][S][ne]
+  AdjRecord* rec = nullptr;        // [cap]
+  size_t bytes = 0;
+};
+
+void adj_branches_release(fierro_sgh* h) {
+  if (!h || !h->adj_br) return;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  cudaFree(h->adj_br->flags);
+  cudaFree(h->adj_br->sel);
+  cudaFree(h->adj_br->rec);
+  delete h->adj_br;
+  h->adj_br = nullptr;
+}
+
 }  // namespace fierro
 
 namespace {
@@ -330,6 +356,111 @@ int replay_segment(fierro_sgh* h, AdjState* a, int g, int n) {
   return FIERRO_OK;
 }
 
+AdjMesh mesh_of(const fierro_sgh* h) {
+  AdjMesh m{};
+  m.ne = (int)h->ne;
+  m.nn = (int)h->nn;
+  m.nie = h->d_nie;
+  m.eie_start = h->d_eie_start;
+  m.eie = h->d_eie;
+  m.cin_start = h->d_cin_start;
+  m.cin = h->d_cin;
+  m.mat = h->d_mat;
+  m.qtab = h->d_qtab;
+  m.bc = h->d_bc;
+  m.elem_mass = h->d_elem_mass;
+  m.node_mass = h->d_node_mass;
+  m.gamma = h->d_gamma;
+  m.csmin = h->d_csmin;
+  return m;
+}
+
+// The handle's state bin c as a tape slot (the fields the dt kernels read).
+Slot bin_slot(const fierro_sgh* h, int c) {
+  Slot s{};
+  s.x = h->d_x[c][0];
+  s.y = h->d_x[c][1];
+  s.z = h->d_x[c][2];
+  s.u = h->d_v[c][0];
+  s.v = h->d_v[c][1];
+  s.w = h->d_v[c][2];
+  s.sie = h->d_sie[c];
+  s.vol = h->d_vol;
+  s.den = h->d_den;
+  s.pres = h->d_pres;
+  s.sspd = h->d_sspd;
+  s.bmat = h->d_bmat;
+  return s;
+}
+
+// Sizes the branch record for `cycles` cycles of this handle.
+int branches_reserve(fierro_sgh* h, AdjBranches* br, long long cycles) {
+  const int S = h->rk_num_stages;
+  if (br->cap >= cycles && br->S == S && br->ne == h->ne) return FIERRO_OK;
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  cudaFree(br->flags);
+  cudaFree(br->sel);
+  cudaFree(br->rec);
+  br->flags = nullptr;
+  br->sel = nullptr;
+  br->rec = nullptr;
+  br->cap = br->cycles = 0;
+  br->bytes = 0;
+  const size_t n = (size_t)cycles * (size_t)S * (size_t)h->ne;
+  cudaError_t e1 = cudaMalloc(&br->flags, std::max<size_t>(n, 1));
+  cudaError_t e2 = e1 == cudaSuccess ? cudaMalloc(&br->sel, std::max<size_t>(n, 1) * sizeof(int)) : e1;
+  cudaError_t e3 = e2 == cudaSuccess ? cudaMalloc(&br->rec, (size_t)cycles * sizeof(AdjRecord)) : e2;
+  if (e3 != cudaSuccess) {
+    cudaFree(br->flags);
+    cudaFree(br->sel);
+    br->flags = nullptr;
+    br->sel = nullptr;
+    br->rec = nullptr;
+    return set_error(FIERRO_ENOMEM, "adjoint branch record for %lld cycles: %s", cycles, cudaGetErrorString(e3));
+  }
+  br->cap = cycles;
+  br->S = S;
+  br->ne = h->ne;
+  br->bytes = n * (1 + sizeof(int)) + (size_t)cycles * sizeof(AdjRecord);
+  return FIERRO_OK;
+}
+
+// One cycle of the handle's own schedule (the launches of its cycle graph) with
+// the force passes recording (mode 1) or replaying (mode 2) cycle i of the
+// branch record, and the time step recorded with its CFL element and node pair
+// (mode 1) or taken along the recorded branch (mode 2).
+void branch_cycle(fierro_sgh* h, AdjBranches* br, long long i, int mode) {
+  const int c = (int)((h->base + h->enq_cycles) & 1);
+  const int S = h->rk_num_stages;
+  const size_t ne = (size_t)h->ne;
+  const AdjLaunch& K = adjoint_kernels();
+  const AdjMesh m = mesh_of(h);
+  const Slot sc = bin_slot(h, c);
+  AdjRecord* r = br->rec + i;
+  if (mode == FIERRO_ADJ_BRANCHES_RECORD) {
+    K.pre(r, h->d_cfl, h->ncfl, h->d_ctrl, h->stream);
+    DtArgs d{};
+    d.cfl_part = h->d_cfl;
+    d.nparts = h->ncfl;
+    d.ctrl = h->d_ctrl;
+    d.lp = h->lp;
+    h->ks->dt(d, h->stream);
+    K.argmin(r, h->d_ctrl, h->lp, m, sc, h->stream);
+    K.pair(r, m, sc, h->stream);
+  } else {
+    K.dt_frozen(r, h->d_ctrl, h->lp, m, sc, h->stream);
+  }
+  for (int s = 0; s < S; ++s) {
+    ForceArgs fa = stage_force_args(h, c, s);
+    fa.br_flags = br->flags + ((size_t)i * S + s) * ne;
+    fa.br_sel = br->sel + ((size_t)i * S + s) * ne;
+    h->ks->force_branch(fa, mode, h->stream);
+    h->ks->node(node_args(h, c, stage_alpha(h, s)), h->stream);
+    h->ks->elem(stage_elem_args(h, c, s), s == S - 1 ? 1 : 0, h->stream);
+  }
+  h->ks->end(h->d_ctrl, h->lp, h->stream);
+}
+
 int upload_seed(fierro_sgh* h, double* dst, const double* src, const std::vector<int64_t>& map, size_t stride,
                 size_t off, int* slot) {
   return upload_gather(h, dst, src, map, stride, off, slot);
@@ -355,8 +486,19 @@ extern "C" int fierro_adj_forward(fierro_sgh* h, const double* sie0, const doubl
   const long long nseg = (cycles + k - 1) / k;
   if (nseg > (1 << 24)) return set_error(FIERRO_EINVAL, "adj_forward: too many checkpoints");
   if (h->adj) h->adj->have_forward = false;
-  TRY(ensure(h, k, (int)nseg));
-  AdjState* a = h->adj;
+  AdjBranches* br = h->adj_br;
+  const int bmode = br ? br->mode : FIERRO_ADJ_BRANCHES_OFF;
+  if (bmode == FIERRO_ADJ_BRANCHES_FREEZE && (br->cycles != cycles || br->S != h->rk_num_stages || br->ne != h->ne))
+    return set_error(FIERRO_EINVAL, "adj_forward: frozen branches were recorded for %lld cycles, %lld asked",
+                     br->cycles, (long long)cycles);
+  if (bmode == FIERRO_ADJ_BRANCHES_RECORD) TRY(branches_reserve(h, br, cycles));
+  // the frozen-branch forward is a plain forward run: no checkpoints, and no
+  // backward pass follows it
+  AdjState* a = nullptr;
+  if (bmode != FIERRO_ADJ_BRANCHES_FREEZE) {
+    TRY(ensure(h, k, (int)nseg));
+    a = h->adj;
+  }
   long long cyc0 = 0;
   TRY(cycles_done(h, &cyc0));
   h->enq_cycles = cyc0;
@@ -369,23 +511,50 @@ extern "C" int fierro_adj_forward(fierro_sgh* h, const double* sie0, const doubl
   // and CFL minima of the resulting state
   adjoint_kernels().eos((int)h->ne, h->d_sie[c], h->d_den, h->d_gamma, h->d_csmin, h->d_pres, h->d_sspd, h->stream);
   h->ks->elem(elem_args(h, c, c, 1.0, div_parity(h, c, 0)), 2, h->stream);
+  long long done = 0;
   for (long long g = 0; g < nseg; ++g) {
-    TRY(save_checkpoint(h, a, (int)g, (int)((h->base + h->enq_cycles) & 1)));
+    if (a) TRY(save_checkpoint(h, a, (int)g, (int)((h->base + h->enq_cycles) & 1)));
     const long long n = std::min<long long>(k, cycles - g * k);
-    for (long long i = 0; i < n; ++i) {
-      CUDA_TRY(cudaGraphLaunch(h->graph[(h->base + h->enq_cycles) & 1], h->stream));
+    for (long long i = 0; i < n; ++i, ++done) {
+      if (bmode == FIERRO_ADJ_BRANCHES_OFF) CUDA_TRY(cudaGraphLaunch(h->graph[(h->base + h->enq_cycles) & 1], h->stream));
+      else branch_cycle(h, br, done, bmode);
       h->enq_cycles++;
     }
   }
+  CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   long long cyc1 = 0;
   TRY(cycles_done(h, &cyc1));
   h->enq_cycles = cyc1;
-  a->cyc0 = cyc0;
-  a->cycles = cyc1 - cyc0;
-  a->have_forward = a->cycles > 0;
-  if (cycles_run) *cycles_run = a->cycles;
+  if (bmode == FIERRO_ADJ_BRANCHES_RECORD) br->cycles = cyc1 - cyc0 == cycles ? cycles : 0;
+  if (cycles_run) *cycles_run = cyc1 - cyc0;
+  if (a) {
+    a->cyc0 = cyc0;
+    a->cycles = cyc1 - cyc0;
+    a->have_forward = a->cycles > 0;
+  }
   return check_status(h);
+}
+
+extern "C" int fierro_adj_branches(fierro_sgh* h, int mode) {
+  clear_error();
+  if (!h) return set_error(FIERRO_EINVAL, "handle is NULL");
+  if (mode == FIERRO_ADJ_BRANCHES_OFF) {
+    adj_branches_release(h);
+    return FIERRO_OK;
+  }
+  if (mode != FIERRO_ADJ_BRANCHES_RECORD && mode != FIERRO_ADJ_BRANCHES_FREEZE)
+    return set_error(FIERRO_EINVAL, "adj_branches: mode %d is not OFF, RECORD or FREEZE", mode);
+  if (h->fp_mode != FIERRO_FP_EXACT || h->strength || h->dims == 2)
+    return set_error(FIERRO_ENOTSUP, "adj_branches: exact-mode gas-only hex handles only, as the adjoint");
+  if (mode == FIERRO_ADJ_BRANCHES_FREEZE && (!h->adj_br || h->adj_br->cycles == 0))
+    return set_error(FIERRO_EINVAL, "adj_branches: no recorded forward to freeze");
+  if (!h->adj_br) {
+    h->adj_br = new (std::nothrow) AdjBranches();
+    if (!h->adj_br) return set_error(FIERRO_ENOMEM, "adj_branches: host allocation failed");
+  }
+  h->adj_br->mode = mode;
+  return FIERRO_OK;
 }
 
 extern "C" int fierro_adj_backward(fierro_sgh* h, const fierro_adj_seed* seed, double* sie0_bar, double* gamma_bar,

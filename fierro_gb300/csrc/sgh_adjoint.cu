@@ -717,6 +717,73 @@ __global__ void __launch_bounds__(256) k_adj_vel0(const AdjMesh m, const AdjBufs
 }
 
 // ---------------------------------------------------------------------------
+// Branch record and frozen-branch forward.
+
+// The first node pair attaining the CFL minimum of the recorded element.
+__global__ void k_adj_pair(AdjRecord* r, const AdjMesh m, const Slot s) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int e = r->estar;
+  r->pair = -1;
+  if (e < 0 || e >= m.ne) return;
+  int nid[8];
+  load_nodes(m.nie, e, nid);
+  double x[8], y[8], z[8];
+  for (int l = 0; l < 8; ++l) {
+    x[l] = s.x[nid[l]];
+    y[l] = s.y[nid[l]];
+    z[l] = s.z[nid[l]];
+  }
+  int pair;
+  min_pair_d2(x, y, z, &pair);
+  r->pair = pair;
+}
+
+// The time step of the frozen-branch forward (time_integration.cpp:54-154 with the
+// recorded cycle's decisions): the growth cap of this run's previous dt, the CFL
+// step of the recorded element and node pair in this run's state, the dt_max /
+// dt_min bounds, or the graphics / final-time clamps of this run's time.  On the
+// recorded trajectory itself it equals the cycle kernels' dt bit for bit.
+__global__ void k_adj_dt_frozen(const AdjRecord* __restrict__ rp, Ctrl* c, const LoopParams lp, const AdjMesh m,
+                                const Slot s) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (c->stopped) {
+    c->active = 0;
+    return;
+  }
+  const AdjRecord r = *rp;
+  double dt_rec;
+  const int br = dt_branch(r.dt_prev, r.time_value, r.graphics_time, r.cfl_key, lp, &dt_rec);
+  double dt = dt_rec;
+  if (br == BR_GROW) {
+    dt = c->dt * 1.1;
+  } else if (br == BR_CFL) {
+    const int e = r.estar;
+    if (e >= 0 && e < m.ne && r.pair >= 0 && r.pair < 28) {
+      int nid[8];
+      load_nodes(m.nie, e, nid);
+      double x[8], y[8], z[8];
+      for (int l = 0; l < 8; ++l) {
+        x[l] = s.x[nid[l]];
+        y[l] = s.y[nid[l]];
+        z[l] = s.z[nid[l]];
+      }
+      const double d2 = cfl::exact_d2(x, y, z, cfl::pair_a(r.pair), cfl::pair_b(r.pair));
+      dt = lp.dt_cfl * sqrt(d2) / (s.sspd[e] + lp.fuzz);
+    }
+  } else if (br == BR_DTMAX) {
+    dt = lp.dt_max;
+  } else if (br == BR_DTMIN) {
+    dt = lp.dt_min;
+  } else if (br == BR_GRAPH) {
+    dt = (c->graphics_time - c->time_value) + lp.fuzz;
+  } else if (br == BR_FINAL) {
+    dt = lp.time_final - c->time_value;
+  }
+  c->dt = dt;
+  c->active = 1;
+}
+
+// ---------------------------------------------------------------------------
 static unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 static void launch_eos(int ne, const double* sie, const double* den, const double* gamma, const double* csmin,
@@ -762,13 +829,21 @@ static void launch_dt(const AdjMesh& m, const AdjBufs& b, const AdjRecord* r, co
 static void launch_vel0(const AdjMesh& m, const AdjBufs& b, const Node6& an, cudaStream_t st) {
   k_adj_vel0<<<blocks_for(m.nn, 256), 256, 0, st>>>(m, b, an);
 }
+static void launch_pair(AdjRecord* r, const AdjMesh& m, const Slot& s, cudaStream_t st) {
+  k_adj_pair<<<1, 32, 0, st>>>(r, m, s);
+}
+static void launch_dt_frozen(const AdjRecord* r, Ctrl* ctrl, const LoopParams& lp, const AdjMesh& m, const Slot& s,
+                             cudaStream_t st) {
+  k_adj_dt_frozen<<<1, 32, 0, st>>>(r, ctrl, lp, m, s);
+}
 
 }  // namespace adj_impl
 
 const AdjLaunch& adjoint_kernels() {
   static const AdjLaunch k = {adj_impl::launch_eos,  adj_impl::launch_pre,   adj_impl::launch_argmin,
                               adj_impl::launch_seed, adj_impl::launch_elem,  adj_impl::launch_node,
-                              adj_impl::launch_force, adj_impl::launch_dt,   adj_impl::launch_vel0};
+                              adj_impl::launch_force, adj_impl::launch_dt,   adj_impl::launch_vel0,
+                              adj_impl::launch_pair,  adj_impl::launch_dt_frozen};
   return k;
 }
 

@@ -46,6 +46,7 @@ struct AdjRecord {
   long long cycle;                                // completed cycles before it
   int estar;                                      // element attaining the CFL minimum
   int active;
+  int pair;                                       // its node pair attaining the minimum (branch record)
 };
 
 #define FIERRO_ADJ_STATUS_DT_MISMATCH 1u  // re-derived dt differs from the recorded one
@@ -116,6 +117,12 @@ struct AdjLaunch {
              int stages, const AdjAlphas& al, const Node6& an_c, double* sie_c, cudaStream_t);
   // velocity adjoint of the uploaded state into b.fbar[0..2]
   void (*vel0)(const AdjMesh& m, const AdjBufs& b, const Node6& an, cudaStream_t);
+  // branch record: the node pair of the recorded CFL element (after argmin)
+  void (*pair)(AdjRecord* r, const AdjMesh& m, const Slot& s, cudaStream_t);
+  // frozen-branch forward: the cycle's dt along the recorded dt branch, from
+  // the current state s and loop scalars
+  void (*dt_frozen)(const AdjRecord* r, Ctrl* ctrl, const LoopParams& lp, const AdjMesh& m, const Slot& s,
+                    cudaStream_t);
 };
 
 const AdjLaunch& adjoint_kernels();

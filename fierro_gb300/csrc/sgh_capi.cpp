@@ -272,6 +272,7 @@ extern "C" int fierro_sgh_destroy(fierro_sgh* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   output_release(h);
   adj_release(h);
+  adj_branches_release(h);
   for (int c = 0; c < 2; ++c)
     if (h->graph[c]) cudaGraphExecDestroy(h->graph[c]);
   for (void* p : h->allocations) cudaFree(p);
@@ -961,6 +962,10 @@ extern "C" int fierro_sgh_solve(const fierro_mesh* mesh, const fierro_material* 
 // dt_start (fierro_sgh_set_state does the same).
 namespace {
 
+// State variables per element a checkpoint may carry (the strength model reads
+// kUserStrengthStateVars of them); larger counts in a header are refused as corrupt.
+constexpr int64_t kMaxCheckpointStateVars = 4096;
+
 struct CkptHeader {
   char magic[8];
   uint32_t version, dims;
@@ -1096,22 +1101,40 @@ extern "C" int fierro_sgh_restart(fierro_sgh* h, const char* path) {
     std::fclose(f);
     return set_error(FIERRO_EINVAL, "restart: %s is not a checkpoint of this library", path);
   }
+  // Every header field is checked against this handle, and the file's length
+  // against the payload the header implies, before anything of the handle
+  // changes: a refused file leaves the current state and graphs as they were.
+  CkptHeader mine = ckpt_header(h);
+  mine.base = hd.base;
+  mine.nsv = hd.nsv;
+  const bool nsv_ok = h->strength ? (hd.nsv >= kUserStrengthStateVars && hd.nsv <= kMaxCheckpointStateVars)
+                                  : hd.nsv == 0;
+  if (std::memcmp(&mine, &hd, sizeof(hd)) != 0 || !nsv_ok || (hd.base != 0 && hd.base != 1)) {
+    std::fclose(f);
+    return set_error(FIERRO_EINVAL, "restart: %s was written by a handle with another mesh, deck or parameters",
+                     path);
+  }
+  size_t payload = 0;
+  for (const Block& b : ckpt_blocks(h)) payload += b.bytes;
+  if (h->strength) {
+    const size_t ne = (size_t)h->ne;
+    payload = payload - sizeof(double) * ne * (size_t)(h->d_statev ? h->nsv : 0) +
+              sizeof(double) * ne * (size_t)hd.nsv;
+  }
+  if (std::fseek(f, 0, SEEK_END) != 0 || std::ftell(f) != (long)(sizeof(hd) + payload) ||
+      std::fseek(f, (long)sizeof(hd), SEEK_SET) != 0) {
+    std::fclose(f);
+    return set_error(FIERRO_EINVAL, "restart: %s is truncated or longer than its header says", path);
+  }
   CUDA_TRY(cudaStreamSynchronize(h->stream));
-  h->has_state = false;
-  if (h->strength && hd.nsv >= kUserStrengthStateVars) {
+  if (h->strength) {
     const int rc = size_statev(h, hd.nsv);
     if (rc) {
       std::fclose(f);
       return rc;
     }
   }
-  CkptHeader mine = ckpt_header(h);
-  mine.base = hd.base;
-  if (std::memcmp(&mine, &hd, sizeof(hd)) != 0) {
-    std::fclose(f);
-    return set_error(FIERRO_EINVAL, "restart: %s was written by a handle with another mesh, deck or parameters",
-                     path);
-  }
+  h->has_state = false;
   if (h->adj) adj_release(h);
   output_reset(h);
   std::vector<char> buf;

@@ -66,6 +66,10 @@ struct ForceArgs {
   // each element, rows of kForceTapeRows x ne, and the limiter's neighbour
   double* tape;
   int* tape_sel;
+  // adjoint branch record / freeze only (force_branch launcher): one byte of
+  // branch bits per element (FIERRO_BR_* below) and the limiter's neighbour
+  unsigned char* br_flags;
+  int* br_sel;
   // strength materials (set when the handle has one; stress rows [9][ne],
   // row i*3+j): the reference's stress(1) as this stage's force reads it, the
   // cycle-start stress(0), and where the stage's stress(1) goes
@@ -79,6 +83,18 @@ struct ForceArgs {
   int copy_stress;     // stage 0: elements without a hypo model carry stress_cur over
   int block;           // threads per block (0: kForceBlock)
 };
+
+// Branch bits of one element's corner force in one stage, recorded on a base
+// trajectory and replayed by the frozen-branch forward (the forward whose
+// central differences are the derivative the discrete adjoint computes).
+#define FIERRO_BR_COMPRESS 1u   // div < 0: the compression coefficients q1, q2
+#define FIERRO_BR_VSTAR 2u      // sum mu > fuzz: the Riemann velocity is the mu-weighted mean
+#define FIERRO_BR_MACH_CLAMP 4u // the Mach switch's argument reached 1 (alpha = 1)
+#define FIERRO_BR_LIM_SHIFT 3   // limiter case, 2 bits: FIERRO_LIM_*
+#define FIERRO_LIM_NONE 0u      // r_min = 1 (no neighbour below): phi0 = 0
+#define FIERRO_LIM_FACE 1u      // 0 < r_min < 1 at the recorded neighbour: phi0 = 1 - r_face
+#define FIERRO_LIM_FULL 2u      // r_min <= 0: phi0 = 1
+#define FIERRO_LIM_IRREGULAR 3u // non-finite or zero divergence: evaluated as the cycle does
 
 // Rows of the force kernel's tape: mu[8], |v_l - v_avg|[8], v*[3], sum mu,
 // phi0 (limiter), the Mach-switch argument, vol^(1/3), the limiter's r_min.
@@ -153,6 +169,9 @@ struct EnergyArgs {
 struct KernelSet {
   void (*force)(const ForceArgs&, cudaStream_t);
   void (*force_tape)(const ForceArgs&, cudaStream_t);  // the same, also writing a.tape / a.tape_sel
+  // mode 1: the plain force, also recording a.br_flags / a.br_sel; mode 2: the
+  // force with those branches frozen (gas-only hex handles, exact mode)
+  void (*force_branch)(const ForceArgs&, int mode, cudaStream_t);
   void (*node)(const NodeArgs&, cudaStream_t);
   void (*elem)(const ElemArgs&, int kind, cudaStream_t);
   void (*dt)(const DtArgs&, cudaStream_t);

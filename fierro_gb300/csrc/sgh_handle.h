@@ -30,6 +30,7 @@
 
 namespace fierro {
 struct AdjState;
+struct AdjBranches;
 struct OutputState;
 struct RzKernelSet;
 }
@@ -78,6 +79,7 @@ struct fierro_sgh {
   bool has_state = false;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   fierro::AdjState* adj = nullptr;  // discrete-adjoint tape and checkpoints (sgh_adjoint.cpp)
+  fierro::AdjBranches* adj_br = nullptr;  // branch record of the frozen-branch forward (sgh_adjoint.cpp)
   // direct transfers (sgh_xfer.cu): caller -> internal maps and the validation word
   bool direct_host = false;
   int* d_node_ext2int = nullptr;
@@ -163,6 +165,8 @@ inline int div_parity(const fierro_sgh* h, int c, int s) { return (c * h->rk_num
 
 // Frees the adjoint's device memory (no-op without one).
 void adj_release(fierro_sgh* h);
+// Frees the branch record of the frozen-branch forward (no-op without one).
+void adj_branches_release(fierro_sgh* h);
 
 // Graphics dumps (sgh_output.cpp).
 void output_release(fierro_sgh* h);

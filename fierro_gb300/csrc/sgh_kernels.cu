@@ -85,7 +85,11 @@ __device__ __forceinline__ void velocity_gradient(const double (&u)[8], const do
 // runs the hypo model (:366-391) with the velocity gradient of this state.
 // TAPE (the adjoint's replay, exact mode) also stores the viscosity
 // intermediates; the stores do not change any value the kernel computes.
-template <bool BATCH, bool TAPE, bool STRENGTH>
+// BR = 1 records the element's branch decisions (compression sign, Riemann
+// velocity, limiter case and neighbour, Mach clamp) without changing any value;
+// BR = 2 takes them from the record instead of deciding them, so the force is a
+// smooth function of the state along the recorded trajectory's branches.
+template <bool BATCH, bool TAPE, bool STRENGTH, int BR = 0>
 __global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
   if (!BATCH && !a.ctrl->active) return;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -105,7 +109,8 @@ __global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
   const double den = a.den[e], pres = a.pres[e], sspd = a.sspd[e], vol = a.vol[e], div = a.div[e];
   const int mat = a.mat[e];
   const double* q = a.qtab + 4 * mat;
-  const bool compress = div < 0;
+  const unsigned br = BR == 2 ? (unsigned)a.br_flags[e] : 0u;
+  const bool compress = BR == 2 ? (br & FIERRO_BR_COMPRESS) != 0 : div < 0;
   const double qa = compress ? q[0] : q[1];  // q1 or q1ex
   const double qb = compress ? q[2] : q[3];  // q2 or q2ex
 
@@ -141,7 +146,7 @@ __global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
     mu[l] = mu_term;
   }
   double vstar0 = 0.0, vstar1 = 0.0, vstar2 = 0.0;
-  if (s3 > a.fuzz) {
+  if (BR == 2 ? (br & FIERRO_BR_VSTAR) != 0 : s3 > a.fuzz) {
     vstar0 = s0 / s3;
     vstar1 = s1 / s3;
     vstar2 = s2 / s3;
@@ -160,9 +165,10 @@ __global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
     kmax = key > kmax ? key : kmax;
   }
   double r_min = 1.0;
+  bool regular = true;
   if (k1 > k0) {
     const double dsel = okey_decode(D > 0 ? kmin : kmax);
-    const bool regular = isfinite(D) && D != 0.0 && isfinite(dsel);
+    regular = isfinite(D) && D != 0.0 && isfinite(dsel);
     if (regular) {
       const double r_face = 0.9 * (dsel + small) / D;
       r_min = okey(r_face) < okey(1.0) ? r_face : 1.0;
@@ -177,7 +183,41 @@ __global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
   // Mach-number detector (:318-328)
   const double c_length = pow_third(vol);
   const double araw = 20.0 * (c_length * fabs(div)) / (sspd + a.fuzz);
-  const double alpha = fmin(1.0, araw);
+  double alpha = fmin(1.0, araw);
+  if (BR == 1) {
+    // the limiter's case, and the neighbour that set r_min on the r_face branch
+    unsigned lim = FIERRO_LIM_NONE;
+    int sel = -1;
+    if (k1 > k0 && !regular) {
+      lim = FIERRO_LIM_IRREGULAR;
+    } else if (r_min < 1.0 && r_min > 0.0) {
+      lim = FIERRO_LIM_FACE;
+      const long long ksel = D > 0 ? kmin : kmax;
+      for (int k = k0; k < k1; ++k) {
+        const int nb = __ldg(a.eie + k);
+        if (okey(__ldg(a.div + nb)) == ksel) {
+          sel = nb;
+          break;
+        }
+      }
+    } else if (!(r_min > 0.0)) {
+      lim = FIERRO_LIM_FULL;
+    }
+    a.br_flags[e] = (unsigned char)((compress ? FIERRO_BR_COMPRESS : 0u) | (s3 > a.fuzz ? FIERRO_BR_VSTAR : 0u) |
+                                    (araw < 1.0 ? 0u : FIERRO_BR_MACH_CLAMP) | (lim << FIERRO_BR_LIM_SHIFT));
+    a.br_sel[e] = sel;
+  }
+  if (BR == 2) {
+    const unsigned lim = (br >> FIERRO_BR_LIM_SHIFT) & 3u;
+    if (lim == FIERRO_LIM_NONE) {
+      phi = 0.0;
+    } else if (lim == FIERRO_LIM_FULL) {
+      phi = 1.0;
+    } else if (lim == FIERRO_LIM_FACE && a.br_sel[e] >= 0) {
+      phi = 1.0 - 0.9 * (__ldg(a.div + a.br_sel[e]) + small) / D;
+    }  // FIERRO_LIM_IRREGULAR: as evaluated above
+    alpha = (br & FIERRO_BR_MACH_CLAMP) ? 1.0 : araw;
+  }
   if (TAPE) {
     double* t = a.tape + e;
 #pragma unroll
@@ -571,6 +611,11 @@ static void launch_force_tape(const ForceArgs& a, cudaStream_t s) {
   const int bs = block_or(a.block, kForceBlock);
   k_force<false, true, false><<<blocks_for(a.ne, bs), bs, 0, s>>>(a);
 }
+static void launch_force_branch(const ForceArgs& a, int mode, cudaStream_t s) {
+  const int bs = block_or(a.block, kForceBlock);
+  if (mode == 1) k_force<false, false, false, 1><<<blocks_for(a.ne, bs), bs, 0, s>>>(a);
+  else k_force<false, false, false, 2><<<blocks_for(a.ne, bs), bs, 0, s>>>(a);
+}
 static void launch_node(const NodeArgs& a, cudaStream_t s) {
   const int bs = a.inst ? kNodeBlock : block_or(a.block, kNodeBlock);
   if (a.inst) k_node<true><<<blocks_for(a.nn, bs), bs, 0, s>>>(a);
@@ -607,14 +652,14 @@ static void launch_energy(const EnergyArgs& a, cudaStream_t s) {
 
 #if FIERRO_FMA
 const KernelSet& kernels_fma() {
-  static const KernelSet k = {fma_impl::launch_force, fma_impl::launch_force_tape, fma_impl::launch_node, fma_impl::launch_elem,
+  static const KernelSet k = {fma_impl::launch_force, fma_impl::launch_force_tape, fma_impl::launch_force_branch, fma_impl::launch_node, fma_impl::launch_elem,
                               fma_impl::launch_dt, fma_impl::launch_end, fma_impl::launch_energy,
                               fma_impl::launch_end_batch, "fma"};
   return k;
 }
 #else
 const KernelSet& kernels_exact() {
-  static const KernelSet k = {exact_impl::launch_force, exact_impl::launch_force_tape, exact_impl::launch_node, exact_impl::launch_elem,
+  static const KernelSet k = {exact_impl::launch_force, exact_impl::launch_force_tape, exact_impl::launch_force_branch, exact_impl::launch_node, exact_impl::launch_elem,
                               exact_impl::launch_dt, exact_impl::launch_end, exact_impl::launch_energy,
                               exact_impl::launch_end_batch, "exact"};
   return k;

@@ -18,6 +18,7 @@
 #include <cstdint>
 #include <mutex>
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "fierro_sgh.h"
@@ -27,7 +28,6 @@ namespace {
 
 constexpr int kTallyBlocks = 512;
 constexpr int kTallyThreads = 256;
-constexpr int kMaxDevices = 64;
 // Largest array length a call accepts: the kernels index with 32-bit integers
 // and stride by the whole grid, so counts stay below 2^31 - grid size.
 constexpr int64_t kTallyMaxLength = (int64_t)1 << 30;
@@ -76,26 +76,87 @@ __global__ void k_tally_final(const double* part, int nblocks, double* out) {
   out[1] = 0.5 * ke;
 }
 
-std::mutex g_setup_mutex;
-double* g_scratch_addr[kMaxDevices] = {};
+// The scratch array's device address belongs to the CUDA context that loaded
+// this module, not to the device: after cudaDeviceReset (or any other teardown
+// and re-creation of the primary context) the module is loaded again, possibly
+// at another address, and a second context on the same device (cuCtxCreate)
+// holds its own copy of the array.  The address is therefore cached per
+// context, under the driver's process-unique context id, and looked up again
+// for a context not seen before.  The lookup (cudaGetSymbolAddress, which may
+// load the module) happens on the first call in each context; that call should
+// come before any stream capture in that context.
+constexpr int kMaxContexts = 64;
 
-// Device address of g_tally_scratch on the current device, looked up once per
-// device.  In host code the array's name is only a host-side stand-in, so the
-// kernels are always given this address.
+struct ScratchEntry {
+  unsigned long long ctx_id;
+  double* addr;
+};
+
+std::mutex g_setup_mutex;
+ScratchEntry g_scratch[kMaxContexts] = {};
+int g_scratch_used = 0, g_scratch_next = 0;
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+// The driver's cuCtxGetCurrent / cuCtxGetId, through the runtime's entry-point
+// query (the library does not link libcuda itself).  Called with the mutex held.
+int driver_entry_points() {
+  if (g_ctx_get_current && g_ctx_get_id) return FIERRO_OK;
+  void* f1 = nullptr;
+  void* f2 = nullptr;
+  cudaDriverEntryPointQueryResult q1{}, q2{};
+  cudaError_t e1 = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+  cudaError_t e2 = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+  if (e1 != cudaSuccess || e2 != cudaSuccess || q1 != cudaDriverEntryPointSuccess ||
+      q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+    return fierro::set_error(FIERRO_ECUDA, "energy tally: driver entry points cuCtxGetCurrent/cuCtxGetId unavailable");
+  g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+  g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f2);
+  return FIERRO_OK;
+}
+
+// Device address of g_tally_scratch in the current context.  In host code the
+// array's name is only a host-side stand-in, so the kernels are always given
+// this address.
 int scratch_address(double** out) {
-  int dev = 0;
-  cudaError_t err = cudaGetDevice(&dev);
-  if (err != cudaSuccess) return fierro::set_error(FIERRO_ECUDA, "cudaGetDevice: %s", cudaGetErrorString(err));
-  if (dev < 0 || dev >= kMaxDevices) return fierro::set_error(FIERRO_EINVAL, "device ordinal %d unsupported", dev);
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    err = cudaGetSymbolAddress(&p, g_tally_scratch);
+  int rc = driver_entry_points();
+  if (rc) return rc;
+  CUcontext ctx = nullptr;
+  if (g_ctx_get_current(&ctx) != CUDA_SUCCESS)
+    return fierro::set_error(FIERRO_ECUDA, "energy tally: cuCtxGetCurrent failed");
+  void* p = nullptr;
+  if (!ctx) {
+    // no context is current on this thread yet: the runtime call below makes
+    // the current device's primary context current
+    cudaError_t err = cudaGetSymbolAddress(&p, g_tally_scratch);
     if (err != cudaSuccess || !p)
       return fierro::set_error(FIERRO_ECUDA, "cudaGetSymbolAddress(tally scratch): %s", cudaGetErrorString(err));
-    g_scratch_addr[dev] = static_cast<double*>(p);
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx)
+      return fierro::set_error(FIERRO_ECUDA, "energy tally: no current CUDA context");
   }
-  *out = g_scratch_addr[dev];
+  unsigned long long id = 0;
+  if (g_ctx_get_id(ctx, &id) != CUDA_SUCCESS) return fierro::set_error(FIERRO_ECUDA, "energy tally: cuCtxGetId failed");
+  for (int i = 0; i < g_scratch_used; ++i)
+    if (g_scratch[i].ctx_id == id) {
+      *out = g_scratch[i].addr;
+      return FIERRO_OK;
+    }
+  if (!p) {
+    cudaError_t err = cudaGetSymbolAddress(&p, g_tally_scratch);
+    if (err != cudaSuccess || !p)
+      return fierro::set_error(FIERRO_ECUDA, "cudaGetSymbolAddress(tally scratch): %s", cudaGetErrorString(err));
+  }
+  // context ids are never reused within a process, so an entry of a destroyed
+  // context is only ever dead weight: the oldest entry makes room when full
+  ScratchEntry& e = g_scratch_used < kMaxContexts ? g_scratch[g_scratch_used++] : g_scratch[g_scratch_next++];
+  if (g_scratch_next == kMaxContexts) g_scratch_next = 0;
+  e.ctx_id = id;
+  e.addr = static_cast<double*>(p);
+  *out = e.addr;
   return FIERRO_OK;
 }
 

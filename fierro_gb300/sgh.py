@@ -24,6 +24,7 @@ LIB_PATH = os.path.join(HERE, "libfierro_sgh.so")
 
 FIERRO_OK, FIERRO_EINVAL, FIERRO_ENOMEM, FIERRO_ECUDA, FIERRO_ENUMERIC, FIERRO_ETIMEDOUT, FIERRO_ENOTSUP = range(7)
 FP_EXACT, FP_FMA = 0, 1
+ADJ_BRANCHES_OFF, ADJ_BRANCHES_RECORD, ADJ_BRANCHES_FREEZE = 0, 1, 2
 HEALTH_BAD_VOLUME, HEALTH_BAD_STATE, HEALTH_DT_FLOOR = 1, 2, 4
 OUTPUT_ENSIGHT, OUTPUT_STATE = 1, 2
 _ERRNAMES = {1: "EINVAL", 2: "ENOMEM", 3: "ECUDA", 4: "ENUMERIC", 5: "ETIMEDOUT", 6: "ENOTSUP"}
@@ -115,6 +116,7 @@ def _load():
     lib.fierro_adj_verify.argtypes = [vp, C.c_int]
     lib.fierro_adj_stats.argtypes = [vp, C.POINTER(i64), i64]
     lib.fierro_adj_release.argtypes = [vp]
+    lib.fierro_adj_branches.argtypes = [vp, C.c_int]
     lib.fierro_sgh_checkpoint.argtypes = [vp, C.c_char_p]
     lib.fierro_sgh_restart.argtypes = [vp, C.c_char_p]
     lib.fierro_sgh_validate.argtypes = [vp]
@@ -399,6 +401,13 @@ class SGHSolver:
 
     def adj_release(self):
         _check(_lib.fierro_adj_release(self.h))
+
+    def adj_branches(self, mode: int):
+        """fierro_adj_branches: ADJ_BRANCHES_RECORD makes the next adj_forward calls
+        record the forward's branch decisions; ADJ_BRANCHES_FREEZE runs later
+        adj_forward calls with the recorded decisions (the frozen-branch forward);
+        ADJ_BRANCHES_OFF returns to plain forwards."""
+        _check(_lib.fierro_adj_branches(self.h, int(mode)))
 
 
 class DeviceView(C.Structure):

@@ -273,9 +273,11 @@ int64_t fierro_batch_device_bytes(const fierro_batch* b);
  * memory belongs to the caller's own arena), and it allocates nothing.  Its
  * scratch is an 8 KiB array held by every GPU that loads the library until the
  * process exits; at most 2^30 elements and 2^30 nodes per call (EINVAL beyond).
- * The first call on each device looks up that array's device address, so make
- * the first call before any stream capture.  All calls share the array: calls
- * that overlap on the GPU race on it. */
+ * The first call in each CUDA context (the device's primary context, again after
+ * a cudaDeviceReset, or a context of the caller's own) looks up that array's
+ * device address in that context, so make the first call in a context before
+ * any stream capture in it.  All calls share the array: calls that overlap on
+ * the GPU race on it. */
 int fierro_energy_tally_noalloc(const double* elem_mass, const double* elem_sie, int64_t num_elems,
                                 const double* node_mass, const double* node_u, const double* node_v,
                                 const double* node_w, int64_t num_nodes, double* ie_ke, void* stream);
@@ -377,6 +379,29 @@ int fierro_adj_stats(const fierro_sgh* h, int64_t* out, int64_t n);
 
 /* Frees the adjoint's device memory (also done by fierro_sgh_destroy). */
 int fierro_adj_release(fierro_sgh* h);
+
+/* Frozen-branch forward (no counterpart in the reference).  The forward has
+ * switches: the corner force's compression coefficients (div < 0), the Riemann
+ * velocity's guard, the shock limiter's minimising neighbour and its clamps to
+ * [0, 1], the Mach switch min(1, .) (force_sgh.cpp:147-329), and the time
+ * step's CFL minimiser (element and node pair), growth cap and clamps
+ * (time_integration.cpp:54-154).  J is therefore piecewise smooth, and the
+ * adjoint is the derivative of the piece the forward's own run lies on.
+ *   FIERRO_ADJ_BRANCHES_RECORD: the next fierro_adj_forward calls also record
+ *     every such decision, cycle by cycle (1 + 4 bytes per element per RK stage
+ *     per cycle, plus one record per cycle; the forward's values are unchanged);
+ *   FIERRO_ADJ_BRANCHES_FREEZE: fierro_adj_forward runs with the decisions of
+ *     the recorded run instead of making them (same cycle count; no checkpoints,
+ *     and no fierro_adj_backward after it).  On the recorded parameters it
+ *     reproduces the recorded run bit for bit; for other parameters its result
+ *     is the smooth piece the adjoint differentiates, so its central
+ *     differences check the adjoint without straddling the switches;
+ *   FIERRO_ADJ_BRANCHES_OFF: plain forwards again; frees the record.
+ * Exact-mode gas-only hex handles (FIERRO_ENOTSUP otherwise). */
+#define FIERRO_ADJ_BRANCHES_OFF 0
+#define FIERRO_ADJ_BRANCHES_RECORD 1
+#define FIERRO_ADJ_BRANCHES_FREEZE 2
+int fierro_adj_branches(fierro_sgh* h, int mode);
 
 #ifdef __cplusplus
 }

@@ -34,7 +34,10 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 STAGE = os.path.join(OUT, "src")
-REF_SGH = "/root/reference/Explicit-Lagrange-Kokkos/SGH_solver"
+# The reference checkout: FIERRO_REFERENCE_ROOT, else the read-only mount of
+# this build machine.
+REF_ROOT = os.environ.get("FIERRO_REFERENCE_ROOT", "/root/reference")
+REF_SGH = os.path.join(REF_ROOT, "Explicit-Lagrange-Kokkos", "SGH_solver")
 
 REF_UNITS = [
     "sgh_solve.cpp", "setup.cpp", "geometry.cpp", "momentum.cpp", "force_sgh.cpp",
@@ -143,6 +146,43 @@ def build_reference(verbose=False, jobs=None):
             _run(["g++", "-fopenmp", "-o", target] + ob + ["-lm"])
         paths[exe] = target
     return paths
+
+
+def build_reference_lib(verbose=False):
+    """fierro_ref_lib: the reference's driver sequence (ref_harness.cpp) with its
+    sgh_solve call replaced by the reference-side binding of the GB300 library
+    (oracle/ref/fierro_sgh_call.inc, the snippet of the integration notes),
+    linked against fierro_gb300/libfierro_sgh.so.  Needs the reference objects
+    (build_reference) and the library.  Returns the executable's path, or None
+    when the reference sources are unavailable."""
+    paths = build_reference()
+    if paths is None:
+        return None
+    root = os.path.dirname(HERE)
+    libdir = os.path.join(root, "fierro_gb300")
+    lib = os.path.join(libdir, "libfierro_sgh.so")
+    if not os.path.exists(lib):
+        raise FileNotFoundError(lib)
+    src_dir = _source_dir()
+    compat = os.path.join(HERE, "compat")
+    ref_dir = os.path.join(HERE, "ref")
+    harness = os.path.join(ref_dir, "ref_harness.cpp")
+    snippet = os.path.join(ref_dir, "fierro_sgh_call.inc")
+    header = os.path.join(root, "include", "fierro_sgh.h")
+    obj = os.path.join(OUT, "obj", "ref_harness_lib.cpp.exact.o")
+    deps = [harness, snippet, header, os.path.join(compat, "matar.h"), __file__] + \
+        [os.path.join(src_dir, h) for h in REF_HEADERS]
+    if not _newer(obj, deps):
+        _run(["g++", "-std=c++17", "-O3", "-fopenmp", "-w", "-ffp-contract=off", "-DFIERRO_REF_CALL_LIBRARY",
+              "-I", compat, "-I", src_dir, "-I", ref_dir, "-I", os.path.join(root, "include"),
+              "-c", harness, "-o", obj])
+    names = REF_UNITS + ["ref_read_mesh_bin.cpp", "ref_input.cpp", "ref_user_mat.cpp"]
+    objs = [os.path.join(OUT, "obj", "%s.exact.o" % n) for n in names] + [obj]
+    target = os.path.join(OUT, "fierro_ref_lib")
+    if not _newer(target, objs + [lib]):
+        _run(["g++", "-fopenmp", "-o", target] + objs +
+             ["-L", libdir, "-lfierro_sgh", "-Wl,-rpath," + libdir, "-lm"])
+    return target
 
 
 def main():

@@ -289,3 +289,24 @@ def run_reference(problem, cycles: int | None = None, kind: str = "fierro_ref", 
     st["setup_seconds"] = float(m.group(1)) if m else float("nan")
     st["stdout"] = p.stdout
     return st
+
+
+def density_mismatch_forward(dm, variant: str = "libm"):
+    """J of a fierro_gb300.adjoint.DensityMismatch computed by the C restatement
+    (the reference's algorithm) instead of the GPU: a callable (sie0, gamma) -> J
+    for dm.fd(..., forward=...), the check of the adjoint against central
+    differences of the reference's forward."""
+    from fierro_gb300.adjoint import eos_state
+
+    def f(sie0, gamma):
+        o = Oracle(dm.problem, variant=variant)
+        st = eos_state(dm.state0, np.asarray(sie0, dtype=np.float64),
+                       np.broadcast_to(np.asarray(gamma, dtype=np.float64), dm.sie0.shape).copy())
+        o.set(ORC_ELEM_SIE, st["elem_sie"])
+        o.set(ORC_ELEM_PRES, st["elem_pres"])
+        o.set(ORC_ELEM_SSPD, st["elem_sspd"])
+        o.set(ORC_ELEM_STATEV, st["elem_statev"])
+        o.run_cycles(dm.cycles)
+        return dm.value(o.get(ORC_ELEM_DEN))
+
+    return f

@@ -5,8 +5,11 @@
 // no-op, since graphics dumps are outside the measured path, except in the
 // fierro_ref_out build (-DFIERRO_REF_REAL_OUTPUTS), which links the reference's
 // own outputs.cpp and writes its EnSight and state files into the working
-// directory.  Linked only into the reference oracle executables built by
-// oracle/build_ref.py.
+// directory, and except in the fierro_ref_lib build (-DFIERRO_REF_CALL_LIBRARY),
+// where the sgh_solve call is replaced by the reference-side binding of the GB300
+// library (oracle/ref/fierro_sgh_call.inc: the same arrays to fierro_sgh_solve),
+// linked against libfierro_sgh.so.  Linked only into the reference oracle
+// executables built by oracle/build_ref.py.
 //
 // usage: fierro_ref <config.txt> <mesh.geo|mesh.bin> <state_out.bin>
 // env FIERRO_REF_WARMUP=W runs W untimed cycles first (see main).
@@ -23,6 +26,11 @@
 #include "matar.h"
 #include "mesh.h"
 #include "state.h"
+#ifdef FIERRO_REF_CALL_LIBRARY
+#include <vector>
+
+#include "fierro_sgh.h"
+#endif
 
 const char* fierro_ref_config_path = nullptr;
 
@@ -122,11 +130,19 @@ int main(int argc, char* argv[]) {
                 graphics_time, graphics_cyc_ival, graphics_dt_ival, warm_cycles, rk_num_stages, dt, fuzz,
                 tiny, small, graphics_times, graphics_id);
 
+#ifdef FIERRO_REF_CALL_LIBRARY
+    // the reference-side binding of the GB300 library, verbatim (the snippet the
+    // integration notes show): the same host arrays go to fierro_sgh_solve
+    {
+#include "fierro_sgh_call.inc"
+    }
+#else
     sgh_solve(material, boundary, mesh, node_coords, node_vel, node_mass, elem_den, elem_pres,
               elem_stress, elem_sspd, elem_sie, elem_vol, elem_div, elem_mass, elem_mat_id,
               elem_statev, corner_force, corner_mass, time_value, time_final, dt_max, dt_min, dt_cfl,
               graphics_time, graphics_cyc_ival, graphics_dt_ival, cycle_stop, rk_num_stages, dt, fuzz,
               tiny, small, graphics_times, graphics_id);
+#endif
 
     FILE* f = std::fopen(argv[3], "wb");
     if (!f) return 3;

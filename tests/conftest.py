@@ -27,6 +27,40 @@ def field_error(got: np.ndarray, ref: np.ndarray, floor: float = 1e-3) -> float:
     return float(np.max(np.abs(got - ref) / np.maximum(np.abs(ref), floor * scale)))
 
 
+# Fields that are positive everywhere in every deck (density, pressure, energy,
+# sound speed, volume, mass): the tight metric compares each value at its own
+# scale.  The vector fields (positions on symmetry planes, velocities at rest)
+# pass through zero and keep a floor.
+POSITIVE_FIELDS = ("den", "pres", "sie", "sspd", "vol", "mass", "node_mass")
+TIGHT_FLOOR = 1e-9
+
+
+def field_error_tight(got: np.ndarray, ref: np.ndarray, key: str) -> float:
+    """The tight parity metric: purely relative, max |got - ref| / |ref|, for the
+    positive fields, so a quiescent cell (Sedov's 1e-10 background energy and
+    pressure) is compared at its own scale; for positions and velocities the
+    floor is 1e-9 of the field's peak instead of field_error's 1e-3."""
+    got = np.asarray(got, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    if not ref.size:
+        return 0.0
+    if key in POSITIVE_FIELDS:
+        return float(np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)))
+    return field_error(got, ref, TIGHT_FLOOR)
+
+
+def assert_fields_tight(got: dict, ref: dict, tol, keys=("coords", "vel", "den", "pres", "sie"), label: str = ""):
+    """field_error_tight within `tol` (a number, or a dict field -> bound for
+    the documented per-field bounds) for every key."""
+    bad = {}
+    for k in keys:
+        t = tol[k] if isinstance(tol, dict) else tol
+        e = field_error_tight(got[k], ref[k], k)
+        if not e <= t:
+            bad[k] = (e, t)
+    assert not bad, "%s: fields over the tight bound (error, bound): %s" % (label, bad)
+
+
 def assert_fields(got: dict, ref: dict, tol: float, keys=("coords", "vel", "den", "pres", "sie"),
                   floor: float = 1e-3, label: str = ""):
     bad = {}

@@ -41,7 +41,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-MESHES = "/root/reference/Explicit-Lagrange/meshes"
+# The reference checkout: FIERRO_REFERENCE_ROOT, else the read-only mount of
+# the machine the fixtures were made on.
+MESHES = os.path.join(os.environ.get("FIERRO_REFERENCE_ROOT", "/root/reference"), "Explicit-Lagrange", "meshes")
 FIELDS = ("coords", "vel", "den", "pres", "sie", "sspd", "vol")
 
 

@@ -225,3 +225,18 @@ def test_host_setup_random_decks(lib_built, oracle_built, dims):
                "pres": st["elem_pres"], "sie": st["elem_sie"][1], "sspd": st["elem_sspd"], "vol": st["elem_vol"],
                "mass": st["elem_mass"], "node_mass": st["node_mass"]}
         assert_bitwise(got, r, list(got), label="%s" % prob.name)
+
+
+def test_integration_notes_show_the_compiled_binding():
+    """The sgh_solve replacement shown in INTEGRATION.md section 1 is the text
+    that tests/test_gpu_binding.py compiles into the reference's driver
+    (oracle/ref/fierro_sgh_call.inc), so the documented binding is the tested one."""
+    import re
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    with open(os.path.join(root, "INTEGRATION.md")) as f:
+        doc = f.read()
+    sec = doc[doc.index("## 1."):doc.index("## 2.")]
+    blocks = re.findall(r"```cpp\n(.*?)```\n", sec, flags=re.S)
+    with open(os.path.join(root, "oracle", "ref", "fierro_sgh_call.inc")) as f:
+        inc = f.read()
+    assert blocks and blocks[0] == inc

@@ -60,7 +60,8 @@ def test_gradient_matches_gpu_finite_differences(lib_built):
 def test_gradient_matches_oracle_finite_differences(lib_built, oracle_built):
     dm = _case()
     J, sb, gb, vb = dm.gradient()
-    f = dm.oracle_forward()
+    from oracle import orc
+    f = orc.density_mismatch_forward(dm)
     assert abs(f(dm.sie0, dm.gamma0) - J) <= 1e-9 * J
     for d_sie, d_g in dm.directions(3, seed=3):
         ad = _directional(sb, gb, d_sie, d_g)
@@ -144,3 +145,45 @@ def test_adjoint_rejects_fma_mode_and_bad_calls(lib_built):
         s.run(1)  # the state moved on: backward must refuse
         with pytest.raises(sgh.FierroError):
             s.adj_backward(den=np.ones(p.mesh.num_elems))
+
+
+def test_frozen_forward_reproduces_the_recorded_run(lib_built):
+    """The frozen-branch forward on the recorded parameters is the recorded run
+    bit for bit (state, time, J), and recording changes neither the forward nor
+    the gradient."""
+    from fierro_gb300 import sgh
+    dm = _case()
+    J, sb, gb, vb = dm.gradient()
+    want = dm.solver.get_state()
+    t_want = dm.solver.time()
+    Jr, sbr, gbr, vbr = dm.gradient_frozen()
+    assert Jr == J and np.array_equal(sbr, sb) and np.array_equal(gbr, gb) and np.array_equal(vbr, vb)
+    Jf = dm.forward()
+    got = dm.solver.get_state()
+    assert Jf == J
+    g, w = sgh.compared_fields(got), sgh.compared_fields(want)
+    for k in w:
+        assert np.array_equal(g[k], w[k]), k
+    assert dm.solver.time() == t_want
+    # no backward after a frozen forward, and a cycle count other than the recorded one is refused
+    with pytest.raises(sgh.FierroError):
+        dm.solver.adj_backward(den=np.ones(dm.problem.mesh.num_elems))
+    dm.solver.set_state(dm.state0)
+    with pytest.raises(sgh.FierroError) as ei:
+        dm.solver.adj_forward(None, None, dm.cycles + 1, dm.ckpt_every)
+    assert ei.value.code == sgh.FIERRO_EINVAL
+    dm.unfreeze()
+    assert dm.forward() == J
+
+
+def test_gradient_matches_frozen_branch_differences(lib_built):
+    """Central differences (step 1e-6) of the frozen-branch forward against the
+    adjoint, 12^3 jittered Sedov, 100 cycles, four seeded directions."""
+    dm = _case()
+    J, sb, gb, vb = dm.gradient_frozen()
+    for d_sie, d_g in dm.directions(4, seed=11):
+        ad = _directional(sb, gb, d_sie, d_g)
+        fd = dm.fd(d_sie, d_g, h=1e-6)
+        assert abs(fd - ad) <= TOL * abs(fd), (fd, ad, abs(fd - ad) / abs(fd))
+    dm.unfreeze()
+

@@ -72,3 +72,56 @@ def test_restart_refuses_other_problems(lib_built, tmp_path):
         with pytest.raises(sgh.FierroError) as ei:
             c.restart(str(tmp_path / "junk.ckpt"))
         assert ei.value.code == sgh.FIERRO_EINVAL
+
+
+@pytest.mark.parametrize("case", ["sedov10_jp", "sedov8_hypo"])
+def test_refused_restart_leaves_the_handle_runnable(lib_built, tmp_path, case):
+    """A checkpoint that is refused (another deck, a corrupt state-variable count,
+    a truncated file, trailing bytes) changes nothing in the handle: its state,
+    time and energies stay as they were and the loop continues bit for bit as an
+    uninterrupted one."""
+    import struct
+    from fierro_gb300 import problems, sgh
+    prob = _problems()[case]()
+    st = sgh.setup(prob)
+    good = tmp_path / "good.ckpt"
+    with sgh.SGHSolver(prob) as w:
+        w.set_state(st)
+        w.run(9)
+        w.checkpoint(str(good))
+    raw = good.read_bytes()
+    bad = {}
+    nsv_off = 8 + 4 + 4 + 8 + 8  # magic, version, dims, nn, ne
+    for name, nsv in (("huge_nsv", 1 << 40), ("negative_nsv", -3), ("other_nsv", 7)):
+        bad[name] = raw[:nsv_off] + struct.pack("<q", nsv) + raw[nsv_off + 8:]
+    bad["truncated"] = raw[:len(raw) - 8]
+    bad["trailing"] = raw + b"\0"
+    other = problems.sedov(10, jitter=0.1, seed=4, permute=True, cycles=60)
+    p_other = tmp_path / "other.ckpt"
+    if case == "sedov10_jp":
+        with sgh.SGHSolver(other) as o:
+            o.set_state(sgh.setup(other))
+            o.run(2)
+            o.checkpoint(str(p_other))
+        bad["other_deck"] = p_other.read_bytes()
+    with sgh.SGHSolver(prob) as ref:
+        ref.set_state(st)
+        ref.run(5 + 11)
+        want = _snapshot(ref)
+    with sgh.SGHSolver(prob) as a:
+        a.set_state(st)
+        a.run(5)
+        before = _snapshot(a)
+        for name, data in bad.items():
+            path = tmp_path / (name + ".ckpt")
+            path.write_bytes(data)
+            with pytest.raises(sgh.FierroError) as ei:
+                a.restart(str(path))
+            assert ei.value.code == sgh.FIERRO_EINVAL, name
+            now = _snapshot(a)
+            for k in before:
+                assert np.array_equal(now[k], before[k]), (name, k)
+        a.run(11)
+        got = _snapshot(a)
+    for k in want:
+        assert np.array_equal(got[k], want[k]), k

@@ -11,7 +11,7 @@ fixtures, whose pow rounding differs from correct rounding in ~0.1% of calls.
 import numpy as np
 import pytest
 
-from conftest import assert_bitwise, assert_fields, field_error, load_golden
+from conftest import assert_bitwise, assert_fields, assert_fields_tight, field_error, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -112,6 +112,22 @@ def test_exact_vs_reference_golden(lib_built, case, cycles, tol):
 
 GATED = ("coords", "vel", "den", "pres", "sie")  # positions, velocities, density, pressure, energy
 
+# The tight metric (conftest.field_error_tight: density, pressure and energy
+# purely relative, so Sedov's 1e-10 background is compared at its own scale;
+# positions and velocities with a floor of 1e-9 of the peak) holds the FMA mode
+# to the same gates, 1e-12 after one cycle and 1e-9 after the full run, except
+# where the reference's own arithmetic is ill-conditioned, bounded per deck:
+#  * Noh after one cycle: the elements the shock has just reached hold
+#    1e-10 + a heating increment that nearly cancels, so their energy (and
+#    pressure) moves by a few 1e-12 of itself under any change of rounding
+#    (measured 2.0e-12 at 32^3, 4.2e-12 at 48^3);
+#  * Noh 32^3 after the full run: nodes in the stagnated core are at rest up to
+#    rounding noise far below 1e-9 of the inflow speed, and the FMA mode's
+#    noise differs from the exact mode's (measured 3.9e-9 against that floor).
+TIGHT_ONE_CYCLE = {k: 1e-12 for k in GATED}
+TIGHT_FULL = {k: 1e-9 for k in GATED}
+TIGHT_BOUNDS = {("noh32", 1): {"sie": 1e-11, "pres": 1e-11}, ("noh32", 500): {"vel": 1e-8}}
+
 
 @pytest.mark.parametrize("case", ["sedov12", "noh32", "sedov16_jp", "noh12_jp"])
 def test_fma_mode_within_tolerance(oracle_built, lib_built, case):
@@ -129,9 +145,12 @@ def test_fma_mode_within_tolerance(oracle_built, lib_built, case):
     r1 = _oracle_state(prob, cycles=1)
     assert_fields(g1, r1, 1e-12, GATED, label=case + " fma 1 cycle")
     assert_fields(g1, r1, 2e-12, ("sspd", "vol"), label=case + " fma 1 cycle")
+    assert_fields_tight(g1, r1, dict(TIGHT_ONE_CYCLE, **TIGHT_BOUNDS.get((case, 1), {})), GATED,
+                        label=case + " fma 1 cycle")
     g = _gpu_state(prob, cycles=n, mode=1)
     r = _oracle_state(prob, cycles=n)
     assert_fields(g, r, 1e-9, FIELDS, label=case + " fma full")
+    assert_fields_tight(g, r, dict(TIGHT_FULL, **TIGHT_BOUNDS.get((case, n), {})), GATED, label=case + " fma full")
 
 
 def test_fma_mode_gates_on_the_bench_mesh_family(lib_built):

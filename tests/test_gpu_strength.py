@@ -14,7 +14,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, assert_bitwise, assert_fields, load_golden
+from conftest import GOLDEN, assert_bitwise, assert_fields, assert_fields_tight, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -109,6 +109,10 @@ def test_fma_mode_within_tolerance(oracle_built, lib_built, case):
     g = _gpu(prob, cycles=prob.params.cycle_stop, mode=1)
     r = _oracle(prob, cycles=prob.params.cycle_stop)
     assert_fields(g, r, 1e-9, keys=FIELDS + ("stress",), label="fma %s" % case)
+    # the tight metric (density, pressure, energy purely relative; positions and
+    # velocities with a floor of 1e-9 of the peak) meets the same gates
+    assert_fields_tight(g1, r1, 1e-12, gated, label="fma %s 1 cycle" % case)
+    assert_fields_tight(g, r, 1e-9, gated, label="fma %s" % case)
 
 
 def test_nonzero_initial_stress_and_history(oracle_built, lib_built):

@@ -11,7 +11,7 @@ import os
 
 import pytest
 
-from conftest import GOLDEN, assert_bitwise, assert_fields, load_golden
+from conftest import GOLDEN, assert_bitwise, assert_fields, assert_fields_tight, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -88,6 +88,18 @@ def test_exact_vs_reference_golden(lib_built, name, cycles):
         assert_fields(g, ref, tol, keys=FIELDS, label="%s c%d" % (name, c))
 
 
+# The tight metric (density, pressure, energy purely relative; positions and
+# velocities with a floor of 1e-9 of the peak) meets the same gates on these
+# decks except for velocities at rest, which both codes leave as rounding noise
+# (a node's corner normals cancel under a uniform pressure only up to rounding,
+# and the FMA mode's normals round differently): bounded per deck at about
+# twice the measured value (triple point after one cycle 3.2e-9; Saltzman
+# 1.2e-5 after one cycle, 1.9e-4 after 400; the noise itself is ~1e-14 of the
+# velocity peak, as the floor-1e-3 metric shows).
+TIGHT_VEL_NOISE = {("triple_point", 1): {"vel": 1e-8}, ("sod_saltzman", 1): {"vel": 3e-5},
+                   ("sod_saltzman", 400): {"vel": 5e-4}}
+
+
 @pytest.mark.parametrize("name,cycles", CASES)
 def test_fma_mode_within_gates(lib_built, name, cycles):
     """The gated fields within 1e-12 after one cycle and 1e-9 after the full run
@@ -109,6 +121,9 @@ def test_fma_mode_within_gates(lib_built, name, cycles):
             assert_fields(g, ref, 2e-11, keys=("vel",), label="fma %s c%d (noise)" % (name, c))
         else:
             assert_fields(g, ref, tol, keys=("coords", "vel", "den", "pres", "sie"), label="fma %s c%d" % (name, c))
+        tight = {k: tol for k in ("coords", "vel", "den", "pres", "sie")}
+        tight.update(TIGHT_VEL_NOISE.get((name, c), {}))
+        assert_fields_tight(g, ref, tight, ("coords", "vel", "den", "pres", "sie"), label="fma %s c%d" % (name, c))
 
 
 @pytest.mark.parametrize("name,cycles", CASES)
