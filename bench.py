@@ -604,8 +604,9 @@ def batch_workload(n_inst: int, seed: int, cycles: int):
 
 def batch_measure(args, modes=None) -> dict:
     """Config 4: the ensemble through fierro_batch_run against looping the plain
-    solver over the same instances, in each arithmetic mode of `modes`, with the
-    clocks sampled over the timed runs."""
+    solver over the same instances, in each arithmetic mode of `modes`: the
+    default launch shape, the shape fierro_batch_autotune picks, and (first mode)
+    the instances reordered smallest first; clocks sampled over the timed runs."""
     import torch
     from fierro_gb300 import sgh
     torch.cuda.set_device(0)
@@ -618,25 +619,39 @@ def batch_measure(args, modes=None) -> dict:
                      % (n, args.batch_cycles), "unit": "instances/s", "elements_total": ne_tot,
            "config": {"workload": "ensemble", "instances": n, "cycles": args.batch_cycles, "seed": args.seed,
                       "launches_per_cycle": 8, "timing": "host wall clock around fierro_batch_run / "
-                      "fierro_sgh_run (each synchronises)"}}
+                      "fierro_sgh_run (each synchronises); the autotuner's own time is reported apart"}}
+
+    def run_batch(ps, sts, mode, tune):
+        stream = torch.cuda.Stream()
+        b = sgh.Batch(ps, fp_mode=mode, stream=stream.cuda_stream)
+        for i, st in enumerate(sts):
+            b.set_state(i, st)
+        tuned = None
+        if tune:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            chosen, log = b.autotune(cycles=3)
+            tuned = {"shape": list(chosen), "autotune_s": time.perf_counter() - t0,
+                     "candidates": [[list(sh), ms] for sh, ms in log]}
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.run(args.batch_cycles)
+        dt = time.perf_counter() - t0
+        cyc = [b.time(i)[2] for i in range(len(ps))]
+        shape = b.shape()
+        b.close()
+        return dt, cyc, shape, tuned
+
     clocks = ClockSampler(0)
     clocks.start()
-    for mname in modes:
+    for k, mname in enumerate(modes):
         mode = sgh.FP_EXACT if mname == "exact" else sgh.FP_FMA
         with sgh.Batch(probs[:2], fp_mode=mode) as w:  # load the batch kernels
             w.set_state(0, states[0])
             w.set_state(1, states[1])
             w.run(3)
-        stream = torch.cuda.Stream()
-        b = sgh.Batch(probs, fp_mode=mode, stream=stream.cuda_stream)
-        for i, st in enumerate(states):
-            b.set_state(i, st)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        b.run(args.batch_cycles)
-        t_batch = time.perf_counter() - t0
-        cycles_done = [b.time(i)[2] for i in range(n)]
-        b.close()
+        t_batch, cycles_done, shape, _ = run_batch(probs, states, mode, False)
+        t_tuned, _, shape_t, tuned = run_batch(probs, states, mode, True)
         # the same instances one after another through the single-problem solver
         t_loop = 0.0
         for p, st in zip(probs, states):
@@ -646,10 +661,18 @@ def batch_measure(args, modes=None) -> dict:
                 t1 = time.perf_counter()
                 s1.run(args.batch_cycles)
                 t_loop += time.perf_counter() - t1
-        out[mname] = {"value": n / t_batch, "loop_value": n / t_loop, "speedup_vs_loop": t_loop / t_batch,
-                      "batch_seconds": t_batch, "loop_seconds": t_loop,
-                      "element_cycles_per_s": sum(p.mesh.num_elems * c for p, c in zip(probs, cycles_done)) / t_batch,
-                      "instances_stopped_early": int(sum(c < args.batch_cycles for c in cycles_done))}
+        r = {"value": n / t_batch, "loop_value": n / t_loop, "speedup_vs_loop": t_loop / t_batch,
+             "batch_seconds": t_batch, "loop_seconds": t_loop, "shape": list(shape),
+             "element_cycles_per_s": sum(p.mesh.num_elems * c for p, c in zip(probs, cycles_done)) / t_batch,
+             "instances_stopped_early": int(sum(c < args.batch_cycles for c in cycles_done)),
+             "tuned": dict(tuned, value=n / t_tuned, batch_seconds=t_tuned,
+                           speedup_vs_loop=t_loop / t_tuned, gain_vs_default=t_batch / t_tuned)}
+        if k == 0:
+            order = sorted(range(n), key=lambda i: probs[i].mesh.num_elems)
+            t_sorted, _, _, _ = run_batch([probs[i] for i in order], [states[i] for i in order], mode, False)
+            r["smallest_first"] = {"value": n / t_sorted, "batch_seconds": t_sorted,
+                                   "gain_vs_default": t_batch / t_sorted}
+        out[mname] = r
     out["clocks"] = clocks.stop()
     return out
 
@@ -709,23 +732,33 @@ def adjoint_measure(args, compact: bool = False) -> dict:
         t_bwd.append(time.perf_counter() - t0)
     tp, tf, tb = min(t_plain), min(t_fwd), min(t_bwd)
     # the frozen-branch check: central differences (step 1e-6) of the forward
-    # with the base run's switch decisions held, along the seeded directions
+    # with the base run's switch decisions held, along the seeded directions;
+    # the three-point difference carries a truncation error h^2 J3 / 6 (J3 the
+    # third derivative along the direction), the five-point one (same step, two
+    # more forwards) O(h^4)
     Jf, sbf, gbf, _ = dm.gradient_frozen()
     frozen = []
     for d_sie, d_g in dm.directions(args.adj_dirs, seed=args.seed):
         ad = float(np.dot(sbf, d_sie) + np.sum(gbf) * d_g)
-        fd = dm.fd(d_sie, d_g, h=1e-6)
-        frozen.append({"ad": ad, "fd": fd, "rel": abs(fd - ad) / abs(fd)})
+        fd3, fd5 = dm.fd5(d_sie, d_g, h=1e-6)
+        frozen.append({"ad": ad, "fd3": fd3, "fd5": fd5, "rel3": abs(fd3 - ad) / abs(fd3),
+                       "rel5": abs(fd5 - ad) / abs(fd5)})
     dm.unfreeze()
-    relf = np.array([d["rel"] for d in frozen]) if frozen else np.zeros(0)
-    fd_frozen = {"directions": len(frozen), "step": 1e-6,
-                 "max_rel": float(relf.max()) if relf.size else None,
-                 "median_rel": float(np.median(relf)) if relf.size else None,
-                 "within_1e-6": int((relf <= 1e-6).sum()),
+    rel3 = np.array([d["rel3"] for d in frozen]) if frozen else np.zeros(0)
+    rel5 = np.array([d["rel5"] for d in frozen]) if frozen else np.zeros(0)
+
+    def summary(rel):
+        return {"max_rel": float(rel.max()) if rel.size else None,
+                "median_rel": float(np.median(rel)) if rel.size else None,
+                "within_1e-6": int((rel <= 1e-6).sum())}
+
+    fd_frozen = {"directions": len(frozen), "step": 1e-6, "five_point": summary(rel5),
+                 "three_point": summary(rel3),
                  "gradient_equals_plain": bool(np.array_equal(sbf, sb) and np.array_equal(gbf, gb)),
-                 "what": "central differences of the frozen-branch forward (fierro_adj_branches FREEZE: the "
-                         "limiter neighbour and clamps, Mach switch, compression sign, Riemann-velocity guard, "
-                         "CFL element and node pair, dt growth cap and clamps held at the base run's decisions)"}
+                 "what": "central differences at step 1e-6 (three-point and five-point stencils) of the "
+                         "frozen-branch forward (fierro_adj_branches FREEZE: the limiter neighbour and clamps, Mach "
+                         "switch, compression sign and |div| sign, Riemann-velocity guard, CFL element and node "
+                         "pair, dt growth cap and clamps held at the base run's decisions)"}
     if not compact:
         fd_frozen["per_direction"] = frozen
     dirs = []

@@ -147,6 +147,19 @@ class DensityMismatch:
         jm = f(self.sie0 - h * d_sie, self.gamma0 - h * d_gamma)
         return (jp - jm) / (2.0 * h)
 
+    def fd5(self, d_sie: np.ndarray, d_gamma: float, h: float = 1e-6, forward=None):
+        """Central differences of J along (d_sie, d_gamma) at step h from the
+        four values J(x + k h d), k = -2, -1, 1, 2: the three-point difference
+        (J(h) - J(-h)) / 2h, whose error is h^2 J3 / 6 (J3 the third derivative
+        along the direction), and the five-point one
+        (8 (J(h) - J(-h)) - (J(2h) - J(-2h))) / 12h, whose error is O(h^4).
+        Returns (three_point, five_point)."""
+        f = forward or self.forward
+        j = {k: f(self.sie0 + k * h * d_sie, self.gamma0 + k * h * d_gamma) for k in (-2, -1, 1, 2)}
+        d1 = j[1] - j[-1]
+        d2 = j[2] - j[-2]
+        return d1 / (2.0 * h), (8.0 * d1 - d2) / (12.0 * h)
+
     def fd_consistent(self, d_sie: np.ndarray, d_gamma: float, steps=(1e-5, 1e-6, 1e-7, 1e-8), forward=None):
         """Central differences at several steps; returns (estimate, step, spread,
         table).  J is piecewise smooth (the forward's switches: limiter, Mach

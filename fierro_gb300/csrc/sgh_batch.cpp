@@ -72,6 +72,11 @@ struct fierro_batch {
   double* h_stage = nullptr;
   size_t stage_elems = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  // launch shape of the cycle kernels (fierro_batch_set_shape / fierro_batch_autotune)
+  fierro_batch_shape shape{kForceBlock, kNodeBlock, kElemBlock, 0};
+  int sm_count = 0;
+  std::vector<fierro_batch_shape> tune_shapes;
+  std::vector<double> tune_ms;
 };
 
 namespace {
@@ -137,6 +142,8 @@ ForceArgs b_force(fierro_batch* b, int rb, int q) {
   a.inst = b->d_inst_e;
   a.fuzz = b->fuzz;
   a.small = b->small;
+  a.block = b->shape.force_block;
+  a.grid = b->shape.persistent ? b->sm_count * b->shape.persistent : 0;
   return a;
 }
 
@@ -167,6 +174,8 @@ NodeArgs b_node(fierro_batch* b, int c, double alpha) {
   a.ctrl = b->d_ctrl;
   a.inst = b->d_inst_n;
   a.rk_alpha = alpha;
+  a.block = b->shape.node_block;
+  a.grid = b->shape.persistent ? b->sm_count * b->shape.persistent : 0;
   return a;
 }
 
@@ -201,6 +210,8 @@ ElemArgs b_elem(fierro_batch* b, int cur_bin, int c, double alpha, int div_out) 
   a.dt_cfl_tab = b->d_dt_cfl;
   a.rk_alpha = alpha;
   a.fuzz = b->fuzz;
+  a.block = b->shape.elem_block;
+  a.grid = b->shape.persistent ? b->sm_count * b->shape.persistent : 0;
   return a;
 }
 
@@ -223,6 +234,42 @@ void b_cycle(fierro_batch* b, int c) {
     b->ks->elem(b_elem(b, c ^ 1, c, alpha, q ^ 1), (s == S - 1) ? 1 : 0, b->stream);
   }
   b->ks->end_batch(b->d_ctrl, b->d_lps, (int)b->n, b->stream);
+}
+
+constexpr int kMinBatchBlock = 32;
+
+bool shape_valid(const fierro_batch_shape& sh) {
+  auto ok = [](int b, int hi) { return b >= kMinBatchBlock && b <= hi && (b & (b - 1)) == 0; };
+  return ok(sh.force_block, kForceBlock) && ok(sh.node_block, 1024) && ok(sh.elem_block, kElemBlock) &&
+         sh.persistent >= 0 && sh.persistent <= 64;
+}
+
+// Makes `sh` the batch's launch shape: the per-instance CFL partial ranges in
+// tiles of sh.elem_block elements, and the two per-parity cycle graphs.
+int apply_shape(fierro_batch* b, const fierro_batch_shape& sh) {
+  if (!shape_valid(sh))
+    return set_error(FIERRO_EINVAL, "batch shape: blocks must be powers of two, force 32..%d, node 32..1024, "
+                     "element 32..%d, persistent 0..64 blocks per SM", kForceBlock, kElemBlock);
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  b->shape = sh;
+  for (size_t i = 0; i < b->part_start.size(); ++i)
+    b->part_start[i] = (int)(b->elem_off[i] / sh.elem_block);
+  b->nparts = b->part_start.back();
+  TRY(put(b, b->d_part_start, b->part_start));
+  for (int c = 0; c < 2; ++c) {
+    if (b->graph[c]) {
+      cudaGraphExecDestroy(b->graph[c]);
+      b->graph[c] = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    b_cycle(b, c);
+    CUDA_TRY(cudaStreamEndCapture(b->stream, &g));
+    cudaError_t err = cudaGraphInstantiate(&b->graph[c], g, 0);
+    cudaGraphDestroy(g);
+    if (err != cudaSuccess) return set_error(FIERRO_ECUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(err));
+  }
+  return FIERRO_OK;
 }
 
 int create_impl(fierro_batch* b, const fierro_batch_instance* inst, int64_t n, int fp_mode, void* stream) {
@@ -266,7 +313,7 @@ int create_impl(fierro_batch* b, const fierro_batch_instance* inst, int64_t n, i
     b->node_off[i + 1] = b->node_off[i] + I.mesh.num_nodes;
     b->elem_off[i + 1] = b->elem_off[i] + ne_pad;
     b->mat_off[i + 1] = b->mat_off[i] + I.num_materials;
-    b->part_start[i + 1] = (int)(b->elem_off[i + 1] / kElemBlock);
+    b->part_start[i + 1] = (int)(b->elem_off[i + 1] / kElemBlock);  // per default block; see apply_shape
     b->lps[i] = LoopParams{p.time_final, p.dt_max, p.dt_min, p.dt_cfl, p.graphics_dt_ival, p.fuzz, p.small,
                            p.graphics_cyc_ival};
     b->dt_start[i] = p.dt_start;
@@ -348,7 +395,7 @@ int create_impl(fierro_batch* b, const fierro_batch_instance* inst, int64_t n, i
   TRY(balloc(b, &b->d_sie[1], (size_t)NE));
   TRY(balloc(b, &b->d_bmat, (size_t)NE * 24));
   TRY(balloc(b, &b->d_force, (size_t)NE * 24));
-  TRY(balloc(b, &b->d_cfl, (size_t)b->nparts));
+  TRY(balloc(b, &b->d_cfl, (size_t)(NE / kMinBatchBlock)));  // one partial per tile of the smallest block
   TRY(balloc(b, &b->d_ctrl, (size_t)n));
   TRY(put(b, b->d_nie, nie));
   TRY(put(b, b->d_cin_start, cin_start));
@@ -375,15 +422,10 @@ int create_impl(fierro_batch* b, const fierro_batch_instance* inst, int64_t n, i
     stage = std::max<size_t>(stage, (size_t)std::max(inst[i].mesh.num_nodes, inst[i].mesh.num_elems));
   b->stage_elems = stage;
   CUDA_TRY(cudaHostAlloc((void**)&b->h_stage, sizeof(double) * stage, cudaHostAllocDefault));
-  for (int c = 0; c < 2; ++c) {
-    cudaGraph_t g = nullptr;
-    CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-    b_cycle(b, c);
-    CUDA_TRY(cudaStreamEndCapture(b->stream, &g));
-    cudaError_t err = cudaGraphInstantiate(&b->graph[c], g, 0);
-    cudaGraphDestroy(g);
-    if (err != cudaSuccess) return set_error(FIERRO_ECUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(err));
-  }
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  CUDA_TRY(cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev));
+  TRY(apply_shape(b, b->shape));
   CUDA_TRY(cudaStreamSynchronize(b->stream));
   return FIERRO_OK;
 }
@@ -545,6 +587,166 @@ extern "C" int fierro_batch_get_state(fierro_batch* b, int64_t i, fierro_sgh_sta
   if (s->corner_force)
     for (int r = 0; r < 24; ++r)
       TRY(scatter_down(b, s->corner_force, b->d_force + (size_t)r * b->NE, eo, t.elem_int2ext, 24, (size_t)r));
+  return FIERRO_OK;
+}
+
+extern "C" int fierro_batch_set_shape(fierro_batch* b, const fierro_batch_shape* shape) {
+  clear_error();
+  if (!b || !shape) return set_error(FIERRO_EINVAL, "batch or shape is NULL");
+  if (b->started) return set_error(FIERRO_EINVAL, "batch: the launch shape is fixed once the batch has run");
+  return apply_shape(b, *shape);
+}
+
+extern "C" int fierro_batch_get_shape(const fierro_batch* b, fierro_batch_shape* shape) {
+  clear_error();
+  if (!b || !shape) return set_error(FIERRO_EINVAL, "batch or shape is NULL");
+  *shape = b->shape;
+  return FIERRO_OK;
+}
+
+namespace {
+
+// The cycle-mutable device arrays of a batch (everything a cycle writes except
+// the CFL partials, which the priming pass rewrites), for the autotuner's
+// save / restore around each timed candidate.
+std::vector<std::pair<void*, size_t>> mutable_arrays(fierro_batch* b) {
+  const size_t nn = sizeof(double) * (size_t)b->NN, ne = sizeof(double) * (size_t)b->NE;
+  std::vector<std::pair<void*, size_t>> v;
+  for (int k = 0; k < 2; ++k)
+    for (int d = 0; d < 3; ++d) {
+      v.push_back({b->d_x[k][d], nn});
+      v.push_back({b->d_v[k][d], nn});
+    }
+  for (int d = 0; d < 3; ++d) v.push_back({b->d_h[d], nn});
+  for (double* p : {b->d_sie[0], b->d_sie[1], b->d_den, b->d_pres, b->d_sspd, b->d_vol, b->d_div[0], b->d_div[1]})
+    v.push_back({p, ne});
+  v.push_back({b->d_bmat, 24 * ne});
+  v.push_back({b->d_force, 24 * ne});
+  v.push_back({b->d_ctrl, sizeof(Ctrl) * (size_t)b->n});
+  return v;
+}
+
+int copy_arrays(fierro_batch* b, char* save, const std::vector<std::pair<void*, size_t>>& arrs, bool to_save) {
+  size_t off = 0;
+  for (const auto& a : arrs) {
+    CUDA_TRY(cudaMemcpyAsync(to_save ? save + off : a.first, to_save ? a.first : save + off, a.second,
+                             cudaMemcpyDeviceToDevice, b->stream));
+    off += a.second;
+  }
+  return FIERRO_OK;
+}
+
+// Primes the uploaded state with the current shape, runs `warm` cycles, then
+// times `cycles` cycles of the captured graphs; ms per cycle.
+int time_shape(fierro_batch* b, int warm, int cycles, double* ms) {
+  b->ks->elem(b_elem(b, 0, 0, 1.0, 0), 2, b->stream);
+  CUDA_TRY(cudaGetLastError());
+  long long k = 0;
+  for (; k < warm; ++k) CUDA_TRY(cudaGraphLaunch(b->graph[k & 1], b->stream));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  cudaError_t err = cudaEventRecord(e0, b->stream);
+  for (long long i = 0; i < cycles && err == cudaSuccess; ++i, ++k) err = cudaGraphLaunch(b->graph[k & 1], b->stream);
+  if (err == cudaSuccess) err = cudaEventRecord(e1, b->stream);
+  if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+  float t = 0.0f;
+  if (err == cudaSuccess) err = cudaEventElapsedTime(&t, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (err != cudaSuccess) return set_error(FIERRO_ECUDA, "batch autotune: %s", cudaGetErrorString(err));
+  *ms = (double)t / std::max(cycles, 1);
+  return FIERRO_OK;
+}
+
+}  // namespace
+
+extern "C" int fierro_batch_autotune(fierro_batch* b, int64_t cycles, fierro_batch_shape* chosen) {
+  clear_error();
+  NvtxRange nvtx_("fierro_batch_autotune");
+  if (!b) return set_error(FIERRO_EINVAL, "batch is NULL");
+  if (b->started) return set_error(FIERRO_EINVAL, "batch: autotune before the first fierro_batch_run");
+  if (cycles < 1 || cycles > 1000) return set_error(FIERRO_EINVAL, "batch autotune: cycles must be 1..1000");
+  for (int64_t i = 0; i < b->n; ++i)
+    if (!b->has_state[i]) return set_error(FIERRO_EINVAL, "batch: instance %lld has no state", (long long)i);
+  const auto arrs = mutable_arrays(b);
+  size_t total = 0;
+  for (const auto& a : arrs) total += a.second;
+  char* save = nullptr;
+  CUDA_TRY(cudaMalloc(&save, total));
+  b->tune_shapes.clear();
+  b->tune_ms.clear();
+  int rc = copy_arrays(b, save, arrs, true);
+  fierro_batch_shape best = b->shape;
+  double best_ms = 0.0;
+  bool have = false;
+  // coordinate descent: force block, node block, element block, persistent grid
+  auto trial = [&](fierro_batch_shape sh) -> int {
+    for (size_t i = 0; i < b->tune_shapes.size(); ++i) {
+      const fierro_batch_shape& o = b->tune_shapes[i];
+      if (o.force_block == sh.force_block && o.node_block == sh.node_block && o.elem_block == sh.elem_block &&
+          o.persistent == sh.persistent)
+        return FIERRO_OK;
+    }
+    TRY(copy_arrays(b, save, arrs, false));
+    TRY(apply_shape(b, sh));
+    double ms = 0.0;
+    TRY(time_shape(b, 1, (int)cycles, &ms));
+    b->tune_shapes.push_back(sh);
+    b->tune_ms.push_back(ms);
+    if (!have || ms < best_ms) {
+      best = sh;
+      best_ms = ms;
+      have = true;
+    }
+    return FIERRO_OK;
+  };
+  const int force_blocks[] = {128, 64, 32}, node_blocks[] = {256, 128, 512, 64}, elem_blocks[] = {128, 64, 32};
+  const int persist[] = {0, 1, 2, 4};
+  for (int fb : force_blocks) {
+    if (rc) break;
+    fierro_batch_shape sh = best;
+    sh.force_block = fb;
+    rc = trial(sh);
+  }
+  for (int nb : node_blocks) {
+    if (rc) break;
+    fierro_batch_shape sh = best;
+    sh.node_block = nb;
+    rc = trial(sh);
+  }
+  for (int eb : elem_blocks) {
+    if (rc) break;
+    fierro_batch_shape sh = best;
+    sh.elem_block = eb;
+    rc = trial(sh);
+  }
+  for (int p : persist) {
+    if (rc) break;
+    fierro_batch_shape sh = best;
+    sh.persistent = p;
+    rc = trial(sh);
+  }
+  // the uploaded state back, with the chosen shape
+  if (!rc) rc = copy_arrays(b, save, arrs, false);
+  cudaStreamSynchronize(b->stream);
+  cudaFree(save);
+  if (rc) return rc;
+  TRY(apply_shape(b, best));
+  if (chosen) *chosen = best;
+  return FIERRO_OK;
+}
+
+extern "C" int fierro_batch_tune_log(const fierro_batch* b, fierro_batch_shape* shapes, double* ms_per_cycle,
+                                     int64_t capacity, int64_t* count) {
+  clear_error();
+  if (!b || !count) return set_error(FIERRO_EINVAL, "batch or count is NULL");
+  const int64_t n = (int64_t)b->tune_shapes.size();
+  *count = n;
+  for (int64_t i = 0; i < n && i < capacity; ++i) {
+    if (shapes) shapes[i] = b->tune_shapes[(size_t)i];
+    if (ms_per_cycle) ms_per_cycle[i] = b->tune_ms[(size_t)i];
+  }
   return FIERRO_OK;
 }
 

@@ -82,6 +82,7 @@ struct ForceArgs {
   double rk_alpha;
   int copy_stress;     // stage 0: elements without a hypo model carry stress_cur over
   int block;           // threads per block (0: kForceBlock)
+  int grid;            // batch only: blocks of a persistent grid (0: one block per tile)
 };
 
 // Branch bits of one element's corner force in one stage, recorded on a base
@@ -114,6 +115,7 @@ struct NodeArgs {
   const int* inst;  // batch only: instance of each node
   double rk_alpha;
   int block;        // threads per block (0: kNodeBlock)
+  int grid;         // batch only: blocks of a persistent grid (0: one block per node tile)
 };
 
 // kind: 0 = stage update, 1 = last stage of a cycle (adds the CFL partial
@@ -143,7 +145,9 @@ struct ElemArgs {
   const double* stress0;  // cycle-start stress(0)
   double* stress1;        // stress(1), updated in place
   double* statev;         // [nsv][ne]
-  int block;              // threads per block, one CFL partial per block (0: kElemBlock; a batch always uses it)
+  int block;              // threads per block, one CFL partial per tile of that many elements (0: kElemBlock;
+                          // a batch's block divides kElemBlock)
+  int grid;               // batch only: blocks of a persistent grid looping over the tiles (0: one per tile)
 };
 
 struct DtArgs {

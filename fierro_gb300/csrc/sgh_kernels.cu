@@ -6,11 +6,14 @@
 //       the reference's order (Explicit-Lagrange-Kokkos/SGH_solver), with IEEE
 //       division and square root, so results match its uncontracted evaluation;
 //   FIERRO_FMA=1 with --fmad=true  -> fierro::fma_impl: the same schedule, the
-//       compiler free to fuse multiply-adds, and the per-node division by mass
-//       done through one reciprocal -- except where the reference's sums cancel
-//       (the hex volume, the element power, the Riemann velocity), which stay
-//       separately rounded (FX_MUL / FX_ADD) so this mode keeps within 1e-12 of
-//       the reference after one cycle and 1e-9 after a full run.
+//       compiler free to fuse multiply-adds, the per-node division by mass
+//       done through one reciprocal, and square and
+//       cube roots by Newton iterations from single-precision seeds (within an
+//       ulp; mode_sqrt / mode_cbrt in sgh_common.cuh) -- except where the
+//       reference's sums cancel (the hex volume, the element power, the Riemann
+//       velocity), which stay separately rounded (FX_MUL / FX_ADD) so this mode
+//       keeps within 1e-12 of the reference after one cycle and 1e-9 after a
+//       full run.
 //
 // One cycle is 2 + 3*rk_num_stages launches:
 //   k_dt                    CFL minimum over the last stage's per-block partials,
@@ -43,6 +46,21 @@
 #define FIERRO_IMPL fma_impl
 #else
 #define FIERRO_IMPL exact_impl
+#endif
+
+// Launch bounds of the force and element kernels.  FIERRO_FORCE_MIN_BLOCKS /
+// FIERRO_ELEM_MIN_BLOCKS, when defined, ask the compiler for that many resident
+// blocks per SM (a register budget of 65536 / (blocks x 128 threads)); undefined,
+// the register count is the compiler's own choice.
+#ifdef FIERRO_FORCE_MIN_BLOCKS
+#define FIERRO_FORCE_BOUNDS __launch_bounds__(kForceBlock, FIERRO_FORCE_MIN_BLOCKS)
+#else
+#define FIERRO_FORCE_BOUNDS __launch_bounds__(kForceBlock)
+#endif
+#ifdef FIERRO_ELEM_MIN_BLOCKS
+#define FIERRO_ELEM_BOUNDS __launch_bounds__(kElemBlock, FIERRO_ELEM_MIN_BLOCKS)
+#else
+#define FIERRO_ELEM_BOUNDS __launch_bounds__(kElemBlock)
 #endif
 
 namespace fierro {
@@ -89,11 +107,8 @@ __device__ __forceinline__ void velocity_gradient(const double (&u)[8], const do
 // velocity, limiter case and neighbour, Mach clamp) without changing any value;
 // BR = 2 takes them from the record instead of deciding them, so the force is a
 // smooth function of the state along the recorded trajectory's branches.
-template <bool BATCH, bool TAPE, bool STRENGTH, int BR = 0>
-__global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
-  if (!BATCH && !a.ctrl->active) return;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= a.ne) return;
+template <bool BATCH, bool TAPE, bool STRENGTH, int BR>
+__device__ __forceinline__ void force_elem(const ForceArgs& a, const int e) {
   if (BATCH && (a.inst[e] < 0 || !a.ctrl[a.inst[e]].active)) return;
   const int ne = a.ne;
   const int4 n03 = __ldg(reinterpret_cast<const int4*>(a.nie) + 2 * e);
@@ -130,12 +145,12 @@ __global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
 #pragma unroll
   for (int l = 0; l < 8; ++l) {
     const double d0 = vu[l] - vs0, d1 = vv[l] - vs1, d2 = vw[l] - vs2;
-    const double mag_vel = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    const double mag_vel = mode_sqrt(d0 * d0 + d1 * d1 + d2 * d2);
     const double muc = den * (q1c + qb * mag_vel);
     const double b0 = a.bmat[(size_t)(l * 3 + 0) * ne + e];
     const double b1 = a.bmat[(size_t)(l * 3 + 1) * ne + e];
     const double b2 = a.bmat[(size_t)(l * 3 + 2) * ne + e];
-    const double mu_term = muc * sqrt(b0 * b0 + b1 * b1 + b2 * b2);
+    const double mu_term = muc * mode_sqrt(b0 * b0 + b1 * b1 + b2 * b2);
     // the Riemann velocity's sums stay separately rounded in both modes: the
     // force's (v* - v) and then the element power cancel, and a contracted v*
     // would move a cold element's energy by ~1e-12 relative after one cycle
@@ -165,10 +180,9 @@ __global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
     kmax = key > kmax ? key : kmax;
   }
   double r_min = 1.0;
-  bool regular = true;
   if (k1 > k0) {
     const double dsel = okey_decode(D > 0 ? kmin : kmax);
-    regular = isfinite(D) && D != 0.0 && isfinite(dsel);
+    const bool regular = isfinite(D) && D != 0.0 && isfinite(dsel);
     if (regular) {
       const double r_face = 0.9 * (dsel + small) / D;
       r_min = okey(r_face) < okey(1.0) ? r_face : 1.0;
@@ -182,12 +196,15 @@ __global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
   double phi = 1.0 - fmax(0.0, r_min);  // pow(phi, 1.0) == phi
   // Mach-number detector (:318-328)
   const double c_length = pow_third(vol);
-  const double araw = 20.0 * (c_length * fabs(div)) / (sspd + a.fuzz);
-  double alpha = fmin(1.0, araw);
+  // |div|: on the frozen trajectory, the sign recorded with the compression bit
+  const double adiv = BR == 2 ? (compress ? -div : div) : fabs(div);
+  const double araw = 20.0 * (c_length * adiv) / (sspd + a.fuzz);
+  const double alpha = BR == 2 ? ((br & FIERRO_BR_MACH_CLAMP) ? 1.0 : araw) : fmin(1.0, araw);
   if (BR == 1) {
     // the limiter's case, and the neighbour that set r_min on the r_face branch
     unsigned lim = FIERRO_LIM_NONE;
     int sel = -1;
+    const bool regular = isfinite(D) && D != 0.0 && isfinite(okey_decode(D > 0 ? kmin : kmax));
     if (k1 > k0 && !regular) {
       lim = FIERRO_LIM_IRREGULAR;
     } else if (r_min < 1.0 && r_min > 0.0) {
@@ -216,7 +233,6 @@ __global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
     } else if (lim == FIERRO_LIM_FACE && a.br_sel[e] >= 0) {
       phi = 1.0 - 0.9 * (__ldg(a.div + a.br_sel[e]) + small) / D;
     }  // FIERRO_LIM_IRREGULAR: as evaluated above
-    alpha = (br & FIERRO_BR_MACH_CLAMP) ? 1.0 : araw;
   }
   if (TAPE) {
     double* t = a.tape + e;
@@ -224,7 +240,7 @@ __global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
     for (int l = 0; l < 8; ++l) {
       const double d0 = vu[l] - vs0, d1 = vv[l] - vs1, d2 = vw[l] - vs2;
       t[(size_t)l * ne] = mu[l];
-      t[(size_t)(8 + l) * ne] = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+      t[(size_t)(8 + l) * ne] = mode_sqrt(d0 * d0 + d1 * d1 + d2 * d2);
     }
     t[(size_t)16 * ne] = vstar0;
     t[(size_t)17 * ne] = vstar1;
@@ -303,14 +319,26 @@ __global__ void __launch_bounds__(kForceBlock) k_force(const ForceArgs a) {
   }
 }
 
+// One thread per element; a batch may run as a persistent grid (a.grid blocks)
+// that strides over the elements.
+template <bool BATCH, bool TAPE, bool STRENGTH, int BR = 0>
+__global__ void FIERRO_FORCE_BOUNDS k_force(const ForceArgs a) {
+  if (BATCH) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < a.ne; e += gridDim.x * blockDim.x)
+      force_elem<true, TAPE, STRENGTH, BR>(a, e);
+  } else {
+    if (!a.ctrl->active) return;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= a.ne) return;
+    force_elem<false, TAPE, STRENGTH, BR>(a, e);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Node update: corner-force gather in the reference's summation order, velocity,
 // boundary conditions, half velocity and position.
 template <bool BATCH>
-__global__ void __launch_bounds__(kNodeBlock) k_node(const NodeArgs a) {
-  if (!BATCH && !a.ctrl->active) return;
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= a.nn) return;
+__device__ __forceinline__ void node_update(const NodeArgs& a, const int n) {
   const Ctrl* ctrl = BATCH ? a.ctrl + a.inst[n] : a.ctrl;
   if (BATCH && !ctrl->active) return;
   const size_t ne = (size_t)a.ne;
@@ -367,19 +395,34 @@ __global__ void __launch_bounds__(kNodeBlock) k_node(const NodeArgs a) {
   a.z1[n] = a.z0[n] + adt * hw;
 }
 
+// One thread per node; a batch may run as a persistent grid striding over the nodes.
+template <bool BATCH>
+__global__ void __launch_bounds__(kNodeBlock) k_node(const NodeArgs a) {
+  if (BATCH) {
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < a.nn; n += gridDim.x * blockDim.x)
+      node_update<true>(a, n);
+  } else {
+    if (!a.ctrl->active) return;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.nn) return;
+    node_update<false>(a, n);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Element update.  KIND 0: stage; 1: last stage (adds the CFL partials);
 // 2: prime (corner normals, divergence and CFL of an uploaded state).
 // STRENGTH (a handle with a hyper material) runs the hyper model between the
 // density and the EOS (properties.cpp:46-95) with the velocity gradient of the
 // updated state.
-// In a batch every block lies inside one instance (instances' element ranges are
-// padded to whole blocks, padding marked by a negative instance id), so the
-// activity test and the CFL partial are per block.
+// A tile is one block's worth of elements, with one CFL partial.  In a batch
+// every tile lies inside one instance (instances' element ranges are padded to
+// whole default blocks, padding marked by a negative instance id, and the block
+// divides the default), so the activity test and the CFL partial are per tile.
 template <int KIND, bool BATCH, bool STRENGTH>
-__global__ void __launch_bounds__(kElemBlock) k_elem(const ElemArgs a) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  const int ib = BATCH ? a.inst[blockIdx.x * kElemBlock] : 0;
+__device__ __forceinline__ void elem_tile(const ElemArgs& a, const int tile) {
+  const int e = tile * blockDim.x + threadIdx.x;
+  const int ib = BATCH ? a.inst[tile * blockDim.x] : 0;
   Ctrl* ctrl = a.ctrl + ib;
   if (KIND != 2 && !ctrl->active) return;
   const bool live = e < a.ne && (!BATCH || a.inst[e] >= 0);
@@ -449,7 +492,7 @@ __global__ void __launch_bounds__(kElemBlock) k_elem(const ElemArgs a) {
       }
       const double gamma = a.gamma[e], csmin = a.csmin[e];
       const double pres = (gamma - 1.0) * sie1 * den;
-      sspd = sqrt(gamma * (gamma - 1.0) * sie1);
+      sspd = mode_sqrt(gamma * (gamma - 1.0) * sie1);
       if (sspd < csmin) sspd = csmin;
       a.den[e] = den;
       a.pres[e] = pres;
@@ -473,14 +516,29 @@ __global__ void __launch_bounds__(kElemBlock) k_elem(const ElemArgs a) {
       }
       const double d2min = cfl::min_d2(x, y, z, &s_xyz[0][threadIdx.x], &s_xyz[8][threadIdx.x],
                                        &s_xyz[16][threadIdx.x], kElemBlock);
-      const double dist_min = sqrt(d2min);
+      const double dist_min = mode_sqrt(d2min);
       const double dt_l = dt_cfl * dist_min / (sspd + a.fuzz);
       dkey = isnan(dt_l) ? 0x7FFFFFFFFFFFFFFFLL : okey(dt_l);
     }
   }
   if (KIND != 0) {
     const long long k = block_min_key(dkey);
-    if (threadIdx.x == 0) a.cfl_part[blockIdx.x] = k;
+    if (threadIdx.x == 0) a.cfl_part[tile] = k;
+  }
+}
+
+// One tile per block; a batch may run as a persistent grid looping over the
+// tiles (a barrier between tiles, as the CFL reduction reuses shared memory).
+template <int KIND, bool BATCH, bool STRENGTH>
+__global__ void FIERRO_ELEM_BOUNDS k_elem(const ElemArgs a) {
+  if (BATCH) {
+    const int ntiles = (a.ne + blockDim.x - 1) / blockDim.x;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      elem_tile<KIND, true, STRENGTH>(a, t);
+      __syncthreads();
+    }
+  } else {
+    elem_tile<KIND, false, STRENGTH>(a, blockIdx.x);
   }
 }
 
@@ -600,10 +658,15 @@ static unsigned blocks_for(long long n, int bs) { return (unsigned)((n + bs - 1)
 // as its instances' element ranges are padded to whole default blocks.
 static int block_or(int b, int def) { return (b >= 32 && b <= def && b % 32 == 0) ? b : def; }
 
+// A batch's persistent grid (a.grid > 0 blocks) never exceeds one block per tile.
+static unsigned grid_or(int grid, unsigned blocks) {
+  return (grid > 0 && (unsigned)grid < blocks) ? (unsigned)grid : blocks;
+}
+
 static void launch_force(const ForceArgs& a, cudaStream_t s) {
-  const int bs = a.inst ? kForceBlock : block_or(a.block, kForceBlock);
+  const int bs = block_or(a.block, kForceBlock);
   const unsigned g = blocks_for(a.ne, bs);
-  if (a.inst) k_force<true, false, false><<<g, bs, 0, s>>>(a);
+  if (a.inst) k_force<true, false, false><<<grid_or(a.grid, g), bs, 0, s>>>(a);
   else if (a.stress_out) k_force<false, false, true><<<g, bs, 0, s>>>(a);
   else k_force<false, false, false><<<g, bs, 0, s>>>(a);
 }
@@ -617,14 +680,14 @@ static void launch_force_branch(const ForceArgs& a, int mode, cudaStream_t s) {
   else k_force<false, false, false, 2><<<blocks_for(a.ne, bs), bs, 0, s>>>(a);
 }
 static void launch_node(const NodeArgs& a, cudaStream_t s) {
-  const int bs = a.inst ? kNodeBlock : block_or(a.block, kNodeBlock);
-  if (a.inst) k_node<true><<<blocks_for(a.nn, bs), bs, 0, s>>>(a);
+  const int bs = block_or(a.block, kNodeBlock);
+  if (a.inst) k_node<true><<<grid_or(a.grid, blocks_for(a.nn, bs)), bs, 0, s>>>(a);
   else k_node<false><<<blocks_for(a.nn, bs), bs, 0, s>>>(a);
 }
 template <bool B, bool S>
 static void launch_elem_t(const ElemArgs& a, int kind, cudaStream_t s) {
-  const int bs = B ? kElemBlock : block_or(a.block, kElemBlock);
-  const unsigned g = blocks_for(a.ne, bs);
+  const int bs = block_or(a.block, kElemBlock);
+  const unsigned g = B ? grid_or(a.grid, blocks_for(a.ne, bs)) : blocks_for(a.ne, bs);
   if (kind == 0) k_elem<0, B, S><<<g, bs, 0, s>>>(a);
   else if (kind == 1) k_elem<1, B, S><<<g, bs, 0, s>>>(a);
   else k_elem<2, B, false><<<g, bs, 0, s>>>(a);

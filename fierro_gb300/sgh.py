@@ -108,6 +108,10 @@ def _load():
     lib.fierro_batch_num_instances.restype = i64
     lib.fierro_batch_device_bytes.argtypes = [vp]
     lib.fierro_batch_device_bytes.restype = i64
+    lib.fierro_batch_set_shape.argtypes = [vp, vp]
+    lib.fierro_batch_get_shape.argtypes = [vp, vp]
+    lib.fierro_batch_autotune.argtypes = [vp, i64, vp]
+    lib.fierro_batch_tune_log.argtypes = [vp, vp, vp, i64, C.POINTER(i64)]
     lib.fierro_sgh_device_view.argtypes = [vp, vp]
     lib.fierro_sgh_set_output.argtypes = [vp, C.c_char_p, C.c_int, C.c_int]
     lib.fierro_sgh_flush_output.argtypes = [vp, C.POINTER(i64)]
@@ -478,6 +482,14 @@ def _f64(a, shape=None):
     return a
 
 
+class BatchShape(C.Structure):
+    _fields_ = [("force_block", C.c_int), ("node_block", C.c_int), ("elem_block", C.c_int),
+                ("persistent", C.c_int)]
+
+    def as_tuple(self):
+        return (self.force_block, self.node_block, self.elem_block, self.persistent)
+
+
 class BatchInstance(C.Structure):
     _fields_ = [("mesh", Mesh), ("materials", C.c_void_p), ("num_materials", C.c_int64), ("boundaries", C.c_void_p),
                 ("num_bcs", C.c_int64), ("params", Params)]
@@ -540,6 +552,27 @@ class Batch:
     @property
     def device_bytes(self) -> int:
         return int(_lib.fierro_batch_device_bytes(self.h))
+
+    def set_shape(self, force_block: int = 128, node_block: int = 256, elem_block: int = 128, persistent: int = 0):
+        """fierro_batch_set_shape: threads per block of the force, node and element
+        passes and the persistent grid (blocks per SM, 0 = one block per tile)."""
+        _check(_lib.fierro_batch_set_shape(self.h, C.byref(BatchShape(force_block, node_block, elem_block,
+                                                                      persistent))))
+
+    def shape(self):
+        sh = BatchShape()
+        _check(_lib.fierro_batch_get_shape(self.h, C.byref(sh)))
+        return sh.as_tuple()
+
+    def autotune(self, cycles: int = 3):
+        """fierro_batch_autotune: times the candidate shapes from the uploaded state
+        and keeps the fastest; returns (chosen shape, [(shape, ms per cycle), ...])."""
+        sh = BatchShape()
+        _check(_lib.fierro_batch_autotune(self.h, int(cycles), C.byref(sh)))
+        cap = 64
+        shapes, ms, n = (BatchShape * cap)(), (C.c_double * cap)(), C.c_int64()
+        _check(_lib.fierro_batch_tune_log(self.h, shapes, ms, cap, C.byref(n)))
+        return sh.as_tuple(), [(shapes[i].as_tuple(), ms[i]) for i in range(min(n.value, cap))]
 
 
 def measure_fp64_rate() -> float:

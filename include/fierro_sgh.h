@@ -265,6 +265,35 @@ int fierro_batch_time(fierro_batch* b, int64_t instance, double* time_value, dou
 int64_t fierro_batch_num_instances(const fierro_batch* b);
 int64_t fierro_batch_device_bytes(const fierro_batch* b);
 
+/* Launch shape of a batch's cycle kernels (no counterpart in the reference):
+ * threads per block of the corner-force, node and element passes (powers of two;
+ * force and element 32..128, node 32..1024), and `persistent`: 0 = one block per
+ * tile of elements or nodes, p > 0 = a persistent grid of p blocks per SM that
+ * loops over the tiles.  Results do not depend on the shape (every element and
+ * node runs the same arithmetic; the CFL minimum is order-independent).
+ * Default {128, 256, 128, 0}. */
+typedef struct {
+  int force_block;
+  int node_block;
+  int elem_block;
+  int persistent;
+} fierro_batch_shape;
+
+/* Set or read the shape; set only before the first fierro_batch_run. */
+int fierro_batch_set_shape(fierro_batch* b, const fierro_batch_shape* shape);
+int fierro_batch_get_shape(const fierro_batch* b, fierro_batch_shape* shape);
+/* Autotuner: after every instance has its state and before the first run, time
+ * `cycles` cycles (after one warm-up cycle) of the captured cycle graphs for each
+ * candidate shape of a coordinate descent over the force block {128, 64, 32}, the
+ * node block {256, 128, 512, 64}, the element block {128, 64, 32} and the
+ * persistent grid {0, 1, 2, 4} blocks per SM, each from the uploaded state
+ * (saved and restored on the device; needs one extra copy of the batch's
+ * state), and keep the fastest.  The state afterwards is the uploaded one. */
+int fierro_batch_autotune(fierro_batch* b, int64_t cycles, fierro_batch_shape* chosen);
+/* The last autotune's candidates in timing order and their ms per cycle. */
+int fierro_batch_tune_log(const fierro_batch* b, fierro_batch_shape* shapes, double* ms_per_cycle, int64_t capacity,
+                          int64_t* count);
+
 /* Energy tallies IE = sum elem_mass*elem_sie and KE = 1/2 sum node_mass*|v|^2
  * over device arrays the caller owns, enqueued on `stream` (NULL = default
  * stream), written as two doubles to the DEVICE pointer ie_ke.  No counterpart in

@@ -187,3 +187,36 @@ def test_gradient_matches_frozen_branch_differences(lib_built):
         assert abs(fd - ad) <= TOL * abs(fd), (fd, ad, abs(fd - ad) / abs(fd))
     dm.unfreeze()
 
+
+
+def test_config5_gradient_within_1e6_of_frozen_branch_differences(lib_built):
+    """The discrete-adjoint configuration at its own size: jittered Sedov 64^3
+    (262,144 elements), 400 RK2 cycles, checkpoint every 20 cycles, J against
+    the origin-energy-0.3 target.  The gradient in sie0 and gamma against central
+    differences at step 1e-6 of the frozen-branch forward along four of the
+    seeded directions (relative sie0 perturbations U(-1,1) and a gamma shift
+    U(-1,1)), each within 1e-6 relative with the five-point stencil.  The
+    frozen forward is smooth (J minus its tangent is a clean quadratic along a
+    direction), so the three-point stencil's error is its truncation term
+    h^2 J3 / 6, a few 1e-6 at this step on this deck: it must fall by ~4x when
+    the step halves, the signature of truncation rather than of a wrong
+    derivative."""
+    from fierro_gb300 import adjoint, problems
+    n, cycles = 64, 400
+    target = adjoint.sedov_target(n, cycles, jitter=0.1, seed=7)
+    dm = adjoint.DensityMismatch(problems.sedov(n, jitter=0.1, seed=7, cycles=cycles), target, cycles,
+                                 ckpt_every=20)
+    J, sb, gb, vb = dm.gradient_frozen()
+    assert J > 0
+    dirs = dm.directions(16, seed=2024)
+    for d_sie, d_g in dirs[:4]:
+        ad = _directional(sb, gb, d_sie, d_g)
+        fd3, fd5 = dm.fd5(d_sie, d_g, h=1e-6)
+        assert abs(fd5 - ad) <= TOL * abs(fd5), (fd5, ad, abs(fd5 - ad) / abs(fd5))
+    d_sie, d_g = dirs[0]
+    ad = _directional(sb, gb, d_sie, d_g)
+    e1 = abs(dm.fd(d_sie, d_g, h=1e-6) - ad)
+    e2 = abs(dm.fd(d_sie, d_g, h=5e-7) - ad)
+    assert 3.0 <= e1 / e2 <= 5.0, (e1, e2)
+    dm.unfreeze()
+    dm.solver.close()

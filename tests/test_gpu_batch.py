@@ -59,3 +59,58 @@ def test_batch_rejects_mismatched_controls(lib_built):
     with pytest.raises(sgh.FierroError) as ei:
         sgh.Batch(ps)
     assert ei.value.code == sgh.FIERRO_EINVAL
+
+
+@pytest.mark.parametrize("shape", [(32, 64, 32, 0), (64, 512, 64, 2), (128, 256, 128, 1)])
+def test_launch_shape_does_not_change_results(lib_built, shape):
+    """Every launch shape (threads per block of the three passes, persistent grid
+    or not) gives the default shape's results bit for bit."""
+    from fierro_gb300 import sgh
+    ps = _problems()
+    states = [sgh.setup(p) for p in ps]
+    out = {}
+    for sh in ((128, 256, 128, 0), shape):
+        with sgh.Batch(ps, fp_mode=sgh.FP_FMA) as b:
+            b.set_shape(*sh)
+            assert b.shape() == sh
+            for i, st in enumerate(states):
+                b.set_state(i, st)
+            b.run(30)
+            out[sh] = ([sgh.compared_fields(b.get_state(i)) for i in range(len(ps))],
+                       [b.time(i) for i in range(len(ps))])
+    ref, got = out[(128, 256, 128, 0)], out[shape]
+    assert ref[1] == got[1]
+    for i in range(len(ps)):
+        assert_bitwise(got[0][i], ref[0][i], FIELDS, label="instance %d shape %s" % (i, shape))
+
+
+def test_autotune_keeps_the_uploaded_state_and_the_results(lib_built):
+    """fierro_batch_autotune times the candidate shapes from the uploaded state,
+    restores it and keeps the fastest; the run that follows equals a run with the
+    default shape bit for bit, and the log holds every timed candidate."""
+    from fierro_gb300 import sgh
+    ps = _problems()
+    states = [sgh.setup(p) for p in ps]
+    with sgh.Batch(ps) as b:
+        for i, st in enumerate(states):
+            b.set_state(i, st)
+        b.run(20)
+        ref = [sgh.compared_fields(b.get_state(i)) for i in range(len(ps))]
+    with sgh.Batch(ps) as b:
+        for i, st in enumerate(states):
+            b.set_state(i, st)
+        chosen, log = b.autotune(cycles=2)
+        assert len(log) >= 10 and all(ms > 0 for _, ms in log)
+        assert chosen == min(log, key=lambda r: r[1])[0] and b.shape() == chosen
+        b.run(20)
+        for i in range(len(ps)):
+            assert_bitwise(sgh.compared_fields(b.get_state(i)), ref[i], FIELDS, label="instance %d" % i)
+        with pytest.raises(sgh.FierroError):
+            b.autotune(cycles=2)  # after the first run
+        with pytest.raises(sgh.FierroError):
+            b.set_shape(64, 256, 128, 0)
+    with sgh.Batch(ps[:1]) as b:
+        with pytest.raises(sgh.FierroError):
+            b.set_shape(48, 256, 128, 0)  # not a power of two
+        with pytest.raises(sgh.FierroError):
+            b.autotune(cycles=2)  # no state yet
