@@ -740,9 +740,14 @@ def adjoint_measure(args, compact: bool = False) -> dict:
     frozen = []
     for d_sie, d_g in dm.directions(args.adj_dirs, seed=args.seed):
         ad = float(np.dot(sbf, d_sie) + np.sum(gbf) * d_g)
+        # the directional derivative's own conditioning: the sum of its terms'
+        # magnitudes against its value (a direction nearly orthogonal to the
+        # gradient has a small derivative and FD rounding noise of the usual size)
+        mag = float(np.sum(np.abs(sbf * d_sie)) + abs(np.sum(gbf) * d_g))
         fd3, fd5 = dm.fd5(d_sie, d_g, h=1e-6)
         frozen.append({"ad": ad, "fd3": fd3, "fd5": fd5, "rel3": abs(fd3 - ad) / abs(fd3),
-                       "rel5": abs(fd5 - ad) / abs(fd5)})
+                       "rel5": abs(fd5 - ad) / abs(fd5), "cancellation": mag / abs(ad),
+                       "rel5_of_terms": abs(fd5 - ad) / mag})
     dm.unfreeze()
     rel3 = np.array([d["rel3"] for d in frozen]) if frozen else np.zeros(0)
     rel5 = np.array([d["rel5"] for d in frozen]) if frozen else np.zeros(0)
@@ -752,8 +757,12 @@ def adjoint_measure(args, compact: bool = False) -> dict:
                 "median_rel": float(np.median(rel)) if rel.size else None,
                 "within_1e-6": int((rel <= 1e-6).sum())}
 
+    worst = max(frozen, key=lambda d: d["rel5"]) if frozen else None
     fd_frozen = {"directions": len(frozen), "step": 1e-6, "five_point": summary(rel5),
                  "three_point": summary(rel3),
+                 "five_point_max_rel_of_terms": max(d["rel5_of_terms"] for d in frozen) if frozen else None,
+                 "worst_direction": None if worst is None else {k: worst[k] for k in ("ad", "fd5", "rel5",
+                                                                                    "cancellation")},
                  "gradient_equals_plain": bool(np.array_equal(sbf, sb) and np.array_equal(gbf, gb)),
                  "what": "central differences at step 1e-6 (three-point and five-point stencils) of the "
                          "frozen-branch forward (fierro_adj_branches FREEZE: the limiter neighbour and clamps, Mach "

@@ -120,6 +120,13 @@ int scatter_down(fierro_batch* b, double* out, const double* src, int64_t off, c
   return FIERRO_OK;
 }
 
+// A persistent grid fills every SM `shape.persistent` times over with the
+// kernel's resident blocks at this block size; 0 = one block per tile.
+int persistent_grid(const fierro_batch* b, int kernel, int block) {
+  if (!b->shape.persistent) return 0;
+  return b->sm_count * b->ks->batch_max_blocks(kernel, block) * b->shape.persistent;
+}
+
 ForceArgs b_force(fierro_batch* b, int rb, int q) {
   ForceArgs a{};
   a.ne = (int)b->NE;
@@ -143,7 +150,7 @@ ForceArgs b_force(fierro_batch* b, int rb, int q) {
   a.fuzz = b->fuzz;
   a.small = b->small;
   a.block = b->shape.force_block;
-  a.grid = b->shape.persistent ? b->sm_count * b->shape.persistent : 0;
+  a.grid = persistent_grid(b, 0, b->shape.force_block);
   return a;
 }
 
@@ -175,7 +182,7 @@ NodeArgs b_node(fierro_batch* b, int c, double alpha) {
   a.inst = b->d_inst_n;
   a.rk_alpha = alpha;
   a.block = b->shape.node_block;
-  a.grid = b->shape.persistent ? b->sm_count * b->shape.persistent : 0;
+  a.grid = persistent_grid(b, 1, b->shape.node_block);
   return a;
 }
 
@@ -211,7 +218,7 @@ ElemArgs b_elem(fierro_batch* b, int cur_bin, int c, double alpha, int div_out) 
   a.rk_alpha = alpha;
   a.fuzz = b->fuzz;
   a.block = b->shape.elem_block;
-  a.grid = b->shape.persistent ? b->sm_count * b->shape.persistent : 0;
+  a.grid = persistent_grid(b, 2, b->shape.elem_block);
   return a;
 }
 
@@ -241,7 +248,7 @@ constexpr int kMinBatchBlock = 32;
 bool shape_valid(const fierro_batch_shape& sh) {
   auto ok = [](int b, int hi) { return b >= kMinBatchBlock && b <= hi && (b & (b - 1)) == 0; };
   return ok(sh.force_block, kForceBlock) && ok(sh.node_block, 1024) && ok(sh.elem_block, kElemBlock) &&
-         sh.persistent >= 0 && sh.persistent <= 64;
+         sh.persistent >= 0 && sh.persistent <= 8;
 }
 
 // Makes `sh` the batch's launch shape: the per-instance CFL partial ranges in
@@ -249,7 +256,7 @@ bool shape_valid(const fierro_batch_shape& sh) {
 int apply_shape(fierro_batch* b, const fierro_batch_shape& sh) {
   if (!shape_valid(sh))
     return set_error(FIERRO_EINVAL, "batch shape: blocks must be powers of two, force 32..%d, node 32..1024, "
-                     "element 32..%d, persistent 0..64 blocks per SM", kForceBlock, kElemBlock);
+                     "element 32..%d, persistent 0..8 fills of the SMs", kForceBlock, kElemBlock);
   CUDA_TRY(cudaStreamSynchronize(b->stream));
   b->shape = sh;
   for (size_t i = 0; i < b->part_start.size(); ++i)
@@ -702,7 +709,7 @@ extern "C" int fierro_batch_autotune(fierro_batch* b, int64_t cycles, fierro_bat
     return FIERRO_OK;
   };
   const int force_blocks[] = {128, 64, 32}, node_blocks[] = {256, 128, 512, 64}, elem_blocks[] = {128, 64, 32};
-  const int persist[] = {0, 1, 2, 4};
+  const int persist[] = {0, 1, 2};
   for (int fb : force_blocks) {
     if (rc) break;
     fierro_batch_shape sh = best;

@@ -183,6 +183,9 @@ struct KernelSet {
   void (*energy)(const EnergyArgs&, cudaStream_t);
   void (*end_batch)(Ctrl*, const LoopParams*, int, cudaStream_t);
   const char* name;
+  // resident blocks per SM of a batch kernel (0 force, 1 node, 2 element) at
+  // `block` threads per block: the unit of a persistent grid
+  int (*batch_max_blocks)(int kernel, int block);
 };
 
 constexpr int kElemBlock = 128;

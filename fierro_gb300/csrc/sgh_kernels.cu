@@ -705,6 +705,14 @@ static void launch_end(Ctrl* c, const LoopParams& lp, cudaStream_t s) { k_end<<<
 static void launch_end_batch(Ctrl* c, const LoopParams* lps, int ninst, cudaStream_t s) {
   k_end_batch<<<blocks_for(ninst, 128), 128, 0, s>>>(c, lps, ninst);
 }
+static int batch_max_blocks(int kernel, int block) {
+  int n = 0;
+  cudaError_t err = cudaSuccess;
+  if (kernel == 0) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_force<true, false, false>, block, 0);
+  else if (kernel == 1) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_node<true>, block, 0);
+  else err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_elem<1, true, false>, block, 0);
+  return err == cudaSuccess && n > 0 ? n : 1;
+}
 static void launch_energy(const EnergyArgs& a, cudaStream_t s) {
   const int nb = 512;
   k_energy_part<<<nb, kEnergyBlock, 0, s>>>(a);
@@ -717,14 +725,14 @@ static void launch_energy(const EnergyArgs& a, cudaStream_t s) {
 const KernelSet& kernels_fma() {
   static const KernelSet k = {fma_impl::launch_force, fma_impl::launch_force_tape, fma_impl::launch_force_branch, fma_impl::launch_node, fma_impl::launch_elem,
                               fma_impl::launch_dt, fma_impl::launch_end, fma_impl::launch_energy,
-                              fma_impl::launch_end_batch, "fma"};
+                              fma_impl::launch_end_batch, "fma", fma_impl::batch_max_blocks};
   return k;
 }
 #else
 const KernelSet& kernels_exact() {
   static const KernelSet k = {exact_impl::launch_force, exact_impl::launch_force_tape, exact_impl::launch_force_branch, exact_impl::launch_node, exact_impl::launch_elem,
                               exact_impl::launch_dt, exact_impl::launch_end, exact_impl::launch_energy,
-                              exact_impl::launch_end_batch, "exact"};
+                              exact_impl::launch_end_batch, "exact", exact_impl::batch_max_blocks};
   return k;
 }
 #endif

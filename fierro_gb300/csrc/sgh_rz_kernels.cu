@@ -196,9 +196,9 @@ __global__ void __launch_bounds__(kRzBlock) k_force_rz(const RzForceArgs a) {
 #pragma unroll
   for (int l = 0; l < 4; ++l) {
     const double d0 = u[l] - vs0, d1 = v[l] - vs1;
-    const double mag_vel = sqrt(d0 * d0 + d1 * d1);
+    const double mag_vel = mode_sqrt(d0 * d0 + d1 * d1);
     const double muc = den * (q1c + qb * mag_vel);
-    const double mu_term = muc * sqrt(B[l][0] * B[l][0] + B[l][1] * B[l][1]);
+    const double mu_term = muc * mode_sqrt(B[l][0] * B[l][0] + B[l][1] * B[l][1]);
     s0 = s0 + mu_term * u[l];
     s1 = s1 + mu_term * v[l];
     s3 = s3 + mu_term;
@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(kRzBlock) k_force_rz(const RzForceArgs a) {
   }
   double phi = 1.0 - fmax(0.0, r_min);
   // Mach-number detector with the characteristic length sqrt(area) (:692-700)
-  const double c_length = sqrt(area);
+  const double c_length = mode_sqrt(area);
   const double alpha = fmin(1.0, 20.0 * (c_length * fabs(div)) / (sspd + a.fuzz));
   phi = alpha * phi;
   // corner forces with the inward normals -B, then the hoop-stress terms (:718-755)
@@ -413,7 +413,7 @@ __global__ void __launch_bounds__(kRzBlock) k_elem_rz(const RzElemArgs a) {
       const double den = a.mass[e] / vol;
       const double gamma = a.gamma[e], csmin = a.csmin[e];
       const double pres = (gamma - 1.0) * sie1 * den;
-      sspd = sqrt(gamma * (gamma - 1.0) * sie1);
+      sspd = mode_sqrt(gamma * (gamma - 1.0) * sie1);
       if (sspd < csmin) sspd = csmin;
       a.den[e] = den;
       a.pres[e] = pres;
@@ -437,7 +437,7 @@ __global__ void __launch_bounds__(kRzBlock) k_elem_rz(const RzElemArgs a) {
           d2 = first ? s : fmin(s, d2);
           first = false;
         }
-      const double dist_min = sqrt(d2);
+      const double dist_min = mode_sqrt(d2);
       const double dt_l = a.dt_cfl * dist_min / (sspd + a.fuzz);
       dkey = isnan(dt_l) ? 0x7FFFFFFFFFFFFFFFLL : okey(dt_l);
     }

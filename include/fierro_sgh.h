@@ -268,8 +268,8 @@ int64_t fierro_batch_device_bytes(const fierro_batch* b);
 /* Launch shape of a batch's cycle kernels (no counterpart in the reference):
  * threads per block of the corner-force, node and element passes (powers of two;
  * force and element 32..128, node 32..1024), and `persistent`: 0 = one block per
- * tile of elements or nodes, p > 0 = a persistent grid of p blocks per SM that
- * loops over the tiles.  Results do not depend on the shape (every element and
+ * tile of elements or nodes, p = 1..8 = a persistent grid that fills every SM p
+ * times over with the kernel's resident blocks and loops over the tiles.  Results do not depend on the shape (every element and
  * node runs the same arithmetic; the CFL minimum is order-independent).
  * Default {128, 256, 128, 0}. */
 typedef struct {
@@ -286,7 +286,7 @@ int fierro_batch_get_shape(const fierro_batch* b, fierro_batch_shape* shape);
  * `cycles` cycles (after one warm-up cycle) of the captured cycle graphs for each
  * candidate shape of a coordinate descent over the force block {128, 64, 32}, the
  * node block {256, 128, 512, 64}, the element block {128, 64, 32} and the
- * persistent grid {0, 1, 2, 4} blocks per SM, each from the uploaded state
+ * persistent grid {0, 1, 2}, each from the uploaded state
  * (saved and restored on the device; needs one extra copy of the batch's
  * state), and keep the fastest.  The state afterwards is the uploaded one. */
 int fierro_batch_autotune(fierro_batch* b, int64_t cycles, fierro_batch_shape* chosen);
