@@ -88,6 +88,9 @@ def parse(argv=None):
     ap.add_argument("--configs", action="store_true",
                     help="the small reference decks (Sedov 12^3 for 200 cycles, Noh 32^3 for 500) on the GPU "
                          "and on the reference CPU solver (all host cores and one)")
+    ap.add_argument("--fp64-peak", action="store_true",
+                    help="survey of the FP64 pipe: a pure fma/add/mul stream over chains per thread and "
+                         "resident blocks (the roof the SGH kernels run at)")
     ap.add_argument("--rz", action="store_true",
                     help="2D-RZ run: jittered, permuted RZ Sedov on an n x n quad mesh (--rz-n)")
     ap.add_argument("--rz-n", type=int, default=4096)
@@ -211,20 +214,22 @@ def alg_bytes(kind: str, nn: int, ne: int, nnz: int) -> float:
     return 0.0
 
 
-# Per-element figures of the kernels from ncu captures of the jittered Sedov
-# 64^3 case (one kernel, three launches, --clock-control none).  FP64 thread
-# instructions per element of one launch, exact and FMA modes.  DRAM bytes
-# (dram__bytes_read + dram__bytes_write) per element of one launch, scaled from
-# 64^3 to 256^3 by the element count (the kernels stream their arrays once, so
-# the traffic grows with the elements); the memory traffic is the same in both
-# modes.  k_elem is the mean of its first-stage and last-stage (CFL) launches.
-DRAM_PER_ELEM_256 = {"k_force": 10053043883 / 16777216, "k_elem": 9796794624 / 16777216}
+# Per-element figures of the kernels from ncu captures of jittered Sedov (one
+# kernel filter, three to six launches, --clock-control none).  FP64 thread
+# instructions per element of one launch, exact and FMA modes, at 64^3.  DRAM
+# bytes (dram__bytes_read + dram__bytes_write) per element of one launch at
+# 128^3 (state 13x the L2), applied to 256^3 by the element count (the kernels
+# stream their arrays once, so the traffic grows with the elements); the memory
+# traffic is the same in both modes.  k_elem is the mean of its first-stage and
+# last-stage (CFL) launches.
+DRAM_PER_ELEM = {"k_force": (848042752 + 371475456) / 2097152,
+                 "k_elem": (716690688 + 467264768 + 717134848 + 465028608) / 2 / 2097152}
 NCU_PER_ELEM = {"exact": {
-    "k_force": {"fp64_ops": 138412032 / 262144, "dram_bytes": DRAM_PER_ELEM_256["k_force"]},
-    "k_elem": {"fp64_ops": (158072832 + 171509792) / 2 / 262144, "dram_bytes": DRAM_PER_ELEM_256["k_elem"]},
+    "k_force": {"fp64_ops": 138412032 / 262144, "dram_bytes": DRAM_PER_ELEM["k_force"]},
+    "k_elem": {"fp64_ops": (158072832 + 171509792) / 2 / 262144, "dram_bytes": DRAM_PER_ELEM["k_elem"]},
 }, "fma": {
-    "k_force": {"fp64_ops": 117964811 / 262144, "dram_bytes": DRAM_PER_ELEM_256["k_force"]},
-    "k_elem": {"fp64_ops": (130809856 + 143716888) / 2 / 262144, "dram_bytes": DRAM_PER_ELEM_256["k_elem"]},
+    "k_force": {"fp64_ops": 108527627 / 262144, "dram_bytes": DRAM_PER_ELEM["k_force"]},
+    "k_elem": {"fp64_ops": (130285568 + 143716888) / 2 / 262144, "dram_bytes": DRAM_PER_ELEM["k_elem"]},
 }}
 
 
@@ -1152,8 +1157,33 @@ def configs_bench(args):
                       "configs": out}))
 
 
+def fp64_peak_bench(args):
+    """FP64 operations per second of a pure stream against chains per thread,
+    threads per block and blocks per SM, fma / add / mul."""
+    import torch
+    from fierro_gb300 import sgh
+    torch.cuda.set_device(0)
+    clocks = ClockSampler(0)
+    clocks.start()
+    rows = []
+    for threads, bps in ((128, 1), (128, 2), (128, 4), (128, 8), (256, 1), (256, 4), (256, 8), (512, 4), (1024, 2)):
+        row = {"threads": threads, "blocks_per_sm": bps}
+        for ch in (1, 2, 4, 8, 16):
+            row["fma_ch%d" % ch] = sgh.fp64_stream_rate(ch, 0, threads, bps) / 1e9
+        row["add_ch8"] = sgh.fp64_stream_rate(8, 1, threads, bps) / 1e9
+        row["mul_ch8"] = sgh.fp64_stream_rate(8, 2, threads, bps) / 1e9
+        rows.append(row)
+    peak = max(max(v for k, v in r.items() if k not in ("threads", "blocks_per_sm")) for r in rows)
+    print(json.dumps({"metric": "FP64 pipe throughput, pure stream", "unit": "G FP64 thread-instructions/s",
+                      "value": peak, "higher_is_better": True, "dtype": "f64", "rows": rows,
+                      "clocks": clocks.stop()}))
+
+
 def main(argv=None):
     args = parse(argv)
+    if args.fp64_peak:
+        fp64_peak_bench(args)
+        return
     if args.configs:
         configs_bench(args)
         return

@@ -63,11 +63,23 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
         nvcc_common += ["-Xptxas", "-v"]
     kern = os.path.join(CSRC, "sgh_kernels.cu")
     rzk = os.path.join(CSRC, "sgh_rz_kernels.cu")
+    # FIERRO_KERNEL_NVCC_FLAGS: extra nvcc flags for the cycle kernels (e.g. the
+    # launch-bounds hooks -DFIERRO_ELEM_MIN_BLOCKS=3, or -DFIERRO_LIBRARY_ROOTS);
+    # a change of them rebuilds those objects
+    kflags = os.environ.get("FIERRO_KERNEL_NVCC_FLAGS", "").split()
+    stamp = os.path.join(OBJ, "kernel_flags.txt")
+    old_flags = open(stamp).read() if os.path.exists(stamp) else ""
+    if old_flags != " ".join(kflags):
+        for o in ("sgh_kernels_exact.o", "sgh_kernels_fma.o"):
+            if os.path.exists(os.path.join(OBJ, o)):
+                os.remove(os.path.join(OBJ, o))
+        with open(stamp, "w") as f:
+            f.write(" ".join(kflags))
     units = [
         (os.path.join(OBJ, "sgh_kernels_exact.o"),
-         nvcc_common + ["-DFIERRO_FMA=0", "--fmad=false", "-c", kern], [kern]),
+         nvcc_common + kflags + ["-DFIERRO_FMA=0", "--fmad=false", "-c", kern], [kern]),
         (os.path.join(OBJ, "sgh_kernels_fma.o"),
-         nvcc_common + ["-DFIERRO_FMA=1", "--fmad=true", "-c", kern], [kern]),
+         nvcc_common + kflags + ["-DFIERRO_FMA=1", "--fmad=true", "-c", kern], [kern]),
         (os.path.join(OBJ, "sgh_rz_kernels_exact.o"),
          nvcc_common + ["-DFIERRO_FMA=0", "--fmad=false", "-c", rzk], [rzk]),
         (os.path.join(OBJ, "sgh_rz_kernels_fma.o"),

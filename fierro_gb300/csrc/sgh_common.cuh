@@ -15,8 +15,9 @@ __device__ __forceinline__ double okey_decode(long long k) {
   return __longlong_as_double(k ^ ((k >> 63) & 0x7FFFFFFFFFFFFFFFLL));
 }
 
-#if FIERRO_FMA
-// Square and cube roots of the fused-multiply-add mode: Newton-Raphson iterations
+#if FIERRO_FMA && !defined(FIERRO_LIBRARY_ROOTS)
+// Square and cube roots of the fused-multiply-add mode (FIERRO_LIBRARY_ROOTS
+// builds the FMA mode with the library's sqrt and cbrt instead, for comparison): Newton-Raphson iterations
 // in FP64 from a single-precision seed (Markstein's scheme, "Computation of
 // elementary functions on the IBM RISC System/6000 processor", IBM J. Res. Dev.
 // 34(1), 1990).  The argument is split into a significand m in [1, 4) (square
@@ -72,6 +73,7 @@ __device__ __forceinline__ double mode_cbrt(double v) {
 }
 #else
 __device__ __forceinline__ double mode_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ double mode_cbrt(double v) { return cbrt(v); }
 #endif
 
 // pow(v, 1.0/3.0) as the reference computes it (force_sgh.cpp:319-320).

@@ -98,6 +98,7 @@ def _load():
     lib.fierro_sgh_device_bytes.restype = i64
     lib.fierro_sgh_run_timed.argtypes = [vp, i64, vp, C.POINTER(C.c_float), C.POINTER(i64)]
     lib.fierro_measure_fp64_rate.argtypes = [C.POINTER(dbl)]
+    lib.fierro_fp64_stream_rate.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(dbl)]
     lib.fierro_batch_create.argtypes = [vp, i64, C.c_int, vp, C.POINTER(vp)]
     lib.fierro_batch_destroy.argtypes = [vp]
     lib.fierro_batch_set_state.argtypes = [vp, i64, vp]
@@ -573,6 +574,14 @@ class Batch:
         shapes, ms, n = (BatchShape * cap)(), (C.c_double * cap)(), C.c_int64()
         _check(_lib.fierro_batch_tune_log(self.h, shapes, ms, cap, C.byref(n)))
         return sh.as_tuple(), [(shapes[i].as_tuple(), ms[i]) for i in range(min(n.value, cap))]
+
+
+def fp64_stream_rate(chains: int, op: int = 0, threads: int = 256, blocks_per_sm: int = 4) -> float:
+    """fierro_fp64_stream_rate: FP64 operations per second of a pure stream of
+    `chains` independent chains per thread (op 0 fma, 1 add, 2 mul)."""
+    r = C.c_double()
+    _check(_lib.fierro_fp64_stream_rate(int(chains), int(op), int(threads), int(blocks_per_sm), C.byref(r)))
+    return r.value
 
 
 def measure_fp64_rate() -> float:

@@ -314,6 +314,11 @@ int fierro_energy_tally_noalloc(const double* elem_mass, const double* elem_sie,
 /* FP64 roof calibration on the current device: dependent-chain-free DFMA
  * throughput, in fused multiply-adds per second (one FMA = 2 FLOP). */
 int fierro_measure_fp64_rate(double* dfma_per_second);
+/* FP64 pipe survey on the current device (no counterpart in the reference): a
+ * pure stream of `chains` (1, 2, 4, 8, 16) independent chains per thread of one
+ * operation (op 0 fma, 1 add, 2 mul), `threads` per block, `blocks_per_sm`
+ * blocks per SM; operations per second, best of two timed launches. */
+int fierro_fp64_stream_rate(int chains, int op, int threads, int blocks_per_sm, double* ops_per_second);
 
 /* Graphics dumps (write_outputs, outputs.cpp:10-506), written off the critical
  * path.  With outputs on, every write event of the cycle loop -- t = 0 of a
