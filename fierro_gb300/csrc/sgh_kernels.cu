@@ -6,10 +6,11 @@
 //       the reference's order (Explicit-Lagrange-Kokkos/SGH_solver), with IEEE
 //       division and square root, so results match its uncontracted evaluation;
 //   FIERRO_FMA=1 with --fmad=true  -> fierro::fma_impl: the same schedule, the
-//       compiler free to fuse multiply-adds, the per-node division by mass
-//       done through one reciprocal, and square and
-//       cube roots by Newton iterations from single-precision seeds (within an
-//       ulp; mode_sqrt / mode_cbrt in sgh_common.cuh) -- except where the
+//       compiler free to fuse multiply-adds, the per-node division by mass and
+//       the Riemann velocity's three divisions done through one reciprocal
+//       each, and square and cube roots by Newton iterations from
+//       single-precision seeds (within an ulp; mode_sqrt / mode_cbrt in
+//       sgh_common.cuh) -- except where the
 //       reference's sums cancel (the hex volume, the element power, the Riemann
 //       velocity), which stay separately rounded (FX_MUL / FX_ADD) so this mode
 //       keeps within 1e-12 of the reference after one cycle and 1e-9 after a
@@ -162,9 +163,16 @@ __device__ __forceinline__ void force_elem(const ForceArgs& a, const int e) {
   }
   double vstar0 = 0.0, vstar1 = 0.0, vstar2 = 0.0;
   if (BR == 2 ? (br & FIERRO_BR_VSTAR) != 0 : s3 > a.fuzz) {
+#if FIERRO_FMA
+    const double rs3 = 1.0 / s3;  // one division for the three components
+    vstar0 = s0 * rs3;
+    vstar1 = s1 * rs3;
+    vstar2 = s2 * rs3;
+#else
     vstar0 = s0 / s3;
     vstar1 = s1 / s3;
     vstar2 = s2 / s3;
+#endif
   }
   // shock detector (:287-315): r_face = 0.9 (div_nb + small) / (div + small) is
   // monotone in div_nb (non-decreasing for div + small > 0, non-increasing for < 0),
