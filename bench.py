@@ -228,7 +228,7 @@ NCU_PER_ELEM = {"exact": {
     "k_force": {"fp64_ops": 138412032 / 262144, "dram_bytes": DRAM_PER_ELEM["k_force"]},
     "k_elem": {"fp64_ops": (158072832 + 171509792) / 2 / 262144, "dram_bytes": DRAM_PER_ELEM["k_elem"]},
 }, "fma": {
-    "k_force": {"fp64_ops": 108527627 / 262144, "dram_bytes": DRAM_PER_ELEM["k_force"]},
+    "k_force": {"fp64_ops": 104333312 / 262144, "dram_bytes": DRAM_PER_ELEM["k_force"]},
     "k_elem": {"fp64_ops": (130285568 + 142668312) / 2 / 262144, "dram_bytes": DRAM_PER_ELEM["k_elem"]},
 }}
 
