@@ -684,6 +684,7 @@ extern "C" int fierro_batch_autotune(fierro_batch* b, int64_t cycles, fierro_bat
   b->tune_shapes.clear();
   b->tune_ms.clear();
   int rc = copy_arrays(b, save, arrs, true);
+  const fierro_batch_shape start = b->shape;
   fierro_batch_shape best = b->shape;
   double best_ms = 0.0;
   bool have = false;
@@ -734,11 +735,16 @@ extern "C" int fierro_batch_autotune(fierro_batch* b, int64_t cycles, fierro_bat
     sh.persistent = p;
     rc = trial(sh);
   }
-  // the uploaded state back, with the chosen shape
-  if (!rc) rc = copy_arrays(b, save, arrs, false);
+  // the uploaded state back (also after a failed candidate), with the chosen
+  // shape, or the shape the batch had when the tuning failed
+  const int rc_restore = copy_arrays(b, save, arrs, false);
   cudaStreamSynchronize(b->stream);
   cudaFree(save);
-  if (rc) return rc;
+  if (rc) {
+    apply_shape(b, start);
+    return rc;
+  }
+  if (rc_restore) return rc_restore;
   TRY(apply_shape(b, best));
   if (chosen) *chosen = best;
   return FIERRO_OK;

@@ -68,3 +68,19 @@ def test_injected_allocation_failure(lib_built, monkeypatch, limit):
     with sgh.SGHSolver(prob) as s:
         s.set_state(sgh.setup(prob))
         assert s.run(3) == 3
+
+
+def test_fp64_rate_probes(lib_built):
+    """The FP64 roof the bench reports against: the calibration rate and the pure
+    FP64 stream of fierro_fp64_stream_rate agree (both measure the same pipe), and
+    the stream rejects shapes it does not run."""
+    from fierro_gb300 import sgh
+    calib = sgh.measure_fp64_rate()
+    stream = sgh.fp64_stream_rate(8, 0, 256, 8)
+    assert calib > 1e11 and stream > 1e11
+    assert abs(stream - calib) <= 0.05 * calib, (stream, calib)
+    assert sgh.fp64_stream_rate(8, 1, 256, 4) > 0.8 * stream  # DADD at the DFMA rate
+    for bad in ((3, 0, 256, 4), (8, 3, 256, 4), (8, 0, 100, 4), (8, 0, 256, 0)):
+        with pytest.raises(sgh.FierroError) as ei:
+            sgh.fp64_stream_rate(*bad)
+        assert ei.value.code == sgh.FIERRO_EINVAL
