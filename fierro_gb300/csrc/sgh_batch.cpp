@@ -60,6 +60,7 @@ struct fierro_batch {
   double *d_qtab = nullptr, *d_dt_cfl = nullptr;
   LoopParams* d_lps = nullptr;
   double *d_node_mass = nullptr, *d_elem_mass = nullptr, *d_gamma = nullptr, *d_csmin = nullptr;
+  double* d_node_rm = nullptr;  // 1 / node mass (FMA-mode node update), formed at the first run
   double* d_x[2][3] = {};
   double* d_v[2][3] = {};
   double* d_h[3] = {};
@@ -162,6 +163,7 @@ NodeArgs b_node(fierro_batch* b, int c, double alpha) {
   a.cin = b->d_cin;
   a.force = b->d_force;
   a.node_mass = b->d_node_mass;
+  a.node_rm = b->d_node_rm;
   a.bc_mask = b->d_bc;
   a.u0 = b->d_v[c][0];
   a.v0 = b->d_v[c][1];
@@ -383,6 +385,7 @@ int create_impl(fierro_batch* b, const fierro_batch_instance* inst, int64_t n, i
   TRY(balloc(b, &b->d_dt_cfl, (size_t)n));
   TRY(balloc(b, &b->d_lps, (size_t)n));
   TRY(balloc(b, &b->d_node_mass, (size_t)NN));
+  if (fp_mode == FIERRO_FP_FMA) TRY(balloc(b, &b->d_node_rm, (size_t)NN));
   TRY(balloc(b, &b->d_elem_mass, (size_t)NE));
   TRY(balloc(b, &b->d_gamma, (size_t)NE));
   TRY(balloc(b, &b->d_csmin, (size_t)NE));
@@ -537,6 +540,7 @@ extern "C" int fierro_batch_run(fierro_batch* b, int64_t cycles) {
     for (int64_t i = 0; i < b->n; ++i)
       if (!b->has_state[i]) return set_error(FIERRO_EINVAL, "batch: instance %lld has no state", (long long)i);
     // prime every instance: corner normals, divergence and CFL partials
+    if (b->d_node_rm) b->ks->reciprocal(b->d_node_mass, b->d_node_rm, (int)b->NN, b->stream);
     b->ks->elem(b_elem(b, 0, 0, 1.0, 0), 2, b->stream);
     CUDA_TRY(cudaGetLastError());
     b->started = true;
@@ -646,6 +650,7 @@ int copy_arrays(fierro_batch* b, char* save, const std::vector<std::pair<void*, 
 // Primes the uploaded state with the current shape, runs `warm` cycles, then
 // times `cycles` cycles of the captured graphs; ms per cycle.
 int time_shape(fierro_batch* b, int warm, int cycles, double* ms) {
+  if (b->d_node_rm) b->ks->reciprocal(b->d_node_mass, b->d_node_rm, (int)b->NN, b->stream);
   b->ks->elem(b_elem(b, 0, 0, 1.0, 0), 2, b->stream);
   CUDA_TRY(cudaGetLastError());
   long long k = 0;

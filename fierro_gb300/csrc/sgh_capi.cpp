@@ -97,6 +97,7 @@ NodeArgs node_args(fierro_sgh* h, int c, double alpha) {
   a.cin = h->d_cin;
   a.force = h->d_force;
   a.node_mass = h->d_node_mass;
+  a.node_rm = h->d_node_rm;
   a.bc_mask = h->d_bc;
   a.u0 = h->d_v[c][0];
   a.v0 = h->d_v[c][1];
@@ -365,6 +366,7 @@ static int create_impl(fierro_sgh* h, const fierro_mesh* mesh, const fierro_mate
   TRY(dalloc(h, &h->d_bc, nn));
   TRY(dalloc(h, &h->d_qtab, (size_t)num_materials * 4));
   TRY(dalloc(h, &h->d_node_mass, nn));
+  if (h->fp_mode == FIERRO_FP_FMA) TRY(dalloc(h, &h->d_node_rm, nn));
   TRY(dalloc(h, &h->d_elem_mass, ne));
   TRY(dalloc(h, &h->d_gamma, ne));
   TRY(dalloc(h, &h->d_csmin, ne));
@@ -477,6 +479,7 @@ static int finish_set_state(fierro_sgh* h, double time_value, double graphics_ti
   h->base = 0;
   h->enq_cycles = 0;
   h->stage = 0;
+  if (h->d_node_rm) h->ks->reciprocal(h->d_node_mass, h->d_node_rm, (int)h->nn, h->stream);
   // prime: corner normals, divergence and CFL partials of the uploaded state
   if (h->dims == 2) TRY(rz::prime(h));
   else h->ks->elem(elem_args(h, 0, 0, 1.0, 0), 2, h->stream);
@@ -1151,6 +1154,7 @@ extern "C" int fierro_sgh_restart(fierro_sgh* h, const char* path) {
     }
   }
   std::fclose(f);
+  if (h->d_node_rm) h->ks->reciprocal(h->d_node_mass, h->d_node_rm, (int)h->nn, h->stream);
   h->base = (int)hd.base;
   h->stage = 0;
   h->has_state = true;

@@ -107,6 +107,7 @@ struct NodeArgs {
   const int* cin;
   const double* force;
   const double* node_mass;
+  const double* node_rm;  // 1 / node_mass, computed once per uploaded state (FMA mode; NULL: divide)
   const unsigned char* bc_mask;
   const double *u0, *v0, *w0, *x0, *y0, *z0;  // cycle start (reference bin 0)
   double *u1, *v1, *w1, *x1, *y1, *z1;        // updated (reference bin 1)
@@ -186,6 +187,8 @@ struct KernelSet {
   // resident blocks per SM of a batch kernel (0 force, 1 node, 2 element) at
   // `block` threads per block: the unit of a persistent grid
   int (*batch_max_blocks)(int kernel, int block);
+  // out[i] = 1 / in[i] (IEEE division), i < n
+  void (*reciprocal)(const double* in, double* out, int n, cudaStream_t);
 };
 
 constexpr int kElemBlock = 128;

@@ -55,6 +55,7 @@ struct fierro_sgh {
   double* d_qtab = nullptr;
   // state
   double *d_node_mass = nullptr, *d_elem_mass = nullptr, *d_gamma = nullptr, *d_csmin = nullptr;
+  double* d_node_rm = nullptr;  // 1 / node mass of the uploaded state (FMA-mode node update, hex meshes)
   double* d_x[2][3] = {};
   double* d_v[2][3] = {};
   double* d_h[3] = {};

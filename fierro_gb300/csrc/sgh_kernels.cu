@@ -375,14 +375,16 @@ __device__ __forceinline__ void node_update(const NodeArgs& a, const int n) {
       }
   }
   const double adt = a.rk_alpha * ctrl->dt;
-  const double m = a.node_mass[n];
   const double u0 = a.u0[n], v0 = a.v0[n], w0 = a.w0[n];
 #if FIERRO_FMA
-  const double rm = 1.0 / m;
+  // the reciprocal of the node's mass, formed once per uploaded state (the
+  // same IEEE division, so the same bits as forming it here every stage)
+  const double rm = a.node_rm ? a.node_rm[n] : 1.0 / a.node_mass[n];
   double u1 = u0 + adt * f0 * rm;
   double v1 = v0 + adt * f1 * rm;
   double w1 = w0 + adt * f2 * rm;
 #else
+  const double m = a.node_mass[n];
   double u1 = u0 + adt * f0 / m;
   double v1 = v0 + adt * f1 / m;
   double w1 = w0 + adt * f2 / m;
@@ -721,6 +723,13 @@ static int batch_max_blocks(int kernel, int block) {
   else err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_elem<1, true, false>, block, 0);
   return err == cudaSuccess && n > 0 ? n : 1;
 }
+__global__ void k_reciprocal(const double* __restrict__ in, double* __restrict__ out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = 1.0 / in[i];
+}
+static void launch_reciprocal(const double* in, double* out, int n, cudaStream_t s) {
+  if (n > 0) k_reciprocal<<<blocks_for(n, 256), 256, 0, s>>>(in, out, n);
+}
 static void launch_energy(const EnergyArgs& a, cudaStream_t s) {
   const int nb = 512;
   k_energy_part<<<nb, kEnergyBlock, 0, s>>>(a);
@@ -733,14 +742,16 @@ static void launch_energy(const EnergyArgs& a, cudaStream_t s) {
 const KernelSet& kernels_fma() {
   static const KernelSet k = {fma_impl::launch_force, fma_impl::launch_force_tape, fma_impl::launch_force_branch, fma_impl::launch_node, fma_impl::launch_elem,
                               fma_impl::launch_dt, fma_impl::launch_end, fma_impl::launch_energy,
-                              fma_impl::launch_end_batch, "fma", fma_impl::batch_max_blocks};
+                              fma_impl::launch_end_batch, "fma", fma_impl::batch_max_blocks,
+                              fma_impl::launch_reciprocal};
   return k;
 }
 #else
 const KernelSet& kernels_exact() {
   static const KernelSet k = {exact_impl::launch_force, exact_impl::launch_force_tape, exact_impl::launch_force_branch, exact_impl::launch_node, exact_impl::launch_elem,
                               exact_impl::launch_dt, exact_impl::launch_end, exact_impl::launch_energy,
-                              exact_impl::launch_end_batch, "exact", exact_impl::batch_max_blocks};
+                              exact_impl::launch_end_batch, "exact", exact_impl::batch_max_blocks,
+                              exact_impl::launch_reciprocal};
   return k;
 }
 #endif
