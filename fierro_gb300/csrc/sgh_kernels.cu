@@ -64,8 +64,18 @@
 #define FIERRO_ELEM_BOUNDS __launch_bounds__(kElemBlock)
 #endif
 
+// Corners whose force loads the node update issues together (FIERRO_NODE_GATHER
+// overrides): eight in the FMA mode, four in the exact mode, where eight
+// measured slower (256^3: FMA 1.66 -> 1.52 ms per launch with eight, exact
+// 2.19 -> 2.26 ms).  The sums keep the corner order either way.
+#ifndef FIERRO_NODE_GATHER
+#define FIERRO_NODE_GATHER (FIERRO_FMA ? 8 : 4)
+#endif
+
 namespace fierro {
 namespace FIERRO_IMPL {
+
+constexpr int kNodeGather = FIERRO_NODE_GATHER;
 
 #include "sgh_common.cuh"
 #include "sgh_hex_geometry.cuh"
@@ -352,22 +362,22 @@ __device__ __forceinline__ void node_update(const NodeArgs& a, const int n) {
   const size_t ne = (size_t)a.ne;
   double f0 = 0.0, f1 = 0.0, f2 = 0.0;
   const int c0 = a.cin_start[n], c1 = a.cin_start[n + 1];
-  // corners four at a time: the corner ids, then the twelve force loads, are
+  // corners kNodeGather at a time: the corner ids, then their force loads, are
   // issued before the sums, which keep the corner order
-  for (int base = c0; base < c1; base += 4) {
-    const int cnt = min(4, c1 - base);
-    int cid[4];
+  for (int base = c0; base < c1; base += kNodeGather) {
+    const int cnt = min(kNodeGather, c1 - base);
+    int cid[kNodeGather];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) cid[k] = k < cnt ? __ldg(a.cin + base + k) : 0;
-    double g[4][3];
+    for (int k = 0; k < kNodeGather; ++k) cid[k] = k < cnt ? __ldg(a.cin + base + k) : 0;
+    double g[kNodeGather][3];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < kNodeGather; ++k) {
       const int e = cid[k] >> 3, l = cid[k] & 7;
 #pragma unroll
       for (int d = 0; d < 3; ++d) g[k][d] = k < cnt ? __ldg(a.force + (size_t)(l * 3 + d) * ne + e) : 0.0;
     }
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
+    for (int k = 0; k < kNodeGather; ++k)
       if (k < cnt) {
         f0 = f0 + g[k][0];
         f1 = f1 + g[k][1];
