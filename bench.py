@@ -415,6 +415,7 @@ def ours(args):
     t_setup = time.time() - t0
     nn, ne = prob.mesh.num_nodes, prob.mesh.num_elems
     fp64_rate = sgh.measure_fp64_rate()
+    energy0 = solver.energy()  # IE + KE of the uploaded state (a full-size invariant)
 
     solver.run(args.warmup)
     torch.cuda.synchronize()
@@ -429,6 +430,7 @@ def ours(args):
     ck = clocks.stop()
     if ran != args.steps:
         raise RuntimeError("only %d of %d cycles ran (time_final reached)" % (ran, args.steps))
+    energy1 = solver.energy()
     t_max = reduce_max(dist, total_ms)
     value = ne * args.steps * world / (t_max * 1e-3)
 
@@ -540,6 +542,11 @@ def ours(args):
         "cpu_baseline": None if cpu is None else {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample",
                                                                      "cpu_model", "one_thread") if k in cpu},
         "parity": parity,
+        "invariants": {
+            "total_energy_rel_change": abs(sum(energy1) - sum(energy0)) / abs(sum(energy0)),
+            "total_energy": [sum(energy0), sum(energy1)], "cycles": args.warmup + args.steps,
+            "what": "IE + KE of the full-size state before the warm-up and after the timed cycles (the SGH update "
+                    "is compatible: total energy is conserved up to rounding, sgh_solve.cpp:686-688)"},
         "clocks": ck,
         "setup_seconds": t_setup,
         "device_bytes": solver.device_bytes,
