@@ -179,7 +179,7 @@ int boundary_masks(const fierro_mesh* mesh, const fierro_boundary* bcs, int64_t 
         if (all)
           for (int k = 0; k < 4; ++k) in_set[nie[e * 8 + hex::PATCH[f][k]]] = 1;
       }
-    uint8_t bits = (bcs[s].hydro_bc == 1) ? (uint8_t)(1u << bcs[s].surface) : (uint8_t)7;
+    uint8_t bits = bc_mask_bits(bcs[s].hydro_bc, bcs[s].surface, 3);
     for (int64_t n = 0; n < nn; ++n)
       if (in_set[n]) {
         (*mask_ext)[n] |= bits;
@@ -227,9 +227,9 @@ int validate_bcs(const fierro_boundary* bcs, int64_t num_bcs) {
   for (int64_t s = 0; s < num_bcs; ++s) {
     if (bcs[s].surface < 0 || bcs[s].surface > 4)
       return set_error(FIERRO_EINVAL, "boundary %lld: surface tag %d unknown", (long long)s, bcs[s].surface);
-    if (bcs[s].hydro_bc != 0 && bcs[s].hydro_bc != 1)
-      return set_error(FIERRO_ENOTSUP, "boundary %lld: hydro_bc %d not supported (fixed=0, reflected=1)",
-                       (long long)s, bcs[s].hydro_bc);
+    if (bcs[s].hydro_bc < 0 || bcs[s].hydro_bc > 5)
+      return set_error(FIERRO_EINVAL, "boundary %lld: hydro_bc %d unknown (fixed 0, reflected 1, velocity 2, "
+                       "pressure 3, acceleration 4, contact 5)", (long long)s, bcs[s].hydro_bc);
     if (bcs[s].hydro_bc == 1 && bcs[s].surface > 2)
       return set_error(FIERRO_EINVAL, "boundary %lld: a reflected condition needs a plane surface", (long long)s);
   }

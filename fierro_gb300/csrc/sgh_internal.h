@@ -13,6 +13,17 @@
 
 namespace fierro {
 
+// Velocity components a boundary set holds at zero, as bits 0..dims-1
+// (boundary.cpp:10-55): reflected zeroes the plane's normal component, fixed
+// every component; the other kinds of bdy_hydro_conds (velocity, pressure,
+// acceleration, contact; mesh.h:910-918) have no branch in boundary_velocity,
+// so their nodes move freely.
+inline unsigned char bc_mask_bits(int hydro_bc, int surface, int dims) {
+  if (hydro_bc == 1) return (unsigned char)(1u << surface);
+  if (hydro_bc == 0) return (unsigned char)((1u << dims) - 1u);
+  return 0;
+}
+
 // An NVTX range around a C-ABI call: the call shows up by name on a profiler's
 // timeline; without an attached tool the push and pop do nothing.
 struct NvtxRange {

@@ -103,7 +103,7 @@ void boundary_rz(const fierro_mesh* mesh, const fierro_boundary* bcs, int64_t nu
   }
   for (int64_t s = 0; s < num_bcs; ++s) {
     // reflected: the surface's component (x plane -> u, y plane -> v); fixed: both
-    const uint8_t bits = (bcs[s].hydro_bc == 1) ? (uint8_t)(1u << bcs[s].surface) : (uint8_t)3;
+    const uint8_t bits = bc_mask_bits(bcs[s].hydro_bc, bcs[s].surface, 2);
     for (int64_t pe : edges) {
       const int64_t e = pe / 4;
       const int p = (int)(pe % 4);
@@ -161,9 +161,9 @@ int validate_bcs_rz(const fierro_boundary* bcs, int64_t num_bcs) {
     if (t != 0 && t != 1 && t != 3)
       return set_error(FIERRO_EINVAL, "boundary %lld: surface %d on a 2D-RZ mesh (x plane 0, y plane 1, "
                        "cylinder 3)", (long long)s, t);
-    if (bcs[s].hydro_bc != 0 && bcs[s].hydro_bc != 1)
-      return set_error(FIERRO_ENOTSUP, "boundary %lld: hydro_bc %d not supported (fixed=0, reflected=1)",
-                       (long long)s, bcs[s].hydro_bc);
+    if (bcs[s].hydro_bc < 0 || bcs[s].hydro_bc > 5)
+      return set_error(FIERRO_EINVAL, "boundary %lld: hydro_bc %d unknown (fixed 0, reflected 1, velocity 2, "
+                       "pressure 3, acceleration 4, contact 5)", (long long)s, bcs[s].hydro_bc);
     if (bcs[s].hydro_bc == 1 && t == 3)
       return set_error(FIERRO_EINVAL, "boundary %lld: a reflected condition needs a plane surface", (long long)s);
   }

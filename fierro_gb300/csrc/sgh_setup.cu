@@ -323,7 +323,7 @@ int run(const fierro_mesh* mesh, const double* state_vars, int64_t num_state_var
   // boundary masks
   std::vector<Bc> hb((size_t)num_bcs);
   for (int64_t s = 0; s < num_bcs; ++s)
-    hb[s] = {boundaries[s].surface, boundaries[s].hydro_bc == 1 ? (1 << boundaries[s].surface) : 7,
+    hb[s] = {boundaries[s].surface, (int)bc_mask_bits(boundaries[s].hydro_bc, boundaries[s].surface, 3),
              boundaries[s].value};
   Bc* d_bcs = nullptr;
   unsigned* mask = nullptr;

@@ -409,7 +409,7 @@ int build_device(fierro_sgh* h, const fierro_mesh* mesh, const fierro_boundary* 
   // ---- boundary node masks
   std::vector<Bc> hb((size_t)num_bcs);
   for (int64_t s = 0; s < num_bcs; ++s)
-    hb[s] = {bcs[s].surface, bcs[s].hydro_bc == 1 ? (1 << bcs[s].surface) : 7, bcs[s].value};
+    hb[s] = {bcs[s].surface, (int)bc_mask_bits(bcs[s].hydro_bc, bcs[s].surface, 3), bcs[s].value};
   Bc* d_bcs = nullptr;
   unsigned* m32 = nullptr;
   TRY(sc.alloc(&d_bcs, hb.size()));

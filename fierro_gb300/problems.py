@@ -20,7 +20,9 @@ VELOCITY = {"cartesian": 0, "radial": 1, "spherical": 2, "radial_linear": 3,
             "spherical_linear": 4, "tg_vortex": 5}
 # bdy::bdy_tag and bdy::bdy_hydro_conds (mesh.h:897-918)
 SURFACE = {"x_plane": 0, "y_plane": 1, "z_plane": 2, "cylinder": 3, "sphere": 4}
-HYDRO_BC = {"fixed": 0, "reflected": 1}
+# bdy_hydro_conds (mesh.h:910-918); boundary_velocity (boundary.cpp:10-55) acts on
+# fixed and reflected sets only, the other kinds leave their nodes free
+HYDRO_BC = {"fixed": 0, "reflected": 1, "velocity": 2, "pressure": 3, "acceleration": 4, "contact": 5}
 # model::strength_tag (state.h:103-113)
 STRENGTH = {"none": 0, "hypo": 1, "hyper": 2}
 

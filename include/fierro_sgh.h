@@ -62,7 +62,10 @@ typedef struct {
 } fierro_material;
 
 /* boundary_t (mesh.h:924-935).  surface: 0 x-plane, 1 y-plane, 2 z-plane,
- * 3 cylinder, 4 sphere.  hydro_bc: 0 fixed, 1 reflected (planes only). */
+ * 3 cylinder, 4 sphere.  hydro_bc (bdy_hydro_conds, mesh.h:910-918): 0 fixed,
+ * 1 reflected (planes only); 2 velocity, 3 pressure, 4 acceleration, 5 contact
+ * are accepted and, as in the reference's boundary_velocity (boundary.cpp:10-55),
+ * hold no velocity component. */
 typedef struct {
   int surface;
   double value;

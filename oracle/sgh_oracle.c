@@ -281,7 +281,7 @@ int orc_set_materials(orc_sim* s, int num_materials, const orc_material* m, int 
 int orc_set_boundaries(orc_sim* s, int num_bcs, const orc_boundary* b) {
   if (num_bcs < 0) return 1;
   for (int i = 0; i < num_bcs; ++i) {
-    if (b[i].hydro_bc != 0 && b[i].hydro_bc != 1) return 1;
+    if (b[i].hydro_bc < 0 || b[i].hydro_bc > 5) return 1; /* bdy_hydro_conds, mesh.h:910-918 */
     if (b[i].hydro_bc == 1 && (b[i].surface < 0 || b[i].surface > 2)) return 1;
     if (b[i].surface < 0 || b[i].surface > 4) return 1;
   }
@@ -851,7 +851,7 @@ int64_t orc_get(const orc_sim* s, int which, void* out) {
     memset(m, 0, sizeof(int32_t) * (size_t)s->nn);
     for (int b = 0; b < s->nsets; ++b)
       for (int64_t k = s->bset_start[b]; k < s->bset_start[b + 1]; ++k)
-        m[s->bset[k]] |= (s->bc[b].hydro_bc == 1) ? (1 << s->bc[b].surface) : 7;
+        m[s->bset[k]] |= s->bc[b].hydro_bc == 1 ? (1 << s->bc[b].surface) : s->bc[b].hydro_bc == 0 ? 7 : 0;
     return s->nn;
   }
   void* p;

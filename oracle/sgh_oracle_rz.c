@@ -295,7 +295,7 @@ int orc_rz_set_materials(orc_rz* s, int num_materials, const orc_material* m, in
 int orc_rz_set_boundaries(orc_rz* s, int num_bcs, const orc_boundary* b) {
   if (num_bcs < 0) return 1;
   for (int i = 0; i < num_bcs; ++i) {
-    if (b[i].hydro_bc != 0 && b[i].hydro_bc != 1) return 1;
+    if (b[i].hydro_bc < 0 || b[i].hydro_bc > 5) return 1; /* bdy_hydro_conds, mesh.h:910-918 */
     if (b[i].surface != 0 && b[i].surface != 1 && b[i].surface != 3) return 1;
     if (b[i].hydro_bc == 1 && b[i].surface == 3) return 1;
   }

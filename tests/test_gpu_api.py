@@ -251,3 +251,30 @@ def test_device_view_is_zero_copy_torch(lib_built):
         assert np.array_equal(v["node_ext2int"].long().cpu().numpy()[n2e], np.arange(prob.mesh.num_nodes))
         # zero copy: a second view aliases the same memory
         assert s.device_view()["den"].data_ptr() == v["den"].data_ptr()
+
+
+@pytest.mark.parametrize("kind", ["velocity", "contact"])
+def test_other_boundary_kinds_leave_nodes_free(oracle_built, lib_built, kind):
+    """Boundary sets of the kinds the reference's boundary_velocity has no
+    branch for run as the reference runs them, holding no velocity component:
+    bit for bit the same run as without the set, and as the restatement."""
+    import copy
+    from fierro_gb300 import problems, sgh
+    from oracle import orc
+    prob = problems.noh(8, jitter=0.1, seed=4, permute=True, cycles=30)
+    plus = copy.deepcopy(prob)
+    plus.boundaries.append(problems.Boundary("x_plane", 1.0, kind))
+    got = {}
+    for name, p in (("plus", plus), ("plain", prob)):
+        with sgh.SGHSolver(p) as s:
+            s.set_state(sgh.setup(p))
+            s.run(30)
+            got[name] = sgh.compared_fields(s.get_state())
+    fields = ("coords", "vel", "den", "pres", "sie", "sspd", "vol")
+    for k in fields:
+        assert np.array_equal(got["plus"][k], got["plain"][k]), k
+    o = orc.Oracle(plus, variant="crpow")
+    o.run_cycles(30)
+    ref = o.state()
+    for k in fields:
+        assert np.array_equal(got["plus"][k], ref[k]), k

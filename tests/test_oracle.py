@@ -232,3 +232,27 @@ def test_oracle_equals_reference_on_shipped_unstructured_meshes(oracle_built, na
     assert st["time"] == float(ref["time"])
     for k in ("coords", "vel", "den", "pres", "sie", "sspd", "vol", "node_mass", "mass"):
         assert np.array_equal(st[k], ref[k]), (name, cycles, k)
+
+
+@pytest.mark.parametrize("kind", ["velocity", "pressure", "acceleration", "contact"])
+def test_other_boundary_kinds_leave_nodes_free(oracle_built, kind):
+    """A boundary set of the kinds boundary_velocity has no branch for
+    (boundary.cpp:10-55; bdy_hydro_conds mesh.h:910-918) holds no velocity
+    component: the reference run with such a set on the far x plane equals the
+    run without it and the restatement, bit for bit."""
+    import copy
+    from fierro_gb300 import problems
+    from oracle import orc
+    prob = problems.noh(8, jitter=0.1, seed=4, permute=True, cycles=30)
+    plus = copy.deepcopy(prob)
+    plus.boundaries.append(problems.Boundary("x_plane", 1.0, kind))
+    o = orc.Oracle(plus)
+    o.run_cycles(30)
+    o_plain = orc.Oracle(prob)
+    o_plain.run_cycles(30)
+    assert_bitwise(o.state(), o_plain.state(), FIELDS, label="restatement %s vs none" % kind)
+    assert not np.any(o.get(orc.ORC_BDY_NODE_MASK) & ~o_plain.get(orc.ORC_BDY_NODE_MASK))
+    if not orc.reference_available("fierro_ref"):
+        pytest.skip("reference executable not built on this machine")
+    ref = orc.run_reference(plus, cycles=30, threads=2)
+    assert_bitwise(o.state(), ref, FIELDS + ("corner_force",), label="%s set vs reference" % kind)
