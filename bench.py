@@ -233,6 +233,34 @@ NCU_PER_ELEM = {"exact": {
 }}
 
 
+def link_rates(nbytes: int = 1 << 30) -> dict:
+    """The host link's copy rate, the roofline of the end-to-end transfers:
+    cudaMemcpyAsync of one 1 GiB pinned buffer to and from HBM (best of three,
+    CUDA events on a side stream)."""
+    import torch
+    host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    dev = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.Stream()
+    out = {}
+    with torch.cuda.stream(s):
+        for name, dst, src in (("h2d_gbs", dev, host), ("d2h_gbs", host, dev)):
+            best = None
+            for _ in range(4):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(s)
+                dst.copy_(src, non_blocking=True)
+                e1.record(s)
+                e1.synchronize()
+                ms = e0.elapsed_time(e1)
+                best = ms if best is None else min(best, ms)
+            out[name] = nbytes / (best * 1e-3) / 1e9
+    s.synchronize()
+    del host, dev
+    out["what"] = "cudaMemcpyAsync of a 1 GiB pinned buffer, best of 4; upload_frac / download_frac: the " \
+                  "state transfer's bytes / time against it"
+    return out
+
+
 def measure_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -483,9 +511,12 @@ def ours(args):
             trials.append((reduce_max(dist, te1 - te0), tu - te0, tr - tu, te1 - tr))
         trials.sort()
         med = trials[1]
+        link = link_rates()
         e2e = {"value": ne * args.steps * world / med[0], "unit": UNIT,
                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
                "upload_s": med[1], "run_s": med[2], "download_s": med[3],
+               "link": dict(link, upload_frac=h2d / med[1] / 1e9 / link["h2d_gbs"],
+                            download_frac=d2h / med[3] / 1e9 / link["d2h_gbs"]),
                "trials_s": [[round(x, 4) for x in t] for t in trials],
                "path": "fierro_sgh_set_state + fierro_sgh_run(K) + fierro_sgh_get_state, host buffers in "
                        "the reference layouts (AoS, caller numbering, resident pages), one upload and one "

@@ -48,3 +48,38 @@ def random_deck(seed: int, dims: int):
     params = Params(time_final=float(rng.uniform(0.05, 1.0)), dt_cfl=float(rng.uniform(0.2, 0.5)),
                     cycle_stop=int(rng.integers(10, 40)), rk_num_stages=int(rng.integers(1, 4)))
     return Problem("fuzz%d_%dd" % (seed, dims), m, mats, fills, bcs, params)
+
+
+# Meshes one element thick in some direction, down to a single element: every
+# node lies on the box's surface, the limiter of a lone element has no
+# neighbour, and the Morton order and the patch tagging see degenerate extents.
+THIN_SHAPES = [(1, 1, 1), (1, 1, 5), (1, 4, 3), (2, 1, 1), (7, 1, 1)]
+THIN_SHAPES_RZ = [(1, 1), (1, 5), (6, 1), (2, 1)]
+
+
+def thin_deck(shape, seed: int = 5, cycles: int = 30):
+    """A jittered, permuted box (hex, or 2D-RZ quads for a two-entry shape) of
+    `shape` elements with a hot, moving block in one corner, a reflecting plane
+    at the origin (x = 0 for hexes, the axis y = 0 for quads) and a fixed plane
+    at a far face (z for hexes, x for quads)."""
+    from fierro_gb300 import mesh
+    from fierro_gb300.problems import Boundary, Fill, Material, Params, Problem
+    rng = np.random.default_rng(seed)
+    dims = len(shape)
+    L = tuple(float(v) for v in rng.uniform(0.5, 1.5, dims))
+    if dims == 3:
+        m = mesh.box_mesh(*shape, length=L, jitter=0.1, seed=seed, permute=True)
+    else:
+        m = mesh.quad_mesh(*shape, length=L, jitter=0.1, seed=seed, permute=True)
+    mats = [Material(q1=1.0, q1ex=1.33, q2=1.0, q2ex=1.33, gamma=1.4, csmin=1e-14)]
+    hot = Fill("box", 0, den=2.0, sie=1.0, velocity="cartesian")
+    hot.x1, hot.x2 = 0.0, 0.6 * L[0]
+    hot.y1, hot.y2 = 0.0, 0.6 * L[1]
+    hot.z1, hot.z2 = (0.0, 0.6 * L[2]) if dims == 3 else (-1.0, 1.0)
+    hot.u, hot.v, hot.w = 0.1, -0.05, 0.2 if dims == 3 else 0.0
+    if dims == 3:
+        bcs = [Boundary("x_plane", 0.0, "reflected"), Boundary("z_plane", L[2], "fixed")]
+    else:
+        bcs = [Boundary("y_plane", 0.0, "reflected"), Boundary("x_plane", L[0], "fixed")]
+    return Problem("thin" + "x".join(str(n) for n in shape), m, mats, [Fill("global", 0, den=1.0, sie=1e-3), hot],
+                   bcs, Params(cycle_stop=cycles))

@@ -227,6 +227,22 @@ def test_host_setup_random_decks(lib_built, oracle_built, dims):
         assert_bitwise(got, r, list(got), label="%s" % prob.name)
 
 
+def test_host_setup_thin_meshes(lib_built, oracle_built):
+    """Host set-up of boxes one element thick, down to one element (hex and
+    2D-RZ), equals the restatement's set-up bit for bit."""
+    from decks import THIN_SHAPES, THIN_SHAPES_RZ, thin_deck
+    from fierro_gb300 import sgh
+    from oracle import orc
+    for shape in THIN_SHAPES + THIN_SHAPES_RZ:
+        prob = thin_deck(shape)
+        st = sgh.setup(prob)
+        r = orc.Oracle(prob).state()
+        got = {"coords": st["node_coords"][1], "vel": st["node_vel"][1], "den": st["elem_den"],
+               "pres": st["elem_pres"], "sie": st["elem_sie"][1], "sspd": st["elem_sspd"], "vol": st["elem_vol"],
+               "mass": st["elem_mass"], "node_mass": st["node_mass"]}
+        assert_bitwise(got, r, list(got), label=prob.name)
+
+
 def test_integration_notes_show_the_compiled_binding():
     """The sgh_solve replacement shown in INTEGRATION.md section 1 is the text
     that tests/test_gpu_binding.py compiles into the reference's driver

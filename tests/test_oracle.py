@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN, assert_bitwise, load_golden
+from decks import THIN_SHAPES, THIN_SHAPES_RZ, thin_deck
 
 FIELDS = ("coords", "vel", "den", "pres", "sie", "sspd", "vol")
 
@@ -256,3 +257,18 @@ def test_other_boundary_kinds_leave_nodes_free(oracle_built, kind):
         pytest.skip("reference executable not built on this machine")
     ref = orc.run_reference(plus, cycles=30, threads=2)
     assert_bitwise(o.state(), ref, FIELDS + ("corner_force",), label="%s set vs reference" % kind)
+
+
+@pytest.mark.parametrize("shape", THIN_SHAPES + THIN_SHAPES_RZ)
+def test_oracle_equals_reference_on_thin_meshes(oracle_built, shape):
+    """Meshes one element thick, down to a single element (every node on the
+    surface, a lone element's limiter with no neighbour), hex and 2D-RZ: the
+    restatement equals the reference executable bit for bit after 30 cycles."""
+    from oracle import orc
+    prob = thin_deck(shape)
+    o = orc.Oracle(prob)
+    o.run_cycles(30)
+    if not orc.reference_available("fierro_ref"):
+        pytest.skip("reference executable not built on this machine")
+    ref = orc.run_reference(prob, cycles=30, threads=2)
+    assert_bitwise(o.state(), ref, FIELDS + ("corner_force", "div"), label=prob.name)
