@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "fierro_sgh.h"
+#include "sgh_device.h"
 #include "sgh_internal.h"
 
 namespace {
@@ -121,5 +122,29 @@ extern "C" int fierro_measure_fp64_rate(double* dfma_per_second) {
   cudaFree(d);
   if (err != cudaSuccess) return set_error(FIERRO_ECUDA, "%s", cudaGetErrorString(err));
   *dfma_per_second = 8.0 * kIters * (double)blocks * threads / (best * 1e-3);
+  return FIERRO_OK;
+}
+
+// The arithmetic mode's square and cube roots, quotients and reciprocals against
+// the library's (the FMA mode's Newton forms; the exact mode calls the library).
+extern "C" int fierro_root_check(int fp_mode, int which, long long n, unsigned long long seed, int lo_exp,
+                                 int hi_exp, unsigned long long* out) {
+  using fierro::set_error;
+  if (!out) return set_error(FIERRO_EINVAL, "NULL output");
+  if ((fp_mode != FIERRO_FP_EXACT && fp_mode != FIERRO_FP_FMA) || which < 0 || which > 3 || n < 8 ||
+      n > (1LL << 36) || lo_exp < -1022 || hi_exp > 1023 || lo_exp > hi_exp)
+    return set_error(FIERRO_EINVAL, "root check: fp_mode 0/1, which 0 sqrt / 1 cbrt / 2 quotient / 3 reciprocal, 8 <= n <= 2^36, "
+                                    "-1022 <= lo_exp <= hi_exp <= 1023");
+  const fierro::KernelSet& ks = fp_mode == FIERRO_FP_FMA ? fierro::kernels_fma() : fierro::kernels_exact();
+  unsigned long long* d = nullptr;
+  if (cudaMalloc(&d, 3 * sizeof(unsigned long long)) != cudaSuccess) return set_error(FIERRO_ENOMEM, "cudaMalloc");
+  cudaError_t err = cudaMemset(d, 0, 3 * sizeof(unsigned long long));
+  if (err == cudaSuccess) {
+    ks.root_check(which, n, seed, lo_exp, hi_exp, d, 0);
+    err = cudaGetLastError();
+  }
+  if (err == cudaSuccess) err = cudaMemcpy(out, d, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (err != cudaSuccess) return set_error(FIERRO_ECUDA, "%s", cudaGetErrorString(err));
   return FIERRO_OK;
 }

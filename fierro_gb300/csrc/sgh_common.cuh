@@ -15,22 +15,9 @@ __device__ __forceinline__ double okey_decode(long long k) {
   return __longlong_as_double(k ^ ((k >> 63) & 0x7FFFFFFFFFFFFFFFLL));
 }
 
-#if FIERRO_FMA && !defined(FIERRO_LIBRARY_ROOTS)
-// Square and cube roots of the fused-multiply-add mode (FIERRO_LIBRARY_ROOTS
-// builds the FMA mode with the library's sqrt and cbrt instead, for comparison): Newton-Raphson iterations
-// in FP64 from a single-precision seed (Markstein's scheme, "Computation of
-// elementary functions on the IBM RISC System/6000 processor", IBM J. Res. Dev.
-// 34(1), 1990).  The argument is split into a significand m in [1, 4) (square
-// root) or [1, 8) (cube root) and a power of two by integer operations; the seed
-// comes from the single-precision hardware reciprocal square root / the
-// single-precision cube root of m's truncated image (about 2^-22 relative); two
-// Newton steps, each one DMUL/DFMA pair around an exactly formed residual, carry
-// it to about 2^-88, so the result is the rounded root up to the final fma's
-// rounding.  Measured on 2^28 random inputs against the library: the square
-// root differs in 1 of 10^6 results by 1 ulp, the cube root in 8.6% by 1 ulp
-// (the library's cube root is not correctly rounded either); both run 1.3x /
-// 1.8x the library's throughput on the FP64 pipe, which bounds these kernels.
-// Zero, negative, subnormal and non-finite arguments take the library's path.
+#if FIERRO_FMA
+// Bit-level conversions between doubles and floats for the FMA mode's roots and
+// quotients (integer operations only: no FP64 pipe work).
 
 // Single-precision image of a positive double within float range (truncated).
 __device__ __forceinline__ float f32_image(double d) {
@@ -38,42 +25,157 @@ __device__ __forceinline__ float f32_image(double d) {
   const int e = (int)((b >> 52) & 0x7FF) - 1023 + 127;
   return __int_as_float((e << 23) | (int)((b >> 29) & 0x7FFFFF));
 }
+// What f32_image drops: the low 29 significand bits of a positive double with
+// exponent in [0, 2], rounded to single precision.
+__device__ __forceinline__ float f32_rest(double d) {
+  const long long b = __double_as_longlong(d);
+  const int e = (int)((b >> 52) & 0x7FF) - 1023;
+  return (float)(int)(b & 0x1FFFFFFF) * __int_as_float((127 + e - 52) << 23);
+}
 // The double of a positive normal float, exactly, from its bits.
 __device__ __forceinline__ double f64_of(float f) {
   const unsigned b = __float_as_uint(f);
   const long long e = (long long)((b >> 23) & 0xFF) - 127 + 1023;
   return __longlong_as_double((e << 52) | ((long long)(b & 0x7FFFFF) << 29));
 }
+// The double of a float of either sign, exactly; zero for zero and subnormal floats.
+__device__ __forceinline__ double f64_of_signed(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xFF;
+  const long long bits = ((long long)(b >> 31) << 63) | ((long long)(e + (1023 - 127)) << 52) |
+                         ((long long)(b & 0x7FFFFF) << 29);
+  return __longlong_as_double(e == 0 ? 0LL : bits);
+}
+#endif
+
+#if FIERRO_FMA && !defined(FIERRO_LIBRARY_ROOTS)
+// Square and cube roots of the fused-multiply-add mode (FIERRO_LIBRARY_ROOTS
+// builds the FMA mode with the library's sqrt and cbrt instead, for comparison),
+// by Newton-Raphson iteration from a single-precision seed (Markstein's scheme,
+// "Computation of elementary functions on the IBM RISC System/6000 processor",
+// IBM J. Res. Dev. 34(1), 1990), arranged so that most of the work runs on the
+// FP32 and integer pipes: the FP64 pipe bounds these kernels, and GB300 issues
+// FP64 at a small fraction of its FP32 rate.
+//
+// The argument is split into a significand m in [1, 4) (square root) or [1, 8)
+// (cube root) and a power of two by integer operations, and m into a pair of
+// floats mh + ml (its top 24 significand bits, exactly, and the next 29 bits
+// rounded).  A single-precision root y0 (hardware reciprocal square root, or
+// cbrtf; ~2^-22 relative) is refined by one Newton step evaluated in single
+// precision on the pair: the residual m - y0^2 (m - y0^3) is formed from the
+// products' exact low parts (fmaf), so the step carries y0 + c to ~2^-43.  One
+// FP64 Newton step around an exactly formed residual then reaches ~2^-66 (square
+// root) before the final rounding; the cube root's residual rounds y^2 once, as
+// the two-step form below does.  Three FP64 operations per square root and four
+// per cube root, against six and seven for two FP64 steps from the float seed
+// (FIERRO_ROOTS_FP64_NEWTON).  The single-precision steps use the _rn
+// intrinsics, which are never contracted: a fused mh - y0*y0 would count the
+// product's low part twice.  Zero, negative, subnormal and non-finite arguments
+// take the library's path (tested on the bits, not on the FP64 pipe).
+
 __device__ __forceinline__ double mode_sqrt(double x) {
   const long long b = __double_as_longlong(x);
   const int ex = (int)((b >> 52) & 0x7FF);
-  if (!(x > 0.0) || ex == 0 || ex == 0x7FF) return sqrt(x);
+  if (b <= 0 || ex == 0 || ex == 0x7FF) return sqrt(x);
   const int k = (ex - 1023) >> 1;                                      // x = m 4^k
   const double m = __longlong_as_double(b - ((long long)(2 * k) << 52));  // [1, 4)
-  const double r = f64_of(rsqrtf(f32_image(m)));                       // ~ 1 / sqrt(m)
-  const double h = __longlong_as_double(__double_as_longlong(r) - (1LL << 52));  // r / 2
-  double y = m * r;
+  const float mh = f32_image(m);
+  const float r = rsqrtf(mh);                                          // ~ 1 / sqrt(m)
+#ifdef FIERRO_ROOTS_FP64_NEWTON
+  const double h = __longlong_as_double(__double_as_longlong(f64_of(r)) - (1LL << 52));  // r / 2
+  double y = m * f64_of(r);
   y = fma(h, fma(-y, y, m), y);
   y = fma(h, fma(-y, y, m), y);
+#else
+  const float y0 = __fmul_rn(mh, r);
+  const float p = __fmul_rn(y0, y0);
+  const float pe = fmaf(y0, y0, -p);                                   // y0^2 = p + pe exactly
+  const float d = __fadd_rn(__fsub_rn(__fsub_rn(mh, p), pe), f32_rest(m));  // m - y0^2 (mh - p exact)
+  const float c = __fmul_rn(d, __fmul_rn(0.5f, r));
+  const double h = __longlong_as_double(__double_as_longlong(f64_of(r)) - (1LL << 52));  // r / 2
+  double y = __dadd_rn(f64_of(y0), f64_of_signed(c));
+  y = fma(h, fma(-y, y, m), y);
+#endif
   return __longlong_as_double(__double_as_longlong(y) + ((long long)k << 52));
 }
 __device__ __forceinline__ double mode_cbrt(double v) {
   const long long b = __double_as_longlong(v);
   const int ex = (int)((b >> 52) & 0x7FF);
-  if (!(v > 0.0) || ex == 0 || ex == 0x7FF) return cbrt(v);
+  if (b <= 0 || ex == 0 || ex == 0x7FF) return cbrt(v);
   const int E = ex - 1023;
   const int k = E >= 0 ? E / 3 : -((2 - E) / 3);                        // floor(E / 3)
   const double m = __longlong_as_double(b - ((long long)(3 * k) << 52));  // [1, 8)
-  const float cf = cbrtf(f32_image(m));
-  const double c0 = f64_of(cf);
-  const double inv = f64_of(__frcp_rn(3.0f * cf * cf));                // ~ 1 / (3 c^2)
-  double c = fma(fma(-(c0 * c0), c0, m), inv, c0);
+  const float mh = f32_image(m);
+  const float c0 = cbrtf(mh);
+#ifdef FIERRO_ROOTS_FP64_NEWTON
+  const double c0d = f64_of(c0);
+  const double inv = f64_of(__frcp_rn(3.0f * c0 * c0));                // ~ 1 / (3 c^2)
+  double c = fma(fma(-(c0d * c0d), c0d, m), inv, c0d);
   c = fma(fma(-(c * c), c, m), inv, c);
+#else
+  const float p = __fmul_rn(c0, c0);
+  const float pe = fmaf(c0, c0, -p);                                   // c0^2 = p + pe exactly
+  const float q = __fmul_rn(p, c0);
+  const float qe = __fadd_rn(fmaf(p, c0, -q), __fmul_rn(pe, c0));      // c0^3 ~ q + qe
+  const float d = __fadd_rn(__fsub_rn(__fsub_rn(mh, q), qe), f32_rest(m));  // m - c0^3 (mh - q exact)
+  const float inv = __frcp_rn(__fmul_rn(3.0f, p));                     // ~ 1 / (3 c0^2)
+  double c = __dadd_rn(f64_of(c0), f64_of_signed(__fmul_rn(d, inv)));
+  const double c2 = c * c;
+  c = fma(fma(-c2, c, m), f64_of(inv), c);
+#endif
   return __longlong_as_double(__double_as_longlong(c) + ((long long)k << 52));
 }
 #else
 __device__ __forceinline__ double mode_sqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ double mode_cbrt(double v) { return cbrt(v); }
+#endif
+
+#if FIERRO_FMA && !defined(FIERRO_LIBRARY_DIV)
+// Quotients and reciprocals of the FMA mode (FIERRO_LIBRARY_DIV builds it with
+// the library's IEEE division instead, for comparison), by the same scheme as
+// the roots above (Markstein's): the single-precision reciprocal of the
+// divisor's truncated image, refined by one Newton step on the float pair
+// b = bh + bl (the residual 1 - b r0 from the product's exact low part), gives
+// 1/b to ~2^-45 as the sum of two floats; one FMA correction around the exactly
+// formed residual a - b q0 then leaves ~2^-90 relative error before the final
+// rounding, so the result is the correctly rounded quotient except where the
+// exact one lies within ~2^-37 ulp of a rounding boundary.  Four FP64 operations
+// per quotient and three per reciprocal.  Operands outside 2^-500 .. 2^500 in
+// magnitude (zero, subnormal, non-finite included) take the library's division
+// (tested on the bits).
+
+// 1/|b| 2^eb ~ 1/|b'| for b' = b scaled into [1, 2): the float pair's sum as a
+// double, scaled back by 2^-eb with b's sign; b normal.
+__device__ __forceinline__ double rcp_seed(long long bb) {
+  const int eb = (int)((bb >> 52) & 0x7FF) - 1023;
+  const double bm = __longlong_as_double((bb & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL);  // [1, 2)
+  const float bh = f32_image(bm);
+  const float r0 = __frcp_rn(bh);
+  const float p = __fmul_rn(bh, r0);
+  const float pe = fmaf(bh, r0, -p);                                    // bh r0 = p + pe exactly
+  const float e = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, p), pe), __fmul_rn(f32_rest(bm), r0));  // 1 - bm r0
+  const double r = __dadd_rn(f64_of(r0), f64_of_signed(__fmul_rn(r0, e)));
+  return __longlong_as_double((__double_as_longlong(r) - ((long long)eb << 52)) ^ (bb & (long long)0x8000000000000000ULL));
+}
+__device__ __forceinline__ bool plain_range(long long bits) {
+  return (unsigned)((bits >> 52) & 0x7FF) - 523u <= 1000u;  // 2^-500 <= |x| < 2^501
+}
+__device__ __forceinline__ double mode_div(double a, double b) {
+  const long long ab = __double_as_longlong(a), bb = __double_as_longlong(b);
+  if (!plain_range(ab) || !plain_range(bb)) return a / b;
+  const double r = rcp_seed(bb);
+  const double q0 = a * r;
+  return fma(fma(-b, q0, a), r, q0);
+}
+__device__ __forceinline__ double mode_rcp(double b) {
+  const long long bb = __double_as_longlong(b);
+  if (!plain_range(bb)) return 1.0 / b;
+  const double r = rcp_seed(bb);
+  return fma(fma(-b, r, 1.0), r, r);
+}
+#else
+__device__ __forceinline__ double mode_div(double a, double b) { return a / b; }
+__device__ __forceinline__ double mode_rcp(double b) { return 1.0 / b; }
 #endif
 
 // pow(v, 1.0/3.0) as the reference computes it (force_sgh.cpp:319-320).

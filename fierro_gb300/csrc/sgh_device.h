@@ -189,6 +189,11 @@ struct KernelSet {
   int (*batch_max_blocks)(int kernel, int block);
   // out[i] = 1 / in[i] (IEEE division), i < n
   void (*reciprocal)(const double* in, double* out, int n, cudaStream_t);
+  // the mode's square root, cube root, quotient or reciprocal (which 0..3)
+  // against the library's on n seeded inputs: out[0] differing, out[1] largest
+  // difference in ulps, out[2] differing by more than one ulp (fierro_root_check)
+  void (*root_check)(int which, long long n, unsigned long long seed, int lo_exp, int hi_exp,
+                     unsigned long long* out, cudaStream_t);
 };
 
 constexpr int kElemBlock = 128;

@@ -8,9 +8,10 @@
 //   FIERRO_FMA=1 with --fmad=true  -> fierro::fma_impl: the same schedule, the
 //       compiler free to fuse multiply-adds, the per-node division by mass and
 //       the Riemann velocity's three divisions done through one reciprocal
-//       each, and square and cube roots by Newton iterations from
-//       single-precision seeds (within an ulp; mode_sqrt / mode_cbrt in
-//       sgh_common.cuh) -- except where the
+//       each, square and cube roots (within an ulp) and the remaining quotients
+//       (the IEEE quotient's bits) by Newton iterations from single-precision
+//       seeds, mostly on the FP32 and integer pipes (mode_sqrt, mode_cbrt,
+//       mode_div, mode_rcp in sgh_common.cuh) -- except where the
 //       reference's sums cancel (the hex volume, the element power, the Riemann
 //       velocity), which stay separately rounded (FX_MUL / FX_ADD) so this mode
 //       keeps within 1e-12 of the reference after one cycle and 1e-9 after a
@@ -35,6 +36,7 @@
 // rk_init's copies (time_integration.cpp:9-44) are replaced by swapping the roles
 // of two state bins.  Nothing is accumulated with atomics: every output has one
 // writer and every reduction has a fixed order.
+#include <algorithm>
 #include <cstdint>
 
 #include "sgh_device.h"
@@ -86,7 +88,7 @@ constexpr int kNodeGather = FIERRO_NODE_GATHER;
 // B the outward corner normals in rows [lid*3+dim][ne], summed over l in order.
 __device__ __forceinline__ void velocity_gradient(const double (&u)[8], const double (&v)[8], const double (&w)[8],
                                                   const double* bmat, int ne, int e, double vol, double (&L)[9]) {
-  const double inverse_vol = 1.0 / vol;
+  const double inverse_vol = mode_rcp(vol);
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
     double b = bmat[(size_t)j * ne + e];
@@ -174,7 +176,7 @@ __device__ __forceinline__ void force_elem(const ForceArgs& a, const int e) {
   double vstar0 = 0.0, vstar1 = 0.0, vstar2 = 0.0;
   if (BR == 2 ? (br & FIERRO_BR_VSTAR) != 0 : s3 > a.fuzz) {
 #if FIERRO_FMA
-    const double rs3 = 1.0 / s3;  // one division for the three components
+    const double rs3 = mode_rcp(s3);  // one reciprocal for the three components
     vstar0 = s0 * rs3;
     vstar1 = s1 * rs3;
     vstar2 = s2 * rs3;
@@ -202,11 +204,11 @@ __device__ __forceinline__ void force_elem(const ForceArgs& a, const int e) {
     const double dsel = okey_decode(D > 0 ? kmin : kmax);
     const bool regular = isfinite(D) && D != 0.0 && isfinite(dsel);
     if (regular) {
-      const double r_face = 0.9 * (dsel + small) / D;
+      const double r_face = mode_div(0.9 * (dsel + small), D);
       r_min = okey(r_face) < okey(1.0) ? r_face : 1.0;
     } else {
       for (int k = k0; k < k1; ++k) {
-        const double r_face = 0.9 * (__ldg(a.div + __ldg(a.eie + k)) + small) / D;
+        const double r_face = mode_div(0.9 * (__ldg(a.div + __ldg(a.eie + k)) + small), D);
         r_min = fmin(r_face, r_min);
       }
     }
@@ -216,7 +218,7 @@ __device__ __forceinline__ void force_elem(const ForceArgs& a, const int e) {
   const double c_length = pow_third(vol);
   // |div|: on the frozen trajectory, the sign recorded with the compression bit
   const double adiv = BR == 2 ? (compress ? -div : div) : fabs(div);
-  const double araw = 20.0 * (c_length * adiv) / (sspd + a.fuzz);
+  const double araw = mode_div(20.0 * (c_length * adiv), sspd + a.fuzz);
   const double alpha = BR == 2 ? ((br & FIERRO_BR_MACH_CLAMP) ? 1.0 : araw) : fmin(1.0, araw);
   if (BR == 1) {
     // the limiter's case, and the neighbour that set r_min on the r_face branch
@@ -249,7 +251,7 @@ __device__ __forceinline__ void force_elem(const ForceArgs& a, const int e) {
     } else if (lim == FIERRO_LIM_FULL) {
       phi = 1.0;
     } else if (lim == FIERRO_LIM_FACE && a.br_sel[e] >= 0) {
-      phi = 1.0 - 0.9 * (__ldg(a.div + a.br_sel[e]) + small) / D;
+      phi = 1.0 - mode_div(0.9 * (__ldg(a.div + a.br_sel[e]) + small), D);
     }  // FIERRO_LIM_IRREGULAR: as evaluated above
   }
   if (TAPE) {
@@ -476,7 +478,7 @@ __device__ __forceinline__ void elem_tile(const ElemArgs& a, const int tile) {
         power = FX_ADD(power, FX_MUL(a.force[(size_t)(l * 3 + 2) * ne + e], __ldg(a.hz + nid[l])));
       }
       const double adt = a.rk_alpha * ctrl->dt;
-      sie1 = a.sie0[e] - FX_MUL(adt / a.mass[e], power);  // not fused: sie1 may cancel sie0
+      sie1 = a.sie0[e] - FX_MUL(mode_div(adt, a.mass[e]), power);  // not fused: sie1 may cancel sie0
       a.sie1[e] = sie1;
     }
     double vol_geo, Sx, Sy, Sz;
@@ -484,7 +486,7 @@ __device__ __forceinline__ void elem_tile(const ElemArgs& a, const int tile) {
     // the priming pass keeps the uploaded volume, as get_divergence reads elem_vol
     const double vol = (KIND == 2) ? a.vol[e] : vol_geo;
     // divergence for the next stage (momentum.cpp:265-286), with this geometry
-    const double inverse_vol = 1.0 / vol;
+    const double inverse_vol = mode_rcp(vol);
     double div = 0.0;
     div = div + Sx * inverse_vol;
     div = div + Sy * inverse_vol;
@@ -494,7 +496,7 @@ __device__ __forceinline__ void elem_tile(const ElemArgs& a, const int tile) {
     if (KIND != 2) {
       a.vol[e] = vol;
       // update_state (properties.cpp:39, 98-109; ideal_gas eos.cpp:35-43)
-      const double den = a.mass[e] / vol;
+      const double den = mode_div(a.mass[e], vol);
       if (STRENGTH) {
         const int mat = a.mat[e];
         if (a.stype[mat] == 2) {
@@ -537,7 +539,7 @@ __device__ __forceinline__ void elem_tile(const ElemArgs& a, const int tile) {
       const double d2min = cfl::min_d2(x, y, z, &s_xyz[0][threadIdx.x], &s_xyz[8][threadIdx.x],
                                        &s_xyz[16][threadIdx.x], kElemBlock);
       const double dist_min = mode_sqrt(d2min);
-      const double dt_l = dt_cfl * dist_min / (sspd + a.fuzz);
+      const double dt_l = mode_div(dt_cfl * dist_min, sspd + a.fuzz);
       dkey = isnan(dt_l) ? 0x7FFFFFFFFFFFFFFFLL : okey(dt_l);
     }
   }
@@ -740,6 +742,69 @@ __global__ void k_reciprocal(const double* __restrict__ in, double* __restrict__
 static void launch_reciprocal(const double* in, double* out, int n, cudaStream_t s) {
   if (n > 0) k_reciprocal<<<blocks_for(n, 256), 256, 0, s>>>(in, out, n);
 }
+// The mode's square and cube roots, quotients and reciprocals (mode_sqrt,
+// mode_cbrt, mode_div, mode_rcp; which 0..3) against the library's on n inputs:
+// eight special values (zero, -0, the smallest subnormal, infinity, NaN, -1, the
+// largest and the smallest normal double), then seeded 2^E (1 + f) with E
+// uniform in [lo_exp, hi_exp] and f's 52 bits uniform (quotients: two such
+// operands of random signs, the special value as the divisor).  out[0] counts
+// results differing, out[1] is the largest difference in ulps, out[2] counts
+// results differing by more than one ulp.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ double seeded_double(unsigned long long h, int lo_exp, int hi_exp, bool sign) {
+  const int E = lo_exp + (int)((h >> 40) % (unsigned long long)(hi_exp - lo_exp + 1));
+  const long long s = sign ? (long long)((mix64(h ^ 0x5555ULL) >> 63) << 63) : 0LL;
+  return __longlong_as_double(s | ((long long)(E + 1023) << 52) | (long long)(mix64(h) & 0xFFFFFFFFFFFFFULL));
+}
+__global__ void __launch_bounds__(256) k_root_check(int which, long long n, unsigned long long seed, int lo_exp,
+                                                    int hi_exp, unsigned long long* out) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const unsigned long long h = mix64(seed ^ (unsigned long long)i * 0xD1B54A32D192ED03ULL);
+    double x;
+    if (i < 8) {
+      const long long special[8] = {0LL, (long long)0x8000000000000000ULL, 1LL, 0x7FF0000000000000LL,
+                                    0x7FF8000000000000LL, (long long)0xBFF0000000000000ULL, 0x7FEFFFFFFFFFFFFFLL,
+                                    0x0010000000000000LL};
+      x = __longlong_as_double(special[i]);
+    } else {
+      x = seeded_double(h, lo_exp, hi_exp, which >= 2);
+    }
+    double a, r;
+    if (which == 0) {
+      a = mode_sqrt(x);
+      r = sqrt(x);
+    } else if (which == 1) {
+      a = mode_cbrt(x);
+      r = cbrt(x);
+    } else if (which == 2) {
+      const double num = seeded_double(mix64(h + 1), lo_exp, hi_exp, true);
+      a = mode_div(num, x);
+      r = num / x;
+    } else {
+      a = mode_rcp(x);
+      r = 1.0 / x;
+    }
+    long long d = __double_as_longlong(a) - __double_as_longlong(r);
+    if (isnan(a) && isnan(r)) d = 0;
+    if (d < 0) d = -d;
+    if (d) {
+      atomicAdd(out, 1ULL);
+      atomicMax(out + 1, (unsigned long long)d);
+      if (d > 1) atomicAdd(out + 2, 1ULL);
+    }
+  }
+}
+static void launch_root_check(int which, long long n, unsigned long long seed, int lo_exp, int hi_exp,
+                              unsigned long long* out, cudaStream_t s) {
+  const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
+  k_root_check<<<(unsigned)blocks, 256, 0, s>>>(which, n, seed, lo_exp, hi_exp, out);
+}
 static void launch_energy(const EnergyArgs& a, cudaStream_t s) {
   const int nb = 512;
   k_energy_part<<<nb, kEnergyBlock, 0, s>>>(a);
@@ -753,7 +818,7 @@ const KernelSet& kernels_fma() {
   static const KernelSet k = {fma_impl::launch_force, fma_impl::launch_force_tape, fma_impl::launch_force_branch, fma_impl::launch_node, fma_impl::launch_elem,
                               fma_impl::launch_dt, fma_impl::launch_end, fma_impl::launch_energy,
                               fma_impl::launch_end_batch, "fma", fma_impl::batch_max_blocks,
-                              fma_impl::launch_reciprocal};
+                              fma_impl::launch_reciprocal, fma_impl::launch_root_check};
   return k;
 }
 #else
@@ -761,7 +826,7 @@ const KernelSet& kernels_exact() {
   static const KernelSet k = {exact_impl::launch_force, exact_impl::launch_force_tape, exact_impl::launch_force_branch, exact_impl::launch_node, exact_impl::launch_elem,
                               exact_impl::launch_dt, exact_impl::launch_end, exact_impl::launch_energy,
                               exact_impl::launch_end_batch, "exact", exact_impl::batch_max_blocks,
-                              exact_impl::launch_reciprocal};
+                              exact_impl::launch_reciprocal, exact_impl::launch_root_check};
   return k;
 }
 #endif

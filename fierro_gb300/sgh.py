@@ -99,6 +99,8 @@ def _load():
     lib.fierro_sgh_run_timed.argtypes = [vp, i64, vp, C.POINTER(C.c_float), C.POINTER(i64)]
     lib.fierro_measure_fp64_rate.argtypes = [C.POINTER(dbl)]
     lib.fierro_fp64_stream_rate.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(dbl)]
+    lib.fierro_root_check.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_ulonglong, C.c_int, C.c_int,
+                                      C.POINTER(C.c_ulonglong)]
     lib.fierro_batch_create.argtypes = [vp, i64, C.c_int, vp, C.POINTER(vp)]
     lib.fierro_batch_destroy.argtypes = [vp]
     lib.fierro_batch_set_state.argtypes = [vp, i64, vp]
@@ -582,6 +584,15 @@ def fp64_stream_rate(chains: int, op: int = 0, threads: int = 256, blocks_per_sm
     r = C.c_double()
     _check(_lib.fierro_fp64_stream_rate(int(chains), int(op), int(threads), int(blocks_per_sm), C.byref(r)))
     return r.value
+
+
+def root_check(fp_mode: int, which: int, n: int, seed: int = 1, lo_exp: int = -1022, hi_exp: int = 1023) -> dict:
+    """fierro_root_check: the mode's square root, cube root, quotient or
+    reciprocal (which 0..3) against the CUDA library's on n inputs (eight special
+    values, then seeded doubles with exponents in [lo_exp, hi_exp])."""
+    out = (C.c_ulonglong * 3)()
+    _check(_lib.fierro_root_check(int(fp_mode), int(which), int(n), int(seed), int(lo_exp), int(hi_exp), out))
+    return {"n": int(n), "differing": int(out[0]), "max_ulp": int(out[1]), "above_one_ulp": int(out[2])}
 
 
 def measure_fp64_rate() -> float:

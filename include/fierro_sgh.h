@@ -322,6 +322,18 @@ int fierro_measure_fp64_rate(double* dfma_per_second);
  * operation (op 0 fma, 1 add, 2 mul), `threads` per block, `blocks_per_sm`
  * blocks per SM; operations per second, best of two timed launches. */
 int fierro_fp64_stream_rate(int chains, int op, int threads, int blocks_per_sm, double* ops_per_second);
+/* The arithmetic mode's square root (which 0), cube root (1), quotient (2) or
+ * reciprocal (3) against the CUDA library's, on the current device (no
+ * counterpart in the reference): n inputs, eight special values (zero, -0, the
+ * smallest subnormal, infinity, NaN, -1, the largest and smallest normal
+ * double; the divisor for a quotient) then seeded 2^E (1 + f), E uniform in
+ * [lo_exp, hi_exp] (within -1022..1023), f's 52 bits uniform (quotients: two such
+ * operands of random signs).  out[0] = results differing, out[1] = the largest
+ * difference in ulps, out[2] = results differing by more than one ulp.  The
+ * exact mode uses the library's functions themselves; the FMA mode its Newton
+ * forms. */
+int fierro_root_check(int fp_mode, int which, long long n, unsigned long long seed, int lo_exp, int hi_exp,
+                      unsigned long long* out);
 
 /* Graphics dumps (write_outputs, outputs.cpp:10-506), written off the critical
  * path.  With outputs on, every write event of the cycle loop -- t = 0 of a

@@ -84,3 +84,29 @@ def test_fp64_rate_probes(lib_built):
         with pytest.raises(sgh.FierroError) as ei:
             sgh.fp64_stream_rate(*bad)
         assert ei.value.code == sgh.FIERRO_EINVAL
+
+
+def test_mode_roots_against_library(lib_built):
+    """The FMA mode's Newton square and cube roots stay within one ulp of the
+    CUDA library's over the whole exponent range and over the range the cycle
+    feeds them (squared speeds and corner-normal lengths, sound speeds, volumes),
+    the square root nearly always equal; its quotients and reciprocals equal the
+    IEEE division's; the exact mode's are the library's own."""
+    from fierro_gb300 import sgh
+    for which in (0, 1, 2, 3):
+        r = sgh.root_check(sgh.FP_EXACT, which, 1 << 20, seed=3)
+        assert r["differing"] == 0, r
+    for lo, hi in ((-1022, 1023), (-90, 8)):
+        n = 1 << 26
+        s = sgh.root_check(sgh.FP_FMA, 0, n, seed=11, lo_exp=lo, hi_exp=hi)
+        assert s["max_ulp"] <= 1 and s["above_one_ulp"] == 0 and s["differing"] <= 1e-5 * n, s
+        c = sgh.root_check(sgh.FP_FMA, 1, n, seed=12, lo_exp=lo, hi_exp=hi)
+        assert c["max_ulp"] <= 1 and c["above_one_ulp"] == 0 and c["differing"] <= 0.15 * n, c
+    for lo, hi in ((-1022, 1023), (-60, 60)):
+        for which in (2, 3):
+            q = sgh.root_check(sgh.FP_FMA, which, 1 << 26, seed=13 + which, lo_exp=lo, hi_exp=hi)
+            assert q["differing"] == 0, q
+    for bad in ((2, 0, 64), (1, 4, 64), (1, 0, 4)):
+        with pytest.raises(sgh.FierroError) as ei:
+            sgh.root_check(*bad)
+        assert ei.value.code == sgh.FIERRO_EINVAL
