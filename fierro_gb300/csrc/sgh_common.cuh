@@ -15,9 +15,45 @@ __device__ __forceinline__ double okey_decode(long long k) {
   return __longlong_as_double(k ^ ((k >> 63) & 0x7FFFFFFFFFFFFFFFLL));
 }
 
-#if FIERRO_FMA
-// Bit-level conversions between doubles and floats for the FMA mode's roots and
-// quotients (integer operations only: no FP64 pipe work).
+// Square roots and quotients by Newton-Raphson iteration from single-precision
+// seeds (Markstein's scheme, "Computation of elementary functions on the IBM
+// RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990), arranged so that
+// most of the work runs on the FP32 and integer pipes: the FP64 pipe bounds
+// these kernels, and GB300 issues FP64 at a small fraction of its FP32 rate.
+//
+// The argument (divisor) is split into a significand m in [1, 4) ([1, 2)) and a
+// power of two by integer operations, and m into a pair of floats mh + ml (its
+// top 24 significand bits, exactly, and the next 29 bits rounded).  A
+// single-precision root y0 (hardware reciprocal square root; ~2^-22 relative) or
+// reciprocal r0 is refined by one Newton step evaluated in single precision on
+// the pair -- the residual m - y0^2 (1 - m r0) formed from the products' exact
+// low parts (fmaf) -- which carries the float pair's sum to ~2^-43.  One FP64
+// Newton step around an exactly formed residual then leaves ~2^-64 (square
+// root) or ~2^-89 (quotient) relative error before the final rounding: three
+// FP64 operations per square root, four per quotient (one reciprocal shared by
+// several quotients: three each), three per reciprocal.  The single-precision
+// steps use the _rn intrinsics, which are never contracted (a fused mh - y0*y0
+// would count the product's low part twice).
+//
+// FMA mode: these results as they are (square roots within an ulp, quotients
+// the IEEE ones but for ~2^-37 of an ulp around rounding boundaries).
+// Exact mode: correctly rounded, so bit for bit the IEEE square root and
+// division.  With the result y (q) within an ulp, the remainder x - y^2
+// (a - b q) is exactly representable and one fma forms it; y is the correctly
+// rounded root iff |x - y^2| < ulp(y) y (up to 2^-52 relative), q the correctly
+// rounded quotient iff |a - b q| < |b| ulp(q) / 2.  The remainder is compared
+// with that bound on the bits, and the result kept only where it lies below the
+// bound by more than 2^-20 of it; elsewhere (about one result in 10^6; above
+// the bound cannot happen within the error above) and where y (q) is a power of
+// two (the ulp below is half the ulp above) the library's operation gives it.  Arguments outside
+// 2^-900 .. 2^900 (square root) or 2^-250 .. 2^251 (quotients), zero, subnormal
+// and non-finite ones included, take the library's operation too (tested on the
+// bits).  FIERRO_LIBRARY_ROOTS / FIERRO_LIBRARY_DIV build either mode with the
+// library's square and cube roots / divisions throughout, for comparison.
+
+constexpr long long kAbsMask = 0x7FFFFFFFFFFFFFFFLL;
+constexpr long long kMantMask = 0x000FFFFFFFFFFFFFLL;
+constexpr long long kHardBand = 1LL << 32;  // 2^-20 relative, on the bits
 
 // Single-precision image of a positive double within float range (truncated).
 __device__ __forceinline__ float f32_image(double d) {
@@ -46,43 +82,17 @@ __device__ __forceinline__ double f64_of_signed(float f) {
                          ((long long)(b & 0x7FFFFF) << 29);
   return __longlong_as_double(e == 0 ? 0LL : bits);
 }
-#endif
 
-#if FIERRO_FMA && !defined(FIERRO_LIBRARY_ROOTS)
-// Square and cube roots of the fused-multiply-add mode (FIERRO_LIBRARY_ROOTS
-// builds the FMA mode with the library's sqrt and cbrt instead, for comparison),
-// by Newton-Raphson iteration from a single-precision seed (Markstein's scheme,
-// "Computation of elementary functions on the IBM RISC System/6000 processor",
-// IBM J. Res. Dev. 34(1), 1990), arranged so that most of the work runs on the
-// FP32 and integer pipes: the FP64 pipe bounds these kernels, and GB300 issues
-// FP64 at a small fraction of its FP32 rate.
-//
-// The argument is split into a significand m in [1, 4) (square root) or [1, 8)
-// (cube root) and a power of two by integer operations, and m into a pair of
-// floats mh + ml (its top 24 significand bits, exactly, and the next 29 bits
-// rounded).  A single-precision root y0 (hardware reciprocal square root, or
-// cbrtf; ~2^-22 relative) is refined by one Newton step evaluated in single
-// precision on the pair: the residual m - y0^2 (m - y0^3) is formed from the
-// products' exact low parts (fmaf), so the step carries y0 + c to ~2^-43.  One
-// FP64 Newton step around an exactly formed residual then reaches ~2^-66 (square
-// root) before the final rounding; the cube root's residual rounds y^2 once, as
-// the two-step form below does.  Three FP64 operations per square root and four
-// per cube root, against six and seven for two FP64 steps from the float seed
-// (FIERRO_ROOTS_FP64_NEWTON).  The single-precision steps use the _rn
-// intrinsics, which are never contracted: a fused mh - y0*y0 would count the
-// product's low part twice.  Zero, negative, subnormal and non-finite arguments
-// take the library's path (tested on the bits, not on the FP64 pipe).
-
-__device__ __forceinline__ double mode_sqrt(double x) {
-  const long long b = __double_as_longlong(x);
-  const int ex = (int)((b >> 52) & 0x7FF);
-  if (b <= 0 || ex == 0 || ex == 0x7FF) return sqrt(x);
+// sqrt(x) to ~2^-64 before the final rounding; b = x's bits, x positive and
+// normal, ex its biased exponent.
+__device__ __forceinline__ double sqrt_newton(double x, long long b, int ex) {
   const int k = (ex - 1023) >> 1;                                      // x = m 4^k
   const double m = __longlong_as_double(b - ((long long)(2 * k) << 52));  // [1, 4)
   const float mh = f32_image(m);
   const float r = rsqrtf(mh);                                          // ~ 1 / sqrt(m)
-#ifdef FIERRO_ROOTS_FP64_NEWTON
   const double h = __longlong_as_double(__double_as_longlong(f64_of(r)) - (1LL << 52));  // r / 2
+#ifdef FIERRO_ROOTS_FP64_NEWTON
+  // the earlier form: two FP64 Newton steps from the float seed
   double y = m * f64_of(r);
   y = fma(h, fma(-y, y, m), y);
   y = fma(h, fma(-y, y, m), y);
@@ -92,12 +102,45 @@ __device__ __forceinline__ double mode_sqrt(double x) {
   const float pe = fmaf(y0, y0, -p);                                   // y0^2 = p + pe exactly
   const float d = __fadd_rn(__fsub_rn(__fsub_rn(mh, p), pe), f32_rest(m));  // m - y0^2 (mh - p exact)
   const float c = __fmul_rn(d, __fmul_rn(0.5f, r));
-  const double h = __longlong_as_double(__double_as_longlong(f64_of(r)) - (1LL << 52));  // r / 2
   double y = __dadd_rn(f64_of(y0), f64_of_signed(c));
   y = fma(h, fma(-y, y, m), y);
 #endif
   return __longlong_as_double(__double_as_longlong(y) + ((long long)k << 52));
 }
+
+// The library's operations for the arguments the Newton forms leave to it, as
+// calls: an inline library operation selected by the exact mode's remainder test
+// was if-converted and ran on every lane (the exact mode's cycle 12 % slower).
+// Zero arguments, frequent in a resting region, return before any FP64 work.
+__device__ __noinline__ double lib_sqrt(double x) { return sqrt(x); }
+__device__ __noinline__ double lib_div(double a, double b) { return a / b; }
+
+#if defined(FIERRO_LIBRARY_ROOTS)
+__device__ __forceinline__ double mode_sqrt(double x) { return sqrt(x); }
+#else
+__device__ __forceinline__ double mode_sqrt(double x) {
+  const long long b = __double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7FF);
+#if FIERRO_FMA
+  if (b <= 0 || ex == 0 || ex == 0x7FF) return (b & kAbsMask) == 0 ? x : lib_sqrt(x);  // sqrt(+-0) = +-0
+  return sqrt_newton(x, b, ex);
+#else
+  if (b <= 0 || (unsigned)(ex - (1023 - 900)) > 1800u) return (b & kAbsMask) == 0 ? x : lib_sqrt(x);
+  const double y = sqrt_newton(x, b, ex);
+  const long long yb = __double_as_longlong(y);
+  const long long tb = yb + ((long long)((int)(yb >> 52) - 1023 - 52) << 52);  // y ulp(y)
+  const long long gap = (__double_as_longlong(fma(-y, y, x)) & kAbsMask) - tb;
+  return (yb & kMantMask) == 0 || gap > -kHardBand ? lib_sqrt(x) : y;
+#endif
+}
+#endif
+
+#if FIERRO_FMA && !defined(FIERRO_LIBRARY_ROOTS)
+// Cube root of the FMA mode, the same way: the float root c0 = cbrtf(mh)
+// refined once on the pair (residual m - c0^3 from the exact low parts of c0^2
+// and c0^3), then one FP64 step whose residual rounds y^2 once (within an ulp of
+// the library's cube root, which is not correctly rounded either).  Four FP64
+// operations.  The exact mode keeps the library's cbrt.
 __device__ __forceinline__ double mode_cbrt(double v) {
   const long long b = __double_as_longlong(v);
   const int ex = (int)((b >> 52) & 0x7FF);
@@ -126,57 +169,76 @@ __device__ __forceinline__ double mode_cbrt(double v) {
   return __longlong_as_double(__double_as_longlong(c) + ((long long)k << 52));
 }
 #else
-__device__ __forceinline__ double mode_sqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ double mode_cbrt(double v) { return cbrt(v); }
 #endif
 
-#if FIERRO_FMA && !defined(FIERRO_LIBRARY_DIV)
-// Quotients and reciprocals of the FMA mode (FIERRO_LIBRARY_DIV builds it with
-// the library's IEEE division instead, for comparison), by the same scheme as
-// the roots above (Markstein's): the single-precision reciprocal of the
-// divisor's truncated image, refined by one Newton step on the float pair
-// b = bh + bl (the residual 1 - b r0 from the product's exact low part), gives
-// 1/b to ~2^-45 as the sum of two floats; one FMA correction around the exactly
-// formed residual a - b q0 then leaves ~2^-90 relative error before the final
-// rounding, so the result is the correctly rounded quotient except where the
-// exact one lies within ~2^-37 ulp of a rounding boundary.  Four FP64 operations
-// per quotient and three per reciprocal.  Operands outside 2^-500 .. 2^500 in
-// magnitude (zero, subnormal, non-finite included) take the library's division
-// (tested on the bits).
-
-// 1/|b| 2^eb ~ 1/|b'| for b' = b scaled into [1, 2): the float pair's sum as a
-// double, scaled back by 2^-eb with b's sign; b normal.
+// 2^-250 <= |x| < 2^251: the operands of the Newton quotients.
+__device__ __forceinline__ bool plain_range(long long bits) {
+  return (unsigned)((bits >> 52) & 0x7FF) - 773u <= 500u;
+}
+// ~ 1/b to ~2^-44: the float pair's sum for b's significand bm in [1, 2) as a
+// double, scaled by b's power of two and given b's sign (b within plain_range).
 __device__ __forceinline__ double rcp_seed(long long bb) {
   const int eb = (int)((bb >> 52) & 0x7FF) - 1023;
-  const double bm = __longlong_as_double((bb & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL);  // [1, 2)
+  const double bm = __longlong_as_double((bb & kMantMask) | 0x3FF0000000000000LL);  // [1, 2)
   const float bh = f32_image(bm);
   const float r0 = __frcp_rn(bh);
   const float p = __fmul_rn(bh, r0);
   const float pe = fmaf(bh, r0, -p);                                    // bh r0 = p + pe exactly
   const float e = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, p), pe), __fmul_rn(f32_rest(bm), r0));  // 1 - bm r0
   const double r = __dadd_rn(f64_of(r0), f64_of_signed(__fmul_rn(r0, e)));
-  return __longlong_as_double((__double_as_longlong(r) - ((long long)eb << 52)) ^ (bb & (long long)0x8000000000000000ULL));
+  return __longlong_as_double((__double_as_longlong(r) - ((long long)eb << 52)) ^ (bb & ~kAbsMask));
 }
-__device__ __forceinline__ bool plain_range(long long bits) {
-  return (unsigned)((bits >> 52) & 0x7FF) - 523u <= 1000u;  // 2^-500 <= |x| < 2^501
-}
-__device__ __forceinline__ double mode_div(double a, double b) {
-  const long long ab = __double_as_longlong(a), bb = __double_as_longlong(b);
-  if (!plain_range(ab) || !plain_range(bb)) return a / b;
-  const double r = rcp_seed(bb);
-  const double q0 = a * r;
-  return fma(fma(-b, q0, a), r, q0);
-}
-__device__ __forceinline__ double mode_rcp(double b) {
+// A divisor prepared once for the quotients that share it.
+struct Divisor {
+  double b, r;
+  bool plain;
+};
+__device__ __forceinline__ Divisor divisor(double b) {
   const long long bb = __double_as_longlong(b);
-  if (!plain_range(bb)) return 1.0 / b;
-  const double r = rcp_seed(bb);
-  return fma(fma(-b, r, 1.0), r, r);
+  return Divisor{b, rcp_seed(bb), plain_range(bb)};
 }
+// The exact mode's test of a Newton quotient q of a / b: false only where q is
+// the correctly rounded quotient (see above).
+__device__ __forceinline__ bool quot_hard(double a, double b, double q) {
+  const long long qb = __double_as_longlong(q);
+  const int eq = (int)((qb >> 52) & 0x7FF) - 1023;
+  const long long tb = (__double_as_longlong(b) & kAbsMask) + ((long long)(eq - 53) << 52);  // |b| ulp(q) / 2
+  const long long gap = (__double_as_longlong(fma(-b, q, a)) & kAbsMask) - tb;
+  return (qb & kMantMask) == 0 || gap > -kHardBand;
+}
+__device__ __forceinline__ double quot(double a, const Divisor& d) {
+#ifdef FIERRO_LIBRARY_DIV
+  return a / d.b;
 #else
-__device__ __forceinline__ double mode_div(double a, double b) { return a / b; }
-__device__ __forceinline__ double mode_rcp(double b) { return 1.0 / b; }
+  const long long ab = __double_as_longlong(a);
+  if (!d.plain || !plain_range(ab))  // +-0 / b: the signed zero a r
+    return d.plain && (ab & kAbsMask) == 0 ? a * d.r : lib_div(a, d.b);
+  const double q0 = a * d.r;
+  const double q = fma(fma(-d.b, q0, a), d.r, q0);
+#if FIERRO_FMA
+  return q;
+#else
+  return quot_hard(a, d.b, q) ? lib_div(a, d.b) : q;
 #endif
+#endif
+}
+__device__ __forceinline__ double mode_div(double a, double b) { return quot(a, divisor(b)); }
+__device__ __forceinline__ double mode_rcp(double b) {
+#ifdef FIERRO_LIBRARY_DIV
+  return 1.0 / b;
+#else
+  const long long bb = __double_as_longlong(b);
+  if (!plain_range(bb)) return lib_div(1.0, b);
+  const double r = rcp_seed(bb);
+  const double q = fma(fma(-b, r, 1.0), r, r);
+#if FIERRO_FMA
+  return q;
+#else
+  return quot_hard(1.0, b, q) ? lib_div(1.0, b) : q;
+#endif
+#endif
+}
 
 // pow(v, 1.0/3.0) as the reference computes it (force_sgh.cpp:319-320).
 // The exponent is fl(1/3) = 1/3 - d, d = 2^-54/3, so the target is

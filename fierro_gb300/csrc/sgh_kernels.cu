@@ -181,9 +181,10 @@ __device__ __forceinline__ void force_elem(const ForceArgs& a, const int e) {
     vstar1 = s1 * rs3;
     vstar2 = s2 * rs3;
 #else
-    vstar0 = s0 / s3;
-    vstar1 = s1 / s3;
-    vstar2 = s2 / s3;
+    const Divisor ds3 = divisor(s3);  // three correctly rounded quotients, one reciprocal seed
+    vstar0 = quot(s0, ds3);
+    vstar1 = quot(s1, ds3);
+    vstar2 = quot(s2, ds3);
 #endif
   }
   // shock detector (:287-315): r_face = 0.9 (div_nb + small) / (div + small) is
@@ -396,10 +397,10 @@ __device__ __forceinline__ void node_update(const NodeArgs& a, const int n) {
   double v1 = v0 + adt * f1 * rm;
   double w1 = w0 + adt * f2 * rm;
 #else
-  const double m = a.node_mass[n];
-  double u1 = u0 + adt * f0 / m;
-  double v1 = v0 + adt * f1 / m;
-  double w1 = w0 + adt * f2 / m;
+  const Divisor m = divisor(a.node_mass[n]);  // correctly rounded quotients, one reciprocal seed
+  double u1 = u0 + quot(adt * f0, m);
+  double v1 = v0 + quot(adt * f1, m);
+  double w1 = w0 + quot(adt * f2, m);
 #endif
   const unsigned bc = a.bc_mask[n];
   if (bc & 1u) u1 = 0.0;
@@ -743,13 +744,21 @@ static void launch_reciprocal(const double* in, double* out, int n, cudaStream_t
   if (n > 0) k_reciprocal<<<blocks_for(n, 256), 256, 0, s>>>(in, out, n);
 }
 // The mode's square and cube roots, quotients and reciprocals (mode_sqrt,
-// mode_cbrt, mode_div, mode_rcp; which 0..3) against the library's on n inputs:
+// mode_cbrt, mode_div, mode_rcp) against the library's on n inputs.  which 0..3:
 // eight special values (zero, -0, the smallest subnormal, infinity, NaN, -1, the
 // largest and the smallest normal double), then seeded 2^E (1 + f) with E
 // uniform in [lo_exp, hi_exp] and f's 52 bits uniform (quotients: two such
-// operands of random signs, the special value as the divisor).  out[0] counts
-// results differing, out[1] is the largest difference in ulps, out[2] counts
-// results differing by more than one ulp.
+// operands of random signs, the special value as the divisor, signed zeros as
+// the dividend of the next eight).  which 4..6: the
+// square root, quotient and reciprocal on arguments whose exact result lies
+// within 2^-55 .. 2^-13 of an ulp of a rounding boundary (scaled by random
+// powers of two): 4^s (1 + (2k+1) 2^-52) and 4^s (1 - (2k+1) 2^-53), whose
+// square roots lie just below the midpoints 4^s/2^s (1 + (2k+1) 2^-53) and
+// 2^s (1 - (2k+1) 2^-54); 2^s (1 - (2k+1) 2^-53), whose reciprocal lies just
+// above the midpoint 2^-s (1 + (2k+1) 2^-53); and 2^t (1 + m 2^-52) / that,
+// just above a midpoint too (k < 2^20, m < 2^16).  out[0] counts results
+// differing, out[1] is the largest difference in ulps, out[2] counts results
+// differing by more than one ulp.
 __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
   z += 0x9E3779B97F4A7C15ULL;
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
@@ -766,24 +775,35 @@ __global__ void __launch_bounds__(256) k_root_check(int which, long long n, unsi
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
     const unsigned long long h = mix64(seed ^ (unsigned long long)i * 0xD1B54A32D192ED03ULL);
+    const long long odd = 2 * (long long)((unsigned long long)i & 0xFFFFF) + 1;  // 2k + 1, k < 2^20
+    const int s = (int)((h >> 40) % 201) - 100;                                  // a power of two in +-100
     double x;
-    if (i < 8) {
+    if (which >= 4) {
+      if (which == 4)
+        x = __longlong_as_double((i & 1) ? ((long long)(1023 + 2 * s) << 52) - odd
+                                         : ((long long)(1023 + 2 * s) << 52) | odd);
+      else
+        x = __longlong_as_double(((long long)(1023 + s) << 52) - odd);
+    } else if (i < 8) {
       const long long special[8] = {0LL, (long long)0x8000000000000000ULL, 1LL, 0x7FF0000000000000LL,
                                     0x7FF8000000000000LL, (long long)0xBFF0000000000000ULL, 0x7FEFFFFFFFFFFFFFLL,
                                     0x0010000000000000LL};
       x = __longlong_as_double(special[i]);
     } else {
-      x = seeded_double(h, lo_exp, hi_exp, which >= 2);
+      x = seeded_double(h, lo_exp, hi_exp, which == 2 || which == 3);
     }
     double a, r;
-    if (which == 0) {
+    if (which == 0 || which == 4) {
       a = mode_sqrt(x);
       r = sqrt(x);
     } else if (which == 1) {
       a = mode_cbrt(x);
       r = cbrt(x);
-    } else if (which == 2) {
-      const double num = seeded_double(mix64(h + 1), lo_exp, hi_exp, true);
+    } else if (which == 2 || which == 5) {
+      const int t = (int)((mix64(h + 7) >> 40) % 201) - 100;
+      double num = which == 2 ? seeded_double(mix64(h + 1), lo_exp, hi_exp, true)
+                              : __longlong_as_double(((long long)(1023 + t) << 52) | (long long)(h & 0xFFFF));
+      if (which == 2 && i >= 8 && i < 16) num = (i & 1) ? -0.0 : 0.0;  // signed zeros over seeded divisors
       a = mode_div(num, x);
       r = num / x;
     } else {

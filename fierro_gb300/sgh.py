@@ -589,7 +589,8 @@ def fp64_stream_rate(chains: int, op: int = 0, threads: int = 256, blocks_per_sm
 def root_check(fp_mode: int, which: int, n: int, seed: int = 1, lo_exp: int = -1022, hi_exp: int = 1023) -> dict:
     """fierro_root_check: the mode's square root, cube root, quotient or
     reciprocal (which 0..3) against the CUDA library's on n inputs (eight special
-    values, then seeded doubles with exponents in [lo_exp, hi_exp])."""
+    values, then seeded doubles with exponents in [lo_exp, hi_exp]); which 4..6:
+    square roots, quotients and reciprocals next to rounding boundaries."""
     out = (C.c_ulonglong * 3)()
     _check(_lib.fierro_root_check(int(fp_mode), int(which), int(n), int(seed), int(lo_exp), int(hi_exp), out))
     return {"n": int(n), "differing": int(out[0]), "max_ulp": int(out[1]), "above_one_ulp": int(out[2])}

@@ -328,10 +328,12 @@ int fierro_fp64_stream_rate(int chains, int op, int threads, int blocks_per_sm, 
  * smallest subnormal, infinity, NaN, -1, the largest and smallest normal
  * double; the divisor for a quotient) then seeded 2^E (1 + f), E uniform in
  * [lo_exp, hi_exp] (within -1022..1023), f's 52 bits uniform (quotients: two such
- * operands of random signs).  out[0] = results differing, out[1] = the largest
- * difference in ulps, out[2] = results differing by more than one ulp.  The
- * exact mode uses the library's functions themselves; the FMA mode its Newton
- * forms. */
+ * operands of random signs).  which 4, 5, 6: the square root, quotient and
+ * reciprocal on arguments whose exact result lies just off a rounding boundary
+ * (the hard cases of correct rounding).  out[0] = results differing, out[1] =
+ * the largest difference in ulps, out[2] = results differing by more than one
+ * ulp.  The exact mode's square roots and quotients are correctly rounded (0
+ * differing); the FMA mode's are within an ulp. */
 int fierro_root_check(int fp_mode, int which, long long n, unsigned long long seed, int lo_exp, int hi_exp,
                       unsigned long long* out);
 

@@ -87,26 +87,34 @@ def test_fp64_rate_probes(lib_built):
 
 
 def test_mode_roots_against_library(lib_built):
-    """The FMA mode's Newton square and cube roots stay within one ulp of the
-    CUDA library's over the whole exponent range and over the range the cycle
-    feeds them (squared speeds and corner-normal lengths, sound speeds, volumes),
-    the square root nearly always equal; its quotients and reciprocals equal the
-    IEEE division's; the exact mode's are the library's own."""
+    """The arithmetic modes' square roots, cube roots, quotients and reciprocals
+    against the CUDA library's.  Exact mode: bit for bit (its Newton square
+    roots and quotients are correctly rounded, with the library's operation
+    where the remainder test cannot decide), also on arguments whose result lies
+    within a tiny fraction of an ulp of a rounding boundary.  FMA mode: square
+    and cube roots within one ulp over the whole exponent range and over the
+    range the cycle feeds them, the square root nearly always equal; quotients
+    and reciprocals equal to the IEEE ones but within one ulp next to a
+    rounding boundary."""
     from fierro_gb300 import sgh
-    for which in (0, 1, 2, 3):
-        r = sgh.root_check(sgh.FP_EXACT, which, 1 << 20, seed=3)
-        assert r["differing"] == 0, r
+    n = 1 << 26
     for lo, hi in ((-1022, 1023), (-90, 8)):
-        n = 1 << 26
+        for which in (0, 1, 2, 3):
+            r = sgh.root_check(sgh.FP_EXACT, which, n, seed=3 + which, lo_exp=lo, hi_exp=hi)
+            assert r["differing"] == 0, (which, lo, r)
         s = sgh.root_check(sgh.FP_FMA, 0, n, seed=11, lo_exp=lo, hi_exp=hi)
         assert s["max_ulp"] <= 1 and s["above_one_ulp"] == 0 and s["differing"] <= 1e-5 * n, s
         c = sgh.root_check(sgh.FP_FMA, 1, n, seed=12, lo_exp=lo, hi_exp=hi)
         assert c["max_ulp"] <= 1 and c["above_one_ulp"] == 0 and c["differing"] <= 0.15 * n, c
-    for lo, hi in ((-1022, 1023), (-60, 60)):
         for which in (2, 3):
-            q = sgh.root_check(sgh.FP_FMA, which, 1 << 26, seed=13 + which, lo_exp=lo, hi_exp=hi)
-            assert q["differing"] == 0, q
-    for bad in ((2, 0, 64), (1, 4, 64), (1, 0, 4)):
+            q = sgh.root_check(sgh.FP_FMA, which, n, seed=13 + which, lo_exp=lo, hi_exp=hi)
+            assert q["differing"] == 0, (which, lo, q)
+    for which in (4, 5, 6):
+        r = sgh.root_check(sgh.FP_EXACT, which, 1 << 24, seed=21 + which)
+        assert r["differing"] == 0, (which, r)
+        f = sgh.root_check(sgh.FP_FMA, which, 1 << 24, seed=21 + which)
+        assert f["max_ulp"] <= 1, (which, f)
+    for bad in ((2, 0, 64), (1, 7, 64), (1, 0, 4)):
         with pytest.raises(sgh.FierroError) as ei:
             sgh.root_check(*bad)
         assert ei.value.code == sgh.FIERRO_EINVAL
