@@ -37,18 +37,24 @@ __device__ __forceinline__ double okey_decode(long long k) {
 //
 // FMA mode: these results as they are (square roots within an ulp, quotients
 // the IEEE ones but for ~2^-37 of an ulp around rounding boundaries).
-// Exact mode: correctly rounded, so bit for bit the IEEE square root and
-// division.  With the result y (q) within an ulp, the remainder x - y^2
-// (a - b q) is exactly representable and one fma forms it; y is the correctly
-// rounded root iff |x - y^2| < ulp(y) y (up to 2^-52 relative), q the correctly
-// rounded quotient iff |a - b q| < |b| ulp(q) / 2.  The remainder is compared
-// with that bound on the bits, and the result kept only where it lies below the
-// bound by more than 2^-20 of it; elsewhere (about one result in 10^6; above
-// the bound cannot happen within the error above) and where y (q) is a power of
-// two (the ulp below is half the ulp above) the library's operation gives it.  Arguments outside
-// 2^-900 .. 2^900 (square root) or 2^-250 .. 2^251 (quotients), zero, subnormal
-// and non-finite ones included, take the library's operation too (tested on the
-// bits).  FIERRO_LIBRARY_ROOTS / FIERRO_LIBRARY_DIV build either mode with the
+// Exact mode (square roots, and quotients that share a divisor): correctly
+// rounded, so bit for bit the IEEE square root and division.  With the result
+// y (q) within an ulp, the remainder x - y^2 (a - b q) is exactly representable
+// and one fma forms it; y is the correctly rounded root iff |x - y^2| < ulp(y) y
+// (up to 2^-52 relative), q the correctly rounded quotient iff
+// |a - b q| < |b| ulp(q) / 2.  The remainder is compared with that bound on the
+// bits, and the result kept only where it lies below the bound by more than
+// 2^-20 of it; elsewhere (about one result in 10^6; above the bound cannot
+// happen within the error above) and where y (q) is a power of two (the ulp
+// below is half the ulp above) the library's operation gives it.
+//
+// Arguments outside 2^-900 .. 2^900 (square root) or 2^-250 .. 2^251
+// (quotients), zero, subnormal and non-finite ones included, take the library's
+// operation too (tested on the bits); zeros, frequent in a resting region,
+// return before any FP64 work.  The library's operations are reached through
+// calls: inline under the exact mode's data-dependent test they were
+// if-converted and ran on every lane (the exact cycle 12 % slower).
+// FIERRO_LIBRARY_ROOTS / FIERRO_LIBRARY_DIV build either mode with the
 // library's square and cube roots / divisions throughout, for comparison.
 
 constexpr long long kAbsMask = 0x7FFFFFFFFFFFFFFFLL;
@@ -108,10 +114,7 @@ __device__ __forceinline__ double sqrt_newton(double x, long long b, int ex) {
   return __longlong_as_double(__double_as_longlong(y) + ((long long)k << 52));
 }
 
-// The library's operations for the arguments the Newton forms leave to it, as
-// calls: an inline library operation selected by the exact mode's remainder test
-// was if-converted and ran on every lane (the exact mode's cycle 12 % slower).
-// Zero arguments, frequent in a resting region, return before any FP64 work.
+// The library's operations for the arguments the Newton forms leave to it.
 __device__ __noinline__ double lib_sqrt(double x) { return sqrt(x); }
 __device__ __noinline__ double lib_div(double a, double b) { return a / b; }
 
@@ -223,20 +226,23 @@ __device__ __forceinline__ double quot(double a, const Divisor& d) {
 #endif
 #endif
 }
+// A single quotient or reciprocal: the Newton form in the FMA mode; the
+// library's division in the exact mode, where the remainder test makes the
+// Newton form no cheaper unless several quotients share the divisor's seed
+// (measured: the exact element pass 1.4 % faster with the library's).
+#if FIERRO_FMA
 __device__ __forceinline__ double mode_div(double a, double b) { return quot(a, divisor(b)); }
+#else
+__device__ __forceinline__ double mode_div(double a, double b) { return a / b; }
+#endif
 __device__ __forceinline__ double mode_rcp(double b) {
-#ifdef FIERRO_LIBRARY_DIV
+#if defined(FIERRO_LIBRARY_DIV) || !FIERRO_FMA
   return 1.0 / b;
 #else
   const long long bb = __double_as_longlong(b);
   if (!plain_range(bb)) return lib_div(1.0, b);
   const double r = rcp_seed(bb);
-  const double q = fma(fma(-b, r, 1.0), r, r);
-#if FIERRO_FMA
-  return q;
-#else
-  return quot_hard(1.0, b, q) ? lib_div(1.0, b) : q;
-#endif
+  return fma(fma(-b, r, 1.0), r, r);
 #endif
 }
 

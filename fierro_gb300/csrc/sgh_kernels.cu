@@ -744,7 +744,7 @@ static void launch_reciprocal(const double* in, double* out, int n, cudaStream_t
   if (n > 0) k_reciprocal<<<blocks_for(n, 256), 256, 0, s>>>(in, out, n);
 }
 // The mode's square and cube roots, quotients and reciprocals (mode_sqrt,
-// mode_cbrt, mode_div, mode_rcp) against the library's on n inputs.  which 0..3:
+// mode_cbrt, quot, mode_rcp) against the library's on n inputs.  which 0..3:
 // eight special values (zero, -0, the smallest subnormal, infinity, NaN, -1, the
 // largest and the smallest normal double), then seeded 2^E (1 + f) with E
 // uniform in [lo_exp, hi_exp] and f's 52 bits uniform (quotients: two such
@@ -804,7 +804,7 @@ __global__ void __launch_bounds__(256) k_root_check(int which, long long n, unsi
       double num = which == 2 ? seeded_double(mix64(h + 1), lo_exp, hi_exp, true)
                               : __longlong_as_double(((long long)(1023 + t) << 52) | (long long)(h & 0xFFFF));
       if (which == 2 && i >= 8 && i < 16) num = (i & 1) ? -0.0 : 0.0;  // signed zeros over seeded divisors
-      a = mode_div(num, x);
+      a = quot(num, divisor(x));  // the shared-divisor form (mode_div in the FMA mode)
       r = num / x;
     } else {
       a = mode_rcp(x);

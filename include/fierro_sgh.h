@@ -333,7 +333,8 @@ int fierro_fp64_stream_rate(int chains, int op, int threads, int blocks_per_sm, 
  * (the hard cases of correct rounding).  out[0] = results differing, out[1] =
  * the largest difference in ulps, out[2] = results differing by more than one
  * ulp.  The exact mode's square roots and quotients are correctly rounded (0
- * differing); the FMA mode's are within an ulp. */
+ * differing; its reciprocals and cube roots are the library's); the FMA mode's
+ * are within an ulp. */
 int fierro_root_check(int fp_mode, int which, long long n, unsigned long long seed, int lo_exp, int hi_exp,
                       unsigned long long* out);
 
