@@ -225,11 +225,11 @@ def alg_bytes(kind: str, nn: int, ne: int, nnz: int) -> float:
 DRAM_PER_ELEM = {"k_force": (848042752 + 371475456) / 2097152,
                  "k_elem": (716690688 + 467264768 + 717134848 + 465028608) / 2 / 2097152}
 NCU_PER_ELEM = {"exact": {
-    "k_force": {"fp64_ops": 138412032 / 262144, "dram_bytes": DRAM_PER_ELEM["k_force"]},
-    "k_elem": {"fp64_ops": (158072832 + 171509792) / 2 / 262144, "dram_bytes": DRAM_PER_ELEM["k_elem"]},
+    "k_force": {"fp64_ops": 124518424 / 262144, "dram_bytes": DRAM_PER_ELEM["k_force"]},
+    "k_elem": {"fp64_ops": (157286400 + 169936928) / 2 / 262144, "dram_bytes": DRAM_PER_ELEM["k_elem"]},
 }, "fma": {
-    "k_force": {"fp64_ops": 104333312 / 262144, "dram_bytes": DRAM_PER_ELEM["k_force"]},
-    "k_elem": {"fp64_ops": (130285568 + 142668312) / 2 / 262144, "dram_bytes": DRAM_PER_ELEM["k_elem"]},
+    "k_force": {"fp64_ops": 88342528 / 262144, "dram_bytes": DRAM_PER_ELEM["k_force"]},
+    "k_elem": {"fp64_ops": (127926272 + 137425432) / 2 / 262144, "dram_bytes": DRAM_PER_ELEM["k_elem"]},
 }}
 
 
@@ -920,10 +920,10 @@ def outputs_bench(args):
 # capture of the 64^3 case (exact mode, mean of the two RK-stage launches): hypo
 # k_force<0,0,1>, hyper k_elem<*,0,1>.
 NCU_PER_ELEM_STRENGTH = {
-    ("hypo", "k_force"): {"fp64_ops": (233308160 + 214695936) / 2 / 262144,
-                          "dram_bytes": (125.731072e6 + 36.583424e6 + 145.0176e6 + 37.52832e6) / 2 / 262144},
-    ("hyper", "k_elem"): {"fp64_ops": (207093760 + 220530720) / 2 / 262144,
-                          "dram_bytes": (109.706496e6 + 43.420928e6 + 109.884416e6 + 43.996672e6) / 2 / 262144},
+    ("hypo", "k_force"): {"fp64_ops": (195035144 + 200802328) / 2 / 262144,
+                          "dram_bytes": (125629952 + 36976128 + 144625152 + 37889536) / 2 / 262144},
+    ("hyper", "k_elem"): {"fp64_ops": (206307328 + 218957856) / 2 / 262144,
+                          "dram_bytes": (109707008 + 43060480 + 109892864 + 43815680) / 2 / 262144},
 }
 
 

@@ -50,8 +50,10 @@ __device__ __forceinline__ double okey_decode(long long k) {
 //
 // Arguments outside 2^-900 .. 2^900 (square root) or 2^-250 .. 2^251
 // (quotients), zero, subnormal and non-finite ones included, take the library's
-// operation too (tested on the bits); zeros, frequent in a resting region,
-// return before any FP64 work.  The library's operations are reached through
+// operation too (tested on the bits); zeros are returned as they are (their
+// root is themselves; a 256^3 Sedov cycle, most of whose mesh is at rest, and a
+// Noh cycle, where every node moves, take the same time).  The library's
+// operations are reached through
 // calls: inline under the exact mode's data-dependent test they were
 // if-converted and ran on every lane (the exact cycle 12 % slower).
 // FIERRO_LIBRARY_ROOTS / FIERRO_LIBRARY_DIV build either mode with the
