@@ -2,8 +2,10 @@
 // Explicit-Lagrange-Kokkos/SGH_solver on quad meshes (x axial, y radial).
 //
 // Compiled twice, like sgh_kernels.cu: FIERRO_FMA=0 with --fmad=false (every
-// operation the reference's, in its order) and FIERRO_FMA=1 (contraction and
-// reciprocal reuse allowed).
+// operation the reference's, in its order; square roots and shared-divisor
+// quotients by the correctly rounded Newton forms of sgh_common.cuh) and
+// FIERRO_FMA=1 (contraction and reciprocal reuse allowed; the Newton square
+// roots, quotients and reciprocals).
 //
 // One cycle is 2 + 4*rk_num_stages launches: k_dt, then per RK stage
 //   k_force_rz (elements)  corner normals, area and Barlow corner areas of the
@@ -207,12 +209,13 @@ __global__ void __launch_bounds__(kRzBlock) k_force_rz(const RzForceArgs a) {
   double vstar0 = 0.0, vstar1 = 0.0;
   if (s3 > a.fuzz) {
 #if FIERRO_FMA
-    const double rs = 1.0 / s3;
+    const double rs = mode_rcp(s3);
     vstar0 = s0 * rs;
     vstar1 = s1 * rs;
 #else
-    vstar0 = s0 / s3;
-    vstar1 = s1 / s3;
+    const Divisor ds3 = divisor(s3);  // correctly rounded quotients, one reciprocal seed
+    vstar0 = quot(s0, ds3);
+    vstar1 = quot(s1, ds3);
 #endif
   }
   // shock detector (:653-690): the minimum over neighbours of the monotone
@@ -231,11 +234,11 @@ __global__ void __launch_bounds__(kRzBlock) k_force_rz(const RzForceArgs a) {
   if (k1 > k0) {
     const double dsel = okey_decode(D > 0 ? kmin : kmax);
     if (isfinite(D) && D != 0.0 && isfinite(dsel)) {
-      const double r_face = 0.9 * (dsel + small) / D;
+      const double r_face = mode_div(0.9 * (dsel + small), D);
       r_min = okey(r_face) < okey(1.0) ? r_face : 1.0;
     } else {
       for (int k = k0; k < k1; ++k) {
-        const double r_face = 0.9 * (__ldg(a.div + __ldg(a.eie + k)) + small) / D;
+        const double r_face = mode_div(0.9 * (__ldg(a.div + __ldg(a.eie + k)) + small), D);
         r_min = fmin(r_face, r_min);
       }
     }
@@ -243,7 +246,7 @@ __global__ void __launch_bounds__(kRzBlock) k_force_rz(const RzForceArgs a) {
   double phi = 1.0 - fmax(0.0, r_min);
   // Mach-number detector with the characteristic length sqrt(area) (:692-700)
   const double c_length = mode_sqrt(area);
-  const double alpha = fmin(1.0, 20.0 * (c_length * fabs(div)) / (sspd + a.fuzz));
+  const double alpha = fmin(1.0, mode_div(20.0 * (c_length * fabs(div)), sspd + a.fuzz));
   phi = alpha * phi;
   // corner forces with the inward normals -B, then the hoop-stress terms (:718-755)
   const double vs[2] = {vstar0, vstar1};
@@ -317,12 +320,13 @@ __global__ void __launch_bounds__(kRzNodeBlock) k_node_rz(const RzNodeArgs a) {
   const double m = a.node_mass[n];
   const double u0 = a.u0[n], v0 = a.v0[n];
 #if FIERRO_FMA
-  const double rm = 1.0 / m;
+  const double rm = mode_rcp(m);
   double u1 = u0 + adt * f0 * rm;
   double v1 = v0 + adt * f1 * rm;
 #else
-  double u1 = u0 + adt * f0 / m;
-  double v1 = v0 + adt * f1 / m;
+  const Divisor dm = divisor(m);  // correctly rounded quotients, one reciprocal seed
+  double u1 = u0 + quot(adt * f0, dm);
+  double v1 = v0 + quot(adt * f1, dm);
 #endif
   const unsigned bc = a.bc_mask[n];
   if (bc & 1u) u1 = 0.0;
@@ -390,7 +394,7 @@ __global__ void __launch_bounds__(kRzBlock) k_elem_rz(const RzElemArgs a) {
         power = power + a.force[(size_t)(l * 2 + 1) * ne + e] * r * __ldg(a.hy + nid[l]);
       }
       const double adt = a.rk_alpha * ctrl->dt;
-      sie1 = a.sie0[e] - adt / a.mass[e] * power;
+      sie1 = a.sie0[e] - mode_div(adt, a.mass[e]) * power;
       a.sie1[e] = sie1;
     }
     const double vol = (KIND == 2) ? a.vol[e] : rz_vol(x, y);
@@ -398,19 +402,19 @@ __global__ void __launch_bounds__(kRzBlock) k_elem_rz(const RzElemArgs a) {
     double B[4][2];
     rz_bmatrix(x, y, B);
     const double area = rz_area(x, y);
-    const double inverse_area = 1.0 / area;
-    const double mean_radius = vol / area;
+    const double inverse_area = mode_rcp(area);
+    const double mean_radius = mode_div(vol, area);
     const double elem_vel_r = 0.25 * (v[0] + v[1] + v[2] + v[3]);
     double div = 0.0;
     div = div + (u[0] * B[0][0] + u[1] * B[1][0] + u[2] * B[2][0] + u[3] * B[3][0]) * inverse_area;
     div = div + ((v[0] * B[0][1] + v[1] * B[1][1] + v[2] * B[2][1] + v[3] * B[3][1]) * inverse_area +
-                 elem_vel_r / mean_radius);
+                 mode_div(elem_vel_r, mean_radius));
     a.div[e] = div;
     double sspd;
     if (KIND != 2) {
       a.vol[e] = vol;
       // update_state2D (properties.cpp:140, eos.cpp:12-46)
-      const double den = a.mass[e] / vol;
+      const double den = mode_div(a.mass[e], vol);
       const double gamma = a.gamma[e], csmin = a.csmin[e];
       const double pres = (gamma - 1.0) * sie1 * den;
       sspd = mode_sqrt(gamma * (gamma - 1.0) * sie1);
@@ -438,7 +442,7 @@ __global__ void __launch_bounds__(kRzBlock) k_elem_rz(const RzElemArgs a) {
           first = false;
         }
       const double dist_min = mode_sqrt(d2);
-      const double dt_l = a.dt_cfl * dist_min / (sspd + a.fuzz);
+      const double dt_l = mode_div(a.dt_cfl * dist_min, sspd + a.fuzz);
       dkey = isnan(dt_l) ? 0x7FFFFFFFFFFFFFFFLL : okey(dt_l);
     }
   }
