@@ -5,7 +5,9 @@
 // minimum) comes out bit-identical to what the cycle kernels computed, so the
 // reverse pass takes exactly the forward run's branches.  The adjoint's own sums
 // have no parity target; they are deterministic (fixed orders, no atomics on
-// floating-point values).
+// floating-point values), and their reciprocals and reciprocal square roots are
+// the ~2^-43 float-pair forms of sgh_common.cuh (fast_rcp, fast_rsqrt: one FP64
+// operation each).
 //
 // Per RK stage the reverse pass is three launches, mirroring the forward ones in
 // reverse order:
@@ -121,7 +123,7 @@ __device__ __forceinline__ void eos_fold(double den, double sie, double gamma, d
   gb += presb * sie * den;
   const double raw = sqrt(gamma * (gamma - 1.0) * sie);
   if (!(raw < csmin) && raw > 0.0) {
-    const double t = sspdb / (2.0 * raw);
+    const double t = sspdb * fast_rcp(2.0 * raw);
     sieb += t * gamma * (gamma - 1.0);
     gb += t * (2.0 * gamma - 1.0) * sie;
   }
@@ -225,7 +227,7 @@ __global__ void __launch_bounds__(256) k_adj_seed(const AdjMesh m, const AdjBufs
     double volb = (mask & 16u) ? eseed[4 * (size_t)ne + e] : 0.0;
     double gb = 0.0;
     eos_fold(den, f.sie[e], m.gamma[e], m.csmin[e], presb, sspdb, sieb, denb, gb);
-    volb -= denb * den / vol;  // den = M / vol
+    volb -= denb * den * fast_rcp(vol);  // den = M / vol
     b.volbar[e] = volb;
     b.divbar[e] = 0.0;
     b.nbv[e] = 0.0;
@@ -275,7 +277,7 @@ __global__ void __launch_bounds__(kAdjElemBlock) k_adj_elem(const AdjMesh m, con
     }
     double volb = b.volbar[e];
     const double vol = s1.vol[e];
-    const double iv = 1.0 / vol;
+    const double iv = fast_rcp(vol);
     const double sb = divb * iv;
     double Bb[24], xb[8], yb[8], zb[8];
     double S = 0.0;
@@ -332,7 +334,7 @@ __global__ void __launch_bounds__(kAdjElemBlock) k_adj_elem(const AdjMesh m, con
                         fma(force[(size_t)(l * 3 + 2) * ne + e], s1.hz[n], power)));
       }
       const double adt = alpha * r->dt;
-      const double iM = sieb / M;
+      const double iM = sieb * fast_rcp(M);
       b.w[e] = -adt * iM;
       adtb = -power * iM;
     }
@@ -401,11 +403,11 @@ __global__ void __launch_bounds__(kAdjNodeBlock) k_adj_node(const AdjMesh m, con
     if (bc & 2u) vb1 = 0.0;
     if (bc & 4u) vb2 = 0.0;
     const double u0b = 0.5 * hb0 + vb0, v0b = 0.5 * hb1 + vb1, w0b = 0.5 * hb2 + vb2;
-    const double mass = m.node_mass[n];
-    b.fbar[0][n] = vb0 * adt / mass;
-    b.fbar[1][n] = vb1 * adt / mass;
-    b.fbar[2][n] = vb2 * adt / mass;
-    adtb += (vb0 * f0 + vb1 * f1 + vb2 * f2) / mass;
+    const double rmass = fast_rcp(m.node_mass[n]);
+    b.fbar[0][n] = vb0 * adt * rmass;
+    b.fbar[1][n] = vb1 * adt * rmass;
+    b.fbar[2][n] = vb2 * adt * rmass;
+    adtb += (vb0 * f0 + vb1 * f1 + vb2 * f2) * rmass;
     if (assign) {
       an_c.p[0][n] = gx;
       an_c.p[1][n] = gy;
@@ -526,24 +528,24 @@ __global__ void __launch_bounds__(kAdjForceBlock, 3) k_adj_force(const AdjMesh m
   const double alphab = phib * phi0, phi0b = phib * alpha;
   double divb = 0.0, sspdb = 0.0, volb = 0.0, denb = 0.0;
   if (araw < 1.0) {
-    const double inv = 1.0 / (sspd + fuzz);
+    const double inv = fast_rcp(sspd + fuzz);
     const double sg = div > 0.0 ? 1.0 : (div < 0.0 ? -1.0 : 0.0);
     const double a20 = 20.0 * alphab * inv;
     divb = a20 * c_length * sg;
     sspdb = -alphab * alpha * inv;
-    volb = a20 * fabs(div) * c_length / (3.0 * vol);
+    volb = a20 * fabs(div) * c_length * fast_rcp(3.0 * vol);
   }
   int nbc = -1;
   double nbv = 0.0;
   if (sel >= 0) {
-    const double rbD = -phi0b / D;  // phi0 = 1 - r_face
+    const double rbD = -phi0b * fast_rcp(D);  // phi0 = 1 - r_face
     nbv = 0.9 * rbD;
     nbc = sel;
     divb = fma(-rbD, r_min, divb);
   }
   double sb0 = 0.0, sb1 = 0.0, sb2 = 0.0, s3b = 0.0;
   if (use_vstar) {
-    const double is3 = 1.0 / s3;
+    const double is3 = fast_rcp(s3);
     sb0 = vsb0 * is3;
     sb1 = vsb1 * is3;
     sb2 = vsb2 * is3;
@@ -566,7 +568,7 @@ __global__ void __launch_bounds__(kAdjForceBlock, 3) k_adj_force(const AdjMesh m
     const size_t i0 = (size_t)(l * 3) * ne + e, i1 = i0 + ne, i2 = i1 + ne;
     const double b0 = s0.bmat[i0], b1 = s0.bmat[i1], b2 = s0.bmat[i2];
     const double qB = fma(b0, b0, fma(b1, b1, b2 * b2));
-    const double rB = rsqrt(qB);
+    const double rB = fast_rsqrt(qB);
     const double nB = qB * rB;
     const double qm = fma(qb, mv[l], q1c);
     const double mucb = mubl * nB;
@@ -578,7 +580,7 @@ __global__ void __launch_bounds__(kAdjForceBlock, 3) k_adj_force(const AdjMesh m
     q1cb = fma(mucb, den, q1cb);
     if (mv[l] > 0.0) {
       const double d0 = vu[l] - vs0, d1 = vv[l] - vs1, d2 = vw[l] - vs2;
-      const double sm = mucb * den * qb * rsqrt(fma(d0, d0, fma(d1, d1, d2 * d2)));
+      const double sm = mucb * den * qb * fast_rsqrt(fma(d0, d0, fma(d1, d1, d2 * d2)));
       vb0 = fma(sm, d0, vb0);
       vb1 = fma(sm, d1, vb1);
       vb2 = fma(sm, d2, vb2);
@@ -601,7 +603,7 @@ __global__ void __launch_bounds__(kAdjForceBlock, 3) k_adj_force(const AdjMesh m
   }
   double sieb = 0.0, gb = 0.0;
   eos_fold(den, s0.sie[e], m.gamma[e], m.csmin[e], presb, sspdb, sieb, denb, gb);
-  volb -= denb * den / vol;  // den = M / vol
+  volb -= denb * den * fast_rcp(vol);  // den = M / vol
   b.volbar[e] = volb;
   b.divbar[e] = divb;
   b.nbc[e] = nbc;

@@ -194,6 +194,33 @@ __device__ __forceinline__ double rcp_seed(long long bb) {
   const double r = __dadd_rn(f64_of(r0), f64_of_signed(__fmul_rn(r0, e)));
   return __longlong_as_double((__double_as_longlong(r) - ((long long)eb << 52)) ^ (bb & ~kAbsMask));
 }
+// Reciprocal and reciprocal square root to ~2^-43 relative, for derivative
+// terms that have no parity target (the adjoint's reverse arithmetic): the float
+// pair of the Newton forms above as a double, without their FP64 step (one FP64
+// addition each).  Arguments outside 2^-250 .. 2^251 (reciprocal) or zero,
+// negative, subnormal and non-finite ones (reciprocal square root) take the
+// library's operation.
+__device__ __forceinline__ double fast_rcp(double b) {
+  const long long bb = __double_as_longlong(b);
+  return plain_range(bb) ? rcp_seed(bb) : 1.0 / b;
+}
+__device__ __forceinline__ double fast_rsqrt(double x) {
+  const long long b = __double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7FF);
+  if (b <= 0 || ex == 0 || ex == 0x7FF) return rsqrt(x);
+  const int k = (ex - 1023) >> 1;                                      // x = m 4^k
+  const double m = __longlong_as_double(b - ((long long)(2 * k) << 52));  // [1, 4)
+  const float mh = f32_image(m);
+  const float r0 = rsqrtf(mh);
+  const float p = __fmul_rn(r0, r0);
+  const float pe = fmaf(r0, r0, -p);                                   // r0^2 = p + pe exactly
+  const float q = __fmul_rn(mh, p);
+  const float qe = fmaf(mh, p, -q);                                    // mh p = q + qe exactly
+  const float e = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, q), qe),
+                            __fadd_rn(__fmul_rn(mh, pe), __fmul_rn(f32_rest(m), p)));  // 1 - m r0^2 (1 - q exact)
+  const double r = __dadd_rn(f64_of(r0), f64_of_signed(__fmul_rn(__fmul_rn(0.5f, r0), e)));  // r0 (1 + e/2)
+  return __longlong_as_double(__double_as_longlong(r) - ((long long)k << 52));
+}
 // A divisor prepared once for the quotients that share it.
 struct Divisor {
   double b, r;
