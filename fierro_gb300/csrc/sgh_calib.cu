@@ -131,10 +131,10 @@ extern "C" int fierro_root_check(int fp_mode, int which, long long n, unsigned l
                                  int hi_exp, unsigned long long* out) {
   using fierro::set_error;
   if (!out) return set_error(FIERRO_EINVAL, "NULL output");
-  if ((fp_mode != FIERRO_FP_EXACT && fp_mode != FIERRO_FP_FMA) || which < 0 || which > 6 || n < 8 ||
+  if ((fp_mode != FIERRO_FP_EXACT && fp_mode != FIERRO_FP_FMA) || which < 0 || which > 8 || n < 8 ||
       n > (1LL << 36) || lo_exp < -1022 || hi_exp > 1023 || lo_exp > hi_exp)
     return set_error(FIERRO_EINVAL, "root check: fp_mode 0/1, which 0 sqrt / 1 cbrt / 2 quotient / 3 reciprocal / 4..6 near-boundary "
-                                    "sqrt, quotient, reciprocal, 8 <= n <= 2^36, "
+                                    "sqrt, quotient, reciprocal / 7, 8 fast reciprocal, rsqrt, 8 <= n <= 2^36, "
                                     "-1022 <= lo_exp <= hi_exp <= 1023");
   const fierro::KernelSet& ks = fp_mode == FIERRO_FP_FMA ? fierro::kernels_fma() : fierro::kernels_exact();
   unsigned long long* d = nullptr;

@@ -756,7 +756,9 @@ static void launch_reciprocal(const double* in, double* out, int n, cudaStream_t
 // square roots lie just below the midpoints 4^s/2^s (1 + (2k+1) 2^-53) and
 // 2^s (1 - (2k+1) 2^-54); 2^s (1 - (2k+1) 2^-53), whose reciprocal lies just
 // above the midpoint 2^-s (1 + (2k+1) 2^-53); and 2^t (1 + m 2^-52) / that,
-// just above a midpoint too (k < 2^20, m < 2^16).  out[0] counts results
+// just above a midpoint too (k < 2^20, m < 2^16).  which 7, 8: the adjoint's
+// ~2^-43 reciprocal and reciprocal square root (fast_rcp, fast_rsqrt) against
+// 1 / x and 1 / sqrt(x), on the seeded arguments.  out[0] counts results
 // differing, out[1] is the largest difference in ulps, out[2] counts results
 // differing by more than one ulp.
 __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
@@ -778,7 +780,7 @@ __global__ void __launch_bounds__(256) k_root_check(int which, long long n, unsi
     const long long odd = 2 * (long long)((unsigned long long)i & 0xFFFFF) + 1;  // 2k + 1, k < 2^20
     const int s = (int)((h >> 40) % 201) - 100;                                  // a power of two in +-100
     double x;
-    if (which >= 4) {
+    if (which >= 4 && which <= 6) {
       if (which == 4)
         x = __longlong_as_double((i & 1) ? ((long long)(1023 + 2 * s) << 52) - odd
                                          : ((long long)(1023 + 2 * s) << 52) | odd);
@@ -790,7 +792,7 @@ __global__ void __launch_bounds__(256) k_root_check(int which, long long n, unsi
                                     0x0010000000000000LL};
       x = __longlong_as_double(special[i]);
     } else {
-      x = seeded_double(h, lo_exp, hi_exp, which == 2 || which == 3);
+      x = seeded_double(h, lo_exp, hi_exp, which == 2 || which == 3 || which == 7);
     }
     double a, r;
     if (which == 0 || which == 4) {
@@ -806,9 +808,15 @@ __global__ void __launch_bounds__(256) k_root_check(int which, long long n, unsi
       if (which == 2 && i >= 8 && i < 16) num = (i & 1) ? -0.0 : 0.0;  // signed zeros over seeded divisors
       a = quot(num, divisor(x));  // the shared-divisor form (mode_div in the FMA mode)
       r = num / x;
-    } else {
+    } else if (which == 3 || which == 6) {
       a = mode_rcp(x);
       r = 1.0 / x;
+    } else if (which == 7) {
+      a = fast_rcp(x);
+      r = 1.0 / x;
+    } else {
+      a = fast_rsqrt(x);
+      r = 1.0 / sqrt(x);
     }
     long long d = __double_as_longlong(a) - __double_as_longlong(r);
     if (isnan(a) && isnan(r)) d = 0;

@@ -330,7 +330,9 @@ int fierro_fp64_stream_rate(int chains, int op, int threads, int blocks_per_sm, 
  * [lo_exp, hi_exp] (within -1022..1023), f's 52 bits uniform (quotients: two such
  * operands of random signs).  which 4, 5, 6: the square root, quotient and
  * reciprocal on arguments whose exact result lies just off a rounding boundary
- * (the hard cases of correct rounding).  out[0] = results differing, out[1] =
+ * (the hard cases of correct rounding); which 7, 8: the adjoint's ~2^-43
+ * reciprocal and reciprocal square root against 1 / x and 1 / sqrt(x).
+ * out[0] = results differing, out[1] =
  * the largest difference in ulps, out[2] = results differing by more than one
  * ulp.  The exact mode's square roots and quotients are correctly rounded (0
  * differing; its reciprocals and cube roots are the library's); the FMA mode's
