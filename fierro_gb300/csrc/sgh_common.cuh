@@ -31,14 +31,17 @@ __device__ __forceinline__ double okey_decode(long long k) {
 // Newton step around an exactly formed residual then leaves ~2^-64 (square
 // root) or ~2^-89 (quotient) relative error before the final rounding: three
 // FP64 operations per square root, four per quotient (one reciprocal shared by
-// several quotients: three each), three per reciprocal.  The single-precision
+// several quotients: three each), three per reciprocal, and in the exact mode
+// one more for the remainder test below.  The single-precision
 // steps use the _rn intrinsics, which are never contracted (a fused mh - y0*y0
 // would count the product's low part twice).
 //
 // FMA mode: these results as they are (square roots within an ulp, quotients
 // the IEEE ones but for ~2^-37 of an ulp around rounding boundaries).
-// Exact mode (square roots, and quotients that share a divisor): correctly
-// rounded, so bit for bit the IEEE square root and division.  With the result
+// Exact mode (square roots, and quotients that share a divisor; its single
+// quotients and reciprocals keep the library's division, which the remainder
+// test would make no cheaper): correctly rounded, so bit for bit the IEEE square
+// root and division.  With the result
 // y (q) within an ulp, the remainder x - y^2 (a - b q) is exactly representable
 // and one fma forms it; y is the correctly rounded root iff |x - y^2| < ulp(y) y
 // (up to 2^-52 relative), q the correctly rounded quotient iff
@@ -53,9 +56,9 @@ __device__ __forceinline__ double okey_decode(long long k) {
 // operation too (tested on the bits); zeros are returned as they are (their
 // root is themselves; a 256^3 Sedov cycle, most of whose mesh is at rest, and a
 // Noh cycle, where every node moves, take the same time).  The library's
-// operations are reached through
-// calls: inline under the exact mode's data-dependent test they were
-// if-converted and ran on every lane (the exact cycle 12 % slower).
+// operations are reached through calls: inline under the exact mode's
+// data-dependent test they were if-converted and ran on every lane (the exact
+// cycle 12 % slower).
 // FIERRO_LIBRARY_ROOTS / FIERRO_LIBRARY_DIV build either mode with the
 // library's square and cube roots / divisions throughout, for comparison.
 
