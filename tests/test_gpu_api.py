@@ -278,3 +278,37 @@ def test_other_boundary_kinds_leave_nodes_free(oracle_built, lib_built, kind):
     ref = o.state()
     for k in fields:
         assert np.array_equal(got["plus"][k], ref[k]), k
+
+
+def _shifted_like(a: np.ndarray, shift: int) -> np.ndarray:
+    """A C-contiguous float64 array shaped like `a` whose data starts `shift`
+    bytes into a fresh buffer (shift 8: 8- but not 16-byte aligned)."""
+    raw = np.zeros(a.nbytes + 64, dtype=np.uint8)
+    base = (-raw.ctypes.data) % 16 + shift
+    return np.frombuffer(raw.data, dtype=a.dtype, count=a.size, offset=base).reshape(a.shape)
+
+
+@pytest.mark.parametrize("strength", [False, True])
+def test_download_into_unevenly_aligned_host_arrays(lib_built, strength):
+    """get_state writes the node, corner-force and stress rows with 16-byte
+    stores where the host address allows: host arrays that start 8 bytes off a
+    16-byte boundary (odd and even node and element counts) receive the same
+    values as 16-byte aligned ones."""
+    from fierro_gb300 import problems, sgh
+    for n in (9, 10):
+        prob = problems.sedov_mixed_strength(n, cycles=6) if strength else \
+            problems.sedov(n, jitter=0.1, seed=4, permute=True, cycles=6)
+        st = sgh.setup(prob)
+        with sgh.SGHSolver(prob) as s:
+            s.set_state(st)
+            s.run(6)
+            ref = s.get_state()
+            for shift in (8, 0):
+                out = {k: (_shifted_like(v, shift) if v.dtype == np.float64 else v.copy()) for k, v in ref.items()}
+                for k in out:
+                    if out[k].dtype == np.float64:
+                        # the written fields start as NaN; the state variables as the handle holds them
+                        out[k][...] = ref[k] if k == "elem_statev" else np.nan
+                s.get_state(out)
+                for k in ref:
+                    assert np.array_equal(out[k], ref[k]), (n, shift, k)
