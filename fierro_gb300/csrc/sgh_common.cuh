@@ -143,16 +143,12 @@ __device__ __forceinline__ double mode_sqrt(double x) {
 }
 #endif
 
-#if FIERRO_FMA && !defined(FIERRO_LIBRARY_ROOTS)
-// Cube root of the FMA mode, the same way: the float root c0 = cbrtf(mh)
-// refined once on the pair (residual m - c0^3 from the exact low parts of c0^2
-// and c0^3), then one FP64 step whose residual rounds y^2 once (within an ulp of
-// the library's cube root, which is not correctly rounded either).  Four FP64
-// operations.  The exact mode keeps the library's cbrt.
-__device__ __forceinline__ double mode_cbrt(double v) {
-  const long long b = __double_as_longlong(v);
-  const int ex = (int)((b >> 52) & 0x7FF);
-  if (b <= 0 || ex == 0 || ex == 0x7FF) return cbrt(v);
+// Cube root, the same way: the float root c0 = cbrtf(mh) refined once on the
+// pair (residual m - c0^3 from the exact low parts of c0^2 and c0^3), then one
+// FP64 step whose residual rounds y^2 once (within an ulp of the library's cube
+// root, which is not correctly rounded either).  Four FP64 operations.  v
+// positive and normal; b its bits, ex its biased exponent.
+__device__ __forceinline__ double cbrt_newton(double v, long long b, int ex) {
   const int E = ex - 1023;
   const int k = E >= 0 ? E / 3 : -((2 - E) / 3);                        // floor(E / 3)
   const double m = __longlong_as_double(b - ((long long)(3 * k) << 52));  // [1, 8)
@@ -175,6 +171,16 @@ __device__ __forceinline__ double mode_cbrt(double v) {
   c = fma(fma(-c2, c, m), f64_of(inv), c);
 #endif
   return __longlong_as_double(__double_as_longlong(c) + ((long long)k << 52));
+}
+
+#if FIERRO_FMA && !defined(FIERRO_LIBRARY_ROOTS)
+// The FMA mode's cube root; the exact mode keeps the library's cbrt (its pow
+// takes the Newton cube root as a starting value only, pow_third below).
+__device__ __forceinline__ double mode_cbrt(double v) {
+  const long long b = __double_as_longlong(v);
+  const int ex = (int)((b >> 52) & 0x7FF);
+  if (b <= 0 || ex == 0 || ex == 0x7FF) return cbrt(v);
+  return cbrt_newton(v, b, ex);
 }
 #else
 __device__ __forceinline__ double mode_cbrt(double v) { return cbrt(v); }
@@ -290,8 +296,14 @@ __device__ __forceinline__ double pow_third(double v) {
 #if FIERRO_FMA
   return mode_cbrt(v);
 #else
-  if (!(v > 1.0e-290 && v < 1.0e290)) return pow(v, 1.0 / 3.0);
+  // 1e-290 < v < 1e290, compared on the bits (positive doubles order as integers)
+  const long long bits = __double_as_longlong(v);
+  if (!(bits > 0x03B8F2B061AEA072LL && bits < 0x7C2485CE9E7A065FLL)) return pow(v, 1.0 / 3.0);
+#ifdef FIERRO_LIBRARY_ROOTS
   const double c0 = cbrt(v);
+#else
+  const double c0 = cbrt_newton(v, bits, (int)((bits >> 52) & 0x7FF));  // within an ulp: a starting value
+#endif
   const double p = c0 * c0;
   const double pe = fma(c0, c0, -p);
   const double q = p * c0;
@@ -301,7 +313,6 @@ __device__ __forceinline__ double pow_third(double v) {
   const float inv3p = __frcp_rn(3.0f * (float)p);
   const float step = rf * inv3p;  // (v - c0^3) / (3 c0^2)
   // ln v from the exponent and a single-precision log of the significand
-  const long long bits = __double_as_longlong(v);
   const int ex = (int)((bits >> 52) & 0x7FF) - 1023;
   const double m = __longlong_as_double((bits & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL);
   const float lnv = (float)ex * 0.69314718f + __logf((float)m);
