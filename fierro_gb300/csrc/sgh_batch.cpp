@@ -70,11 +70,13 @@ struct fierro_batch {
   double *d_bmat = nullptr, *d_force = nullptr;
   long long* d_cfl = nullptr;
   Ctrl* d_ctrl = nullptr;
+  unsigned int* d_sync = nullptr;  // fused stage: arrival counter, generation, timeout status
+  cudaError_t capture_err = cudaSuccess;
   double* h_stage = nullptr;
   size_t stage_elems = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   // launch shape of the cycle kernels (fierro_batch_set_shape / fierro_batch_autotune)
-  fierro_batch_shape shape{kForceBlock, kNodeBlock, kElemBlock, 0};
+  fierro_batch_shape shape{kForceBlock, kNodeBlock, kElemBlock, 0, 0};
   int sm_count = 0;
   std::vector<fierro_batch_shape> tune_shapes;
   std::vector<double> tune_ms;
@@ -126,6 +128,26 @@ int scatter_down(fierro_batch* b, double* out, const double* src, int64_t off, c
 int persistent_grid(const fierro_batch* b, int kernel, int block) {
   if (!b->shape.persistent) return 0;
   return b->sm_count * b->ks->batch_max_blocks(kernel, block) * b->shape.persistent;
+}
+
+// A fused stage whose grid barrier gave up waiting (never expected: the launch
+// is cooperative) leaves results that cannot be trusted: report it, and reset
+// the barrier for the next launch.  Call with the stream idle.
+int check_sync(fierro_batch* b) {
+  if (!b->shape.fused_stage) return FIERRO_OK;
+  unsigned int st = 0;
+  CUDA_TRY(cudaMemcpy(&st, b->d_sync + 2, sizeof(st), cudaMemcpyDeviceToHost));
+  if (st == 0) return FIERRO_OK;
+  CUDA_TRY(cudaMemset(b->d_sync, 0, 3 * sizeof(unsigned int)));
+  return set_error(FIERRO_ETIMEDOUT, "batch: a fused stage's grid barrier timed out");
+}
+
+// The fused stage's grid: every resident block of the cooperative kernel at the
+// element block size, at most one per element tile.
+int fused_grid(const fierro_batch* b) {
+  const long long tiles = b->NE / b->shape.elem_block;
+  const long long resident = (long long)b->sm_count * b->ks->fused_max_blocks(b->shape.elem_block);
+  return (int)std::max<long long>(1, std::min(tiles, resident));
 }
 
 ForceArgs b_force(fierro_batch* b, int rb, int q) {
@@ -238,6 +260,18 @@ void b_cycle(fierro_batch* b, int c) {
     const double alpha = 1.0 / ((double)S - (double)s);  // sgh_solve.cpp:353
     const int rb = (s == 0) ? c : (c ^ 1);
     const int q = (c * S + s) & 1;
+    if (b->shape.fused_stage) {
+      // one cooperative launch for the stage, its barrier's arrival count reset first
+      ForceArgs fa = b_force(b, rb, q);
+      NodeArgs na = b_node(b, c, alpha);
+      ElemArgs ea = b_elem(b, c ^ 1, c, alpha, q ^ 1);
+      fa.grid = na.grid = ea.grid = 0;
+      const StageSync sync{b->d_sync, b->d_sync + 1, b->d_sync + 2};
+      cudaError_t err = cudaMemsetAsync(b->d_sync, 0, sizeof(unsigned int), b->stream);
+      if (err == cudaSuccess) err = b->ks->stage_fused(fa, na, ea, (s == S - 1) ? 1 : 0, sync, fused_grid(b), b->stream);
+      if (err != cudaSuccess && b->capture_err == cudaSuccess) b->capture_err = err;
+      continue;
+    }
     b->ks->force(b_force(b, rb, q), b->stream);
     b->ks->node(b_node(b, c, alpha), b->stream);
     b->ks->elem(b_elem(b, c ^ 1, c, alpha, q ^ 1), (s == S - 1) ? 1 : 0, b->stream);
@@ -250,7 +284,7 @@ constexpr int kMinBatchBlock = 32;
 bool shape_valid(const fierro_batch_shape& sh) {
   auto ok = [](int b, int hi) { return b >= kMinBatchBlock && b <= hi && (b & (b - 1)) == 0; };
   return ok(sh.force_block, kForceBlock) && ok(sh.node_block, 1024) && ok(sh.elem_block, kElemBlock) &&
-         sh.persistent >= 0 && sh.persistent <= 8;
+         sh.persistent >= 0 && sh.persistent <= 8 && (sh.fused_stage == 0 || sh.fused_stage == 1);
 }
 
 // Makes `sh` the batch's launch shape: the per-instance CFL partial ranges in
@@ -258,7 +292,7 @@ bool shape_valid(const fierro_batch_shape& sh) {
 int apply_shape(fierro_batch* b, const fierro_batch_shape& sh) {
   if (!shape_valid(sh))
     return set_error(FIERRO_EINVAL, "batch shape: blocks must be powers of two, force 32..%d, node 32..1024, "
-                     "element 32..%d, persistent 0..8 fills of the SMs", kForceBlock, kElemBlock);
+                     "element 32..%d, persistent 0..8 fills of the SMs, fused_stage 0 or 1", kForceBlock, kElemBlock);
   CUDA_TRY(cudaStreamSynchronize(b->stream));
   b->shape = sh;
   for (size_t i = 0; i < b->part_start.size(); ++i)
@@ -271,12 +305,14 @@ int apply_shape(fierro_batch* b, const fierro_batch_shape& sh) {
       b->graph[c] = nullptr;
     }
     cudaGraph_t g = nullptr;
+    b->capture_err = cudaSuccess;
     CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     b_cycle(b, c);
-    CUDA_TRY(cudaStreamEndCapture(b->stream, &g));
-    cudaError_t err = cudaGraphInstantiate(&b->graph[c], g, 0);
-    cudaGraphDestroy(g);
-    if (err != cudaSuccess) return set_error(FIERRO_ECUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(err));
+    cudaError_t err = cudaStreamEndCapture(b->stream, &g);
+    if (err == cudaSuccess && b->capture_err != cudaSuccess) err = b->capture_err;
+    if (err == cudaSuccess) err = cudaGraphInstantiate(&b->graph[c], g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (err != cudaSuccess) return set_error(FIERRO_ECUDA, "batch cycle graph: %s", cudaGetErrorString(err));
   }
   return FIERRO_OK;
 }
@@ -407,6 +443,8 @@ int create_impl(fierro_batch* b, const fierro_batch_instance* inst, int64_t n, i
   TRY(balloc(b, &b->d_force, (size_t)NE * 24));
   TRY(balloc(b, &b->d_cfl, (size_t)(NE / kMinBatchBlock)));  // one partial per tile of the smallest block
   TRY(balloc(b, &b->d_ctrl, (size_t)n));
+  TRY(balloc(b, &b->d_sync, 3));
+  CUDA_TRY(cudaMemsetAsync(b->d_sync, 0, 3 * sizeof(unsigned int), b->stream));
   TRY(put(b, b->d_nie, nie));
   TRY(put(b, b->d_cin_start, cin_start));
   TRY(put(b, b->d_cin, cin));
@@ -550,6 +588,7 @@ extern "C" int fierro_batch_run(fierro_batch* b, int64_t cycles) {
     b->enq_cycles++;
   }
   CUDA_TRY(cudaStreamSynchronize(b->stream));
+  TRY(check_sync(b));
   std::vector<Ctrl> cs((size_t)b->n);
   CUDA_TRY(cudaMemcpy(cs.data(), b->d_ctrl, sizeof(Ctrl) * (size_t)b->n, cudaMemcpyDeviceToHost));
   for (int64_t i = 0; i < b->n; ++i) {
@@ -667,6 +706,7 @@ int time_shape(fierro_batch* b, int warm, int cycles, double* ms) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (err != cudaSuccess) return set_error(FIERRO_ECUDA, "batch autotune: %s", cudaGetErrorString(err));
+  TRY(check_sync(b));
   *ms = (double)t / std::max(cycles, 1);
   return FIERRO_OK;
 }
@@ -698,7 +738,7 @@ extern "C" int fierro_batch_autotune(fierro_batch* b, int64_t cycles, fierro_bat
     for (size_t i = 0; i < b->tune_shapes.size(); ++i) {
       const fierro_batch_shape& o = b->tune_shapes[i];
       if (o.force_block == sh.force_block && o.node_block == sh.node_block && o.elem_block == sh.elem_block &&
-          o.persistent == sh.persistent)
+          o.persistent == sh.persistent && o.fused_stage == sh.fused_stage)
         return FIERRO_OK;
     }
     TRY(copy_arrays(b, save, arrs, false));
@@ -739,6 +779,14 @@ extern "C" int fierro_batch_autotune(fierro_batch* b, int64_t cycles, fierro_bat
     fierro_batch_shape sh = best;
     sh.persistent = p;
     rc = trial(sh);
+  }
+  // the fused stage (one cooperative launch per stage, at the chosen element
+  // block); a candidate the device cannot run is left out of the choice
+  if (!rc) {
+    fierro_batch_shape sh = best;
+    sh.persistent = 0;
+    sh.fused_stage = 1;
+    if (trial(sh) != FIERRO_OK) clear_error();
   }
   // the uploaded state back (also after a failed candidate), with the chosen
   // shape, or the shape the batch had when the tuning failed

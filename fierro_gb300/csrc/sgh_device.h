@@ -151,6 +151,17 @@ struct ElemArgs {
   int grid;               // batch only: blocks of a persistent grid looping over the tiles (0: one per tile)
 };
 
+// Grid barrier of the batch's fused stage kernel: an arrival counter and a
+// generation counter in device memory, and a status word a block sets when its
+// wait ran out (the launch is cooperative, so every block is resident and the
+// limit is only a guard).
+struct StageSync {
+  unsigned int* arrive;
+  unsigned int* gen;
+  unsigned int* status;
+};
+#define FIERRO_SYNC_TIMEOUT 1u
+
 struct DtArgs {
   const long long* cfl_part;
   int nparts;
@@ -194,6 +205,12 @@ struct KernelSet {
   // difference in ulps, out[2] differing by more than one ulp (fierro_root_check)
   void (*root_check)(int which, long long n, unsigned long long seed, int lo_exp, int hi_exp,
                      unsigned long long* out, cudaStream_t);
+  // a batch's RK stage as one cooperative launch: the force, node and element
+  // passes over `grid` resident blocks of ea.block threads with grid barriers
+  // between them (kind as for elem); and that kernel's resident blocks per SM
+  cudaError_t (*stage_fused)(const ForceArgs& fa, const NodeArgs& na, const ElemArgs& ea, int kind,
+                             const StageSync& sync, int grid, cudaStream_t);
+  int (*fused_max_blocks)(int block);
 };
 
 constexpr int kElemBlock = 128;

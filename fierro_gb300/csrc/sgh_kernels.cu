@@ -79,6 +79,18 @@ namespace FIERRO_IMPL {
 
 constexpr int kNodeGather = FIERRO_NODE_GATHER;
 
+// Loads of values an earlier phase of the same launch wrote (the batch's fused
+// stage kernel, COH): from L2 (ld.global.cg), never from a line another phase
+// left in this SM's L1.  Otherwise the read-only path (__ldg) or a plain load.
+template <bool COH>
+__device__ __forceinline__ double ld_ro(const double* p) {
+  return COH ? __ldcg(p) : __ldg(p);
+}
+template <bool COH>
+__device__ __forceinline__ double ld_pl(const double* p) {
+  return COH ? __ldcg(p) : *p;
+}
+
 #include "sgh_common.cuh"
 #include "sgh_hex_geometry.cuh"
 #include "sgh_cfl.cuh"
@@ -358,7 +370,7 @@ __global__ void FIERRO_FORCE_BOUNDS k_force(const ForceArgs a) {
 // ---------------------------------------------------------------------------
 // Node update: corner-force gather in the reference's summation order, velocity,
 // boundary conditions, half velocity and position.
-template <bool BATCH>
+template <bool BATCH, bool COH = false>
 __device__ __forceinline__ void node_update(const NodeArgs& a, const int n) {
   const Ctrl* ctrl = BATCH ? a.ctrl + a.inst[n] : a.ctrl;
   if (BATCH && !ctrl->active) return;
@@ -377,7 +389,7 @@ __device__ __forceinline__ void node_update(const NodeArgs& a, const int n) {
     for (int k = 0; k < kNodeGather; ++k) {
       const int e = cid[k] >> 3, l = cid[k] & 7;
 #pragma unroll
-      for (int d = 0; d < 3; ++d) g[k][d] = k < cnt ? __ldg(a.force + (size_t)(l * 3 + d) * ne + e) : 0.0;
+      for (int d = 0; d < 3; ++d) g[k][d] = k < cnt ? ld_ro<COH>(a.force + (size_t)(l * 3 + d) * ne + e) : 0.0;
     }
 #pragma unroll
     for (int k = 0; k < kNodeGather; ++k)
@@ -442,7 +454,7 @@ __global__ void __launch_bounds__(kNodeBlock) k_node(const NodeArgs a) {
 // every tile lies inside one instance (instances' element ranges are padded to
 // whole default blocks, padding marked by a negative instance id, and the block
 // divides the default), so the activity test and the CFL partial are per tile.
-template <int KIND, bool BATCH, bool STRENGTH>
+template <int KIND, bool BATCH, bool STRENGTH, bool COH = false>
 __device__ __forceinline__ void elem_tile(const ElemArgs& a, const int tile) {
   const int e = tile * blockDim.x + threadIdx.x;
   const int ib = BATCH ? a.inst[tile * blockDim.x] : 0;
@@ -459,12 +471,12 @@ __device__ __forceinline__ void elem_tile(const ElemArgs& a, const int tile) {
     double x[8], y[8], z[8], u[8], v[8], w[8];
 #pragma unroll
     for (int l = 0; l < 8; ++l) {
-      x[l] = __ldg(a.x + nid[l]);
-      y[l] = __ldg(a.y + nid[l]);
-      z[l] = __ldg(a.z + nid[l]);
-      u[l] = __ldg(a.u + nid[l]);
-      v[l] = __ldg(a.v + nid[l]);
-      w[l] = __ldg(a.w + nid[l]);
+      x[l] = ld_ro<COH>(a.x + nid[l]);
+      y[l] = ld_ro<COH>(a.y + nid[l]);
+      z[l] = ld_ro<COH>(a.z + nid[l]);
+      u[l] = ld_ro<COH>(a.u + nid[l]);
+      v[l] = ld_ro<COH>(a.v + nid[l]);
+      w[l] = ld_ro<COH>(a.w + nid[l]);
     }
     double sie1 = 0.0;
     if (KIND != 2) {
@@ -474,9 +486,9 @@ __device__ __forceinline__ void elem_tile(const ElemArgs& a, const int tile) {
       double power = 0.0;
 #pragma unroll
       for (int l = 0; l < 8; ++l) {
-        power = FX_ADD(power, FX_MUL(a.force[(size_t)(l * 3 + 0) * ne + e], __ldg(a.hx + nid[l])));
-        power = FX_ADD(power, FX_MUL(a.force[(size_t)(l * 3 + 1) * ne + e], __ldg(a.hy + nid[l])));
-        power = FX_ADD(power, FX_MUL(a.force[(size_t)(l * 3 + 2) * ne + e], __ldg(a.hz + nid[l])));
+        power = FX_ADD(power, FX_MUL(ld_pl<COH>(a.force + (size_t)(l * 3 + 0) * ne + e), ld_ro<COH>(a.hx + nid[l])));
+        power = FX_ADD(power, FX_MUL(ld_pl<COH>(a.force + (size_t)(l * 3 + 1) * ne + e), ld_ro<COH>(a.hy + nid[l])));
+        power = FX_ADD(power, FX_MUL(ld_pl<COH>(a.force + (size_t)(l * 3 + 2) * ne + e), ld_ro<COH>(a.hz + nid[l])));
       }
       const double adt = a.rk_alpha * ctrl->dt;
       sie1 = a.sie0[e] - FX_MUL(mode_div(adt, a.mass[e]), power);  // not fused: sie1 may cancel sie0
@@ -562,6 +574,61 @@ __global__ void FIERRO_ELEM_BOUNDS k_elem(const ElemArgs a) {
     }
   } else {
     elem_tile<KIND, false, STRENGTH>(a, blockIdx.x);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// A batch's RK stage in one cooperative launch: the force pass, a grid barrier,
+// the node pass, a grid barrier, the element pass, each over the whole batch
+// with the grid's resident blocks striding over elements, nodes and element
+// tiles (the same device functions as the three separate kernels, so the same
+// results bit for bit).  Values an earlier phase wrote are read from L2 (COH).
+// Every wait at a barrier has an iteration limit: a block that gives up sets
+// FIERRO_SYNC_TIMEOUT and returns, and so does every other block at its own
+// limit, so a launch always ends.
+constexpr unsigned kSyncSpins = 1u << 23;  // x ~128 ns: about a second
+
+__device__ __forceinline__ bool grid_barrier(const StageSync& s) {
+  __shared__ unsigned ok_s;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned ok = 1u;
+    volatile unsigned* gen = s.gen;
+    const unsigned g = *gen;
+    if (atomicAdd(s.arrive, 1u) == gridDim.x - 1) {
+      atomicExch(s.arrive, 0u);
+      __threadfence();
+      atomicAdd(s.gen, 1u);
+    } else {
+      for (unsigned it = 0; *gen == g; ++it) {
+        if (it > kSyncSpins) {
+          atomicOr(s.status, FIERRO_SYNC_TIMEOUT);
+          ok = 0u;
+          break;
+        }
+        __nanosleep(128);
+      }
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0u;
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kElemBlock) k_stage_fused(const ForceArgs fa, const NodeArgs na, const ElemArgs ea,
+                                                            const StageSync sync) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < fa.ne; e += stride) force_elem<true, false, false, 0>(fa, e);
+  if (!grid_barrier(sync)) return;
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < na.nn; n += stride) node_update<true, true>(na, n);
+  if (!grid_barrier(sync)) return;
+  const int ntiles = (ea.ne + blockDim.x - 1) / blockDim.x;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    elem_tile<KIND, true, false, true>(ea, t);
+    __syncthreads();
   }
 }
 
@@ -833,6 +900,28 @@ static void launch_root_check(int which, long long n, unsigned long long seed, i
   const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
   k_root_check<<<(unsigned)blocks, 256, 0, s>>>(which, n, seed, lo_exp, hi_exp, out);
 }
+static cudaError_t launch_stage_fused(const ForceArgs& fa, const NodeArgs& na, const ElemArgs& ea, int kind,
+                                      const StageSync& sync, int grid, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block_or(ea.block, kElemBlock));
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return kind == 1 ? cudaLaunchKernelEx(&cfg, k_stage_fused<1>, fa, na, ea, sync)
+                   : cudaLaunchKernelEx(&cfg, k_stage_fused<0>, fa, na, ea, sync);
+}
+static int fused_max_blocks(int block) {
+  int n0 = 0, n1 = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n0, k_stage_fused<0>, block, 0) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_stage_fused<1>, block, 0) != cudaSuccess)
+    return 0;
+  return n0 < n1 ? n0 : n1;
+}
 static void launch_energy(const EnergyArgs& a, cudaStream_t s) {
   const int nb = 512;
   k_energy_part<<<nb, kEnergyBlock, 0, s>>>(a);
@@ -846,7 +935,8 @@ const KernelSet& kernels_fma() {
   static const KernelSet k = {fma_impl::launch_force, fma_impl::launch_force_tape, fma_impl::launch_force_branch, fma_impl::launch_node, fma_impl::launch_elem,
                               fma_impl::launch_dt, fma_impl::launch_end, fma_impl::launch_energy,
                               fma_impl::launch_end_batch, "fma", fma_impl::batch_max_blocks,
-                              fma_impl::launch_reciprocal, fma_impl::launch_root_check};
+                              fma_impl::launch_reciprocal, fma_impl::launch_root_check,
+                              fma_impl::launch_stage_fused, fma_impl::fused_max_blocks};
   return k;
 }
 #else
@@ -854,7 +944,8 @@ const KernelSet& kernels_exact() {
   static const KernelSet k = {exact_impl::launch_force, exact_impl::launch_force_tape, exact_impl::launch_force_branch, exact_impl::launch_node, exact_impl::launch_elem,
                               exact_impl::launch_dt, exact_impl::launch_end, exact_impl::launch_energy,
                               exact_impl::launch_end_batch, "exact", exact_impl::batch_max_blocks,
-                              exact_impl::launch_reciprocal, exact_impl::launch_root_check};
+                              exact_impl::launch_reciprocal, exact_impl::launch_root_check,
+                              exact_impl::launch_stage_fused, exact_impl::fused_max_blocks};
   return k;
 }
 #endif

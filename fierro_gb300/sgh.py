@@ -487,10 +487,10 @@ def _f64(a, shape=None):
 
 class BatchShape(C.Structure):
     _fields_ = [("force_block", C.c_int), ("node_block", C.c_int), ("elem_block", C.c_int),
-                ("persistent", C.c_int)]
+                ("persistent", C.c_int), ("fused_stage", C.c_int)]
 
     def as_tuple(self):
-        return (self.force_block, self.node_block, self.elem_block, self.persistent)
+        return (self.force_block, self.node_block, self.elem_block, self.persistent, self.fused_stage)
 
 
 class BatchInstance(C.Structure):
@@ -556,11 +556,13 @@ class Batch:
     def device_bytes(self) -> int:
         return int(_lib.fierro_batch_device_bytes(self.h))
 
-    def set_shape(self, force_block: int = 128, node_block: int = 256, elem_block: int = 128, persistent: int = 0):
+    def set_shape(self, force_block: int = 128, node_block: int = 256, elem_block: int = 128, persistent: int = 0,
+                  fused_stage: int = 0):
         """fierro_batch_set_shape: threads per block of the force, node and element
-        passes and the persistent grid (blocks per SM, 0 = one block per tile)."""
+        passes, the persistent grid (fills of the SMs, 0 = one block per tile) and
+        the fused stage (1: one cooperative launch per RK stage)."""
         _check(_lib.fierro_batch_set_shape(self.h, C.byref(BatchShape(force_block, node_block, elem_block,
-                                                                      persistent))))
+                                                                      persistent, fused_stage))))
 
     def shape(self):
         sh = BatchShape()

@@ -272,14 +272,19 @@ int64_t fierro_batch_device_bytes(const fierro_batch* b);
  * threads per block of the corner-force, node and element passes (powers of two;
  * force and element 32..128, node 32..1024), and `persistent`: 0 = one block per
  * tile of elements or nodes, p = 1..8 = a persistent grid that fills every SM p
- * times over with the kernel's resident blocks and loops over the tiles.  Results do not depend on the shape (every element and
- * node runs the same arithmetic; the CFL minimum is order-independent).
- * Default {128, 256, 128, 0}. */
+ * times over with the kernel's resident blocks and loops over the tiles.
+ * `fused_stage` 1 runs each RK stage as ONE cooperative launch of elem_block
+ * threads per block over the resident grid (force pass, grid barrier, node pass,
+ * grid barrier, element pass; the other blocks and `persistent` are then
+ * unused).  Results do not depend on the shape (every element and node runs the
+ * same arithmetic; the CFL minimum is order-independent).
+ * Default {128, 256, 128, 0, 0}. */
 typedef struct {
   int force_block;
   int node_block;
   int elem_block;
   int persistent;
+  int fused_stage;
 } fierro_batch_shape;
 
 /* Set or read the shape; set only before the first fierro_batch_run. */
@@ -288,10 +293,12 @@ int fierro_batch_get_shape(const fierro_batch* b, fierro_batch_shape* shape);
 /* Autotuner: after every instance has its state and before the first run, time
  * `cycles` cycles (after one warm-up cycle) of the captured cycle graphs for each
  * candidate shape of a coordinate descent over the force block {128, 64, 32}, the
- * node block {256, 128, 512, 64}, the element block {128, 64, 32} and the
- * persistent grid {0, 1, 2}, each from the uploaded state
- * (saved and restored on the device; needs one extra copy of the batch's
- * state), and keep the fastest.  The state afterwards is the uploaded one. */
+ * node block {256, 128, 512, 64}, the element block {128, 64, 32}, the
+ * persistent grid {0, 1, 2} and the fused stage at the chosen element block,
+ * each from the uploaded state (saved and restored on the device; needs one
+ * extra copy of the batch's state), and keep the fastest.  The state afterwards
+ * is the uploaded one.  fierro_batch_run returns FIERRO_ETIMEDOUT if a fused
+ * stage's grid barrier gave up waiting (its wait is bounded). */
 int fierro_batch_autotune(fierro_batch* b, int64_t cycles, fierro_batch_shape* chosen);
 /* The last autotune's candidates in timing order and their ms per cycle. */
 int fierro_batch_tune_log(const fierro_batch* b, fierro_batch_shape* shapes, double* ms_per_cycle, int64_t capacity,

@@ -61,16 +61,19 @@ def test_batch_rejects_mismatched_controls(lib_built):
     assert ei.value.code == sgh.FIERRO_EINVAL
 
 
-@pytest.mark.parametrize("shape", [(32, 64, 32, 0), (64, 512, 64, 2), (128, 256, 128, 1)])
-def test_launch_shape_does_not_change_results(lib_built, shape):
+@pytest.mark.parametrize("mode", ["fma", "exact"])
+@pytest.mark.parametrize("shape", [(32, 64, 32, 0, 0), (64, 512, 64, 2, 0), (128, 256, 128, 1, 0),
+                                   (128, 256, 128, 0, 1), (128, 256, 32, 0, 1)])
+def test_launch_shape_does_not_change_results(lib_built, shape, mode):
     """Every launch shape (threads per block of the three passes, persistent grid
-    or not) gives the default shape's results bit for bit."""
+    or not, the fused stage: one cooperative launch per RK stage with grid
+    barriers) gives the default shape's results bit for bit, in both modes."""
     from fierro_gb300 import sgh
     ps = _problems()
     states = [sgh.setup(p) for p in ps]
     out = {}
-    for sh in ((128, 256, 128, 0), shape):
-        with sgh.Batch(ps, fp_mode=sgh.FP_FMA) as b:
+    for sh in ((128, 256, 128, 0, 0), shape):
+        with sgh.Batch(ps, fp_mode=sgh.FP_FMA if mode == "fma" else sgh.FP_EXACT) as b:
             b.set_shape(*sh)
             assert b.shape() == sh
             for i, st in enumerate(states):
@@ -78,7 +81,7 @@ def test_launch_shape_does_not_change_results(lib_built, shape):
             b.run(30)
             out[sh] = ([sgh.compared_fields(b.get_state(i)) for i in range(len(ps))],
                        [b.time(i) for i in range(len(ps))])
-    ref, got = out[(128, 256, 128, 0)], out[shape]
+    ref, got = out[(128, 256, 128, 0, 0)], out[shape]
     assert ref[1] == got[1]
     for i in range(len(ps)):
         assert_bitwise(got[0][i], ref[0][i], FIELDS, label="instance %d shape %s" % (i, shape))
@@ -101,6 +104,7 @@ def test_autotune_keeps_the_uploaded_state_and_the_results(lib_built):
             b.set_state(i, st)
         chosen, log = b.autotune(cycles=2)
         assert len(log) >= 10 and all(ms > 0 for _, ms in log)
+        assert any(sh[4] == 1 for sh, _ in log)  # the fused stage was timed
         assert chosen == min(log, key=lambda r: r[1])[0] and b.shape() == chosen
         b.run(20)
         for i in range(len(ps)):
@@ -112,5 +116,7 @@ def test_autotune_keeps_the_uploaded_state_and_the_results(lib_built):
     with sgh.Batch(ps[:1]) as b:
         with pytest.raises(sgh.FierroError):
             b.set_shape(48, 256, 128, 0)  # not a power of two
+        with pytest.raises(sgh.FierroError):
+            b.set_shape(128, 256, 128, 0, 2)  # fused_stage is 0 or 1
         with pytest.raises(sgh.FierroError):
             b.autotune(cycles=2)  # no state yet
