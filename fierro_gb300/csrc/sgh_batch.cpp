@@ -9,6 +9,7 @@
 // instance nothing changes: same numbering rules, summation orders and
 // arithmetic as the single-problem handle, so results agree bit for bit.
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -143,10 +144,19 @@ int check_sync(fierro_batch* b) {
 }
 
 // The fused stage's grid: every resident block of the cooperative kernel at the
-// element block size, at most one per element tile.
+// element block size, at most one per element tile.  Failure-detection test hook
+// (host side, like FIERRO_FAIL_ALLOC_AFTER): FIERRO_FUSED_OVERSUBSCRIBE=k > 1
+// launches k times the resident blocks without the cooperative attribute, so the
+// grid barrier cannot complete and every block's bounded wait runs out.
+int fused_oversubscribe() {
+  const char* env = std::getenv("FIERRO_FUSED_OVERSUBSCRIBE");
+  const int k = env ? std::atoi(env) : 0;
+  return k > 1 && k <= 16 ? k : 0;
+}
 int fused_grid(const fierro_batch* b) {
   const long long tiles = b->NE / b->shape.elem_block;
   const long long resident = (long long)b->sm_count * b->ks->fused_max_blocks(b->shape.elem_block);
+  if (const int k = fused_oversubscribe()) return (int)std::max<long long>(1, resident * k);
   return (int)std::max<long long>(1, std::min(tiles, resident));
 }
 
@@ -268,7 +278,9 @@ void b_cycle(fierro_batch* b, int c) {
       fa.grid = na.grid = ea.grid = 0;
       const StageSync sync{b->d_sync, b->d_sync + 1, b->d_sync + 2};
       cudaError_t err = cudaMemsetAsync(b->d_sync, 0, sizeof(unsigned int), b->stream);
-      if (err == cudaSuccess) err = b->ks->stage_fused(fa, na, ea, (s == S - 1) ? 1 : 0, sync, fused_grid(b), b->stream);
+      if (err == cudaSuccess)
+        err = b->ks->stage_fused(fa, na, ea, (s == S - 1) ? 1 : 0, sync, fused_grid(b), fused_oversubscribe() ? 0 : 1,
+                                 b->stream);
       if (err != cudaSuccess && b->capture_err == cudaSuccess) b->capture_err = err;
       continue;
     }

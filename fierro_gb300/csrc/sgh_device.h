@@ -207,9 +207,10 @@ struct KernelSet {
                      unsigned long long* out, cudaStream_t);
   // a batch's RK stage as one cooperative launch: the force, node and element
   // passes over `grid` resident blocks of ea.block threads with grid barriers
-  // between them (kind as for elem); and that kernel's resident blocks per SM
+  // between them (kind as for elem; cooperative 0 only for the timeout test);
+  // and that kernel's resident blocks per SM
   cudaError_t (*stage_fused)(const ForceArgs& fa, const NodeArgs& na, const ElemArgs& ea, int kind,
-                             const StageSync& sync, int grid, cudaStream_t);
+                             const StageSync& sync, int grid, int cooperative, cudaStream_t);
   int (*fused_max_blocks)(int block);
 };
 

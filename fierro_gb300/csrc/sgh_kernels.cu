@@ -901,7 +901,7 @@ static void launch_root_check(int which, long long n, unsigned long long seed, i
   k_root_check<<<(unsigned)blocks, 256, 0, s>>>(which, n, seed, lo_exp, hi_exp, out);
 }
 static cudaError_t launch_stage_fused(const ForceArgs& fa, const NodeArgs& na, const ElemArgs& ea, int kind,
-                                      const StageSync& sync, int grid, cudaStream_t s) {
+                                      const StageSync& sync, int grid, int cooperative, cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3((unsigned)block_or(ea.block, kElemBlock));
@@ -911,7 +911,7 @@ static cudaError_t launch_stage_fused(const ForceArgs& fa, const NodeArgs& na, c
   attr[0].id = cudaLaunchAttributeCooperative;
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = cooperative ? 1 : 0;
   return kind == 1 ? cudaLaunchKernelEx(&cfg, k_stage_fused<1>, fa, na, ea, sync)
                    : cudaLaunchKernelEx(&cfg, k_stage_fused<0>, fa, na, ea, sync);
 }

@@ -120,3 +120,32 @@ def test_autotune_keeps_the_uploaded_state_and_the_results(lib_built):
             b.set_shape(128, 256, 128, 0, 2)  # fused_stage is 0 or 1
         with pytest.raises(sgh.FierroError):
             b.autotune(cycles=2)  # no state yet
+
+
+def test_fused_stage_barrier_wait_is_bounded(lib_built, monkeypatch):
+    """The fused stage's grid barrier waits a bounded time.  Launched with four
+    times the blocks that can be resident and without the cooperative attribute
+    (FIERRO_FUSED_OVERSUBSCRIBE, a host-side test hook), the barrier cannot
+    complete: every block's wait runs out, the launch ends, and
+    fierro_batch_run returns FIERRO_ETIMEDOUT.  A batch made without the hook
+    then runs the fused stage normally."""
+    import time
+    from fierro_gb300 import sgh
+    ps = _problems()[:2]
+    states = [sgh.setup(p) for p in ps]
+    monkeypatch.setenv("FIERRO_FUSED_OVERSUBSCRIBE", "4")
+    with sgh.Batch(ps) as b:
+        b.set_shape(128, 256, 128, 0, 1)
+        for i, st in enumerate(states):
+            b.set_state(i, st)
+        t0 = time.perf_counter()
+        with pytest.raises(sgh.FierroError) as ei:
+            b.run(1)
+        assert ei.value.code == sgh.FIERRO_ETIMEDOUT
+        assert time.perf_counter() - t0 < 120.0
+    monkeypatch.delenv("FIERRO_FUSED_OVERSUBSCRIBE")
+    with sgh.Batch(ps) as b:
+        b.set_shape(128, 256, 128, 0, 1)
+        for i, st in enumerate(states):
+            b.set_state(i, st)
+        b.run(3)
