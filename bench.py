@@ -222,8 +222,8 @@ def alg_bytes(kind: str, nn: int, ne: int, nnz: int) -> float:
 # stream their arrays once, so the traffic grows with the elements); the memory
 # traffic is the same in both modes.  k_elem is the mean of its first-stage and
 # last-stage (CFL) launches.
-DRAM_PER_ELEM = {"k_force": (848042752 + 371475456) / 2097152,
-                 "k_elem": (716690688 + 467264768 + 717134848 + 465028608) / 2 / 2097152}
+DRAM_PER_ELEM = {"k_force": (847900928 + 373555200) / 2097152,
+                 "k_elem": (716255232 + 464538624 + 717109760 + 462138624) / 2 / 2097152}
 NCU_PER_ELEM = {"exact": {
     "k_force": {"fp64_ops": 124518424 / 262144, "dram_bytes": DRAM_PER_ELEM["k_force"]},
     "k_elem": {"fp64_ops": (157286400 + 169936928) / 2 / 262144, "dram_bytes": DRAM_PER_ELEM["k_elem"]},
