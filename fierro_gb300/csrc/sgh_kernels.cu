@@ -35,7 +35,9 @@
 //                           (sgh_solve.cpp:590-632)
 // rk_init's copies (time_integration.cpp:9-44) are replaced by swapping the roles
 // of two state bins.  Nothing is accumulated with atomics: every output has one
-// writer and every reduction has a fixed order.
+// writer and every reduction has a fixed order.  A batch may instead run each
+// RK stage as one cooperative launch of k_stage_fused (the three passes with
+// grid barriers between them).
 #include <algorithm>
 #include <cstdint>
 
